@@ -1,0 +1,164 @@
+/*
+ * topomax_gb300 -- C ABI of the GB300 (sm_103a) elasticity design loop.
+ *
+ * One context holds one structured design problem on one GPU: the CG1 design
+ * space on the (nx+1) x (ny+1) vertex lattice, the vector-P2 displacement
+ * space on the (2nx+1) x (2ny+1) node lattice, the Helmholtz filter, the
+ * SIMP elasticity operator, the load vector and the clamped nodes.
+ *
+ * Conventions
+ *   - every array argument is a DEVICE pointer owned by the caller, FP64;
+ *   - CG1 vectors: vertex (i,j) at index j*(nx+1)+i;
+ *   - P2 displacement: node (a,b) at index b*(2nx+1)+a, component c at
+ *     2*index+c;
+ *   - calls are stream-ordered on the stream passed in; a call returns after
+ *     its work is enqueued, except where a host decision needs a device value
+ *     (iterative solves and the projection synchronise the stream);
+ *   - return 0 on success, a negative TOPO_ERR_* code otherwise; the message
+ *     of the last failure is available from topo_last_error();
+ *   - a context is not thread-safe: use one host thread and one stream per
+ *     context.
+ *
+ * Each entry point names the reference interface (Emilinya/topomax) it
+ * replaces.
+ */
+#ifndef TOPOMAX_GB300_H
+#define TOPOMAX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* topo_stream_t; /* == cudaStream_t */
+typedef struct topo_ctx topo_ctx;
+
+#define TOPO_OK 0
+#define TOPO_ERR_ARG (-1)           /* invalid argument / size */
+#define TOPO_ERR_NOT_CONVERGED (-2) /* iterative solve hit its iteration cap */
+#define TOPO_ERR_TIMEOUT (-3)       /* bounded device wait gave up */
+#define TOPO_ERR_NAN (-4)           /* non-finite value met */
+#define TOPO_ERR_CUDA (-5)          /* CUDA runtime error */
+#define TOPO_ERR_STATE (-6)         /* call order violated (e.g. no penalisation set) */
+#define TOPO_ERR_PROJECTION (-7)    /* volume projection failed to bracket/converge */
+
+/* sides, FEM_src/domains.py:18-38 / designs/definitions.py:22-46 */
+#define TOPO_SIDE_LEFT 1
+#define TOPO_SIDE_RIGHT 2
+#define TOPO_SIDE_TOP 4
+#define TOPO_SIDE_BOTTOM 8
+
+/* arithmetic of the iterative solves */
+#define TOPO_PREC_FP64 0  /* FP64 multigrid-preconditioned CG */
+#define TOPO_PREC_MIXED 1 /* FP32 multigrid-preconditioned CG inside FP64 iterative refinement */
+
+/* flags of the solve calls */
+#define TOPO_SOLVE_WARM 1 /* use the output array's contents as the initial guess */
+
+typedef struct {
+  double width, height; /* domain [0,width] x [0,height] */
+  int nx, ny;           /* squares along x and y (each split in two triangles) */
+} topo_grid_desc;
+
+typedef struct {
+  double young_modulus, poisson_ratio; /* designs/definitions.py:169-200 */
+  double filter_radius;                /* Helmholtz filter epsilon */
+  double penal_min;                    /* SIMP minimum m (src/penalizers.py:34: 1e-6) */
+} topo_material;
+
+typedef struct {
+  int fixed_sides;          /* OR of TOPO_SIDE_*: zero displacement on whole sides */
+  int n_fixed_points;       /* extension: clamped mesh vertices */
+  const double* fixed_points; /* host array of (x, y) pairs, snapped to the nearest vertex */
+} topo_bc_desc;
+
+typedef struct {
+  int side; /* TOPO_SIDE_* */
+  double center, length, value_x, value_y;
+} topo_traction;
+
+typedef struct {
+  int has_body_force; /* circular body force, FEM_src/elasisity_problem.py:20-36 */
+  double center_x, center_y, radius, value_x, value_y;
+  int n_tractions;                /* FEM_src/elasisity_problem.py:39-73 */
+  const topo_traction* tractions; /* host array */
+} topo_load_desc;
+
+/* Problem set-up: mesh (FEM_src/solver.py:38-49), spaces (FEM_src/elasisity_problem.py:194-196),
+ * clamped sides (FEM_src/elasisity_problem.py:171-192), the pre-assembled load vector
+ * (FEM_src/pde_solver.py:102-104) and the filter operator (FEM_src/filter.py:15-38).
+ * Replaces ElasticityProblem.__init__ (FEM_src/elasisity_problem.py:79-102). */
+topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, const topo_bc_desc* bc,
+                      const topo_load_desc* load, int precision, int* status);
+
+/* Filter-only context: replaces HelmholtzFilter.__init__ (FEM_src/filter.py:15-38). */
+topo_ctx* topo_create_filter(const topo_grid_desc* grid, double epsilon, int precision, int* status);
+
+void topo_destroy(topo_ctx* ctx);
+
+/* Message of the last failed call on this context ("" if none). */
+const char* topo_last_error(const topo_ctx* ctx);
+
+/* Sizes: CG1 vertices and P2 displacement dofs. */
+int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs);
+
+/* Replaces Problem.set_penalization (src/problem.py:13, src/penalizers.py:14-20). */
+int topo_set_penalization(topo_ctx* ctx, double p);
+
+/* xi = A_f^-1 M1 f for a CG1 field f: replaces HelmholtzFilter.apply
+ * (FEM_src/filter.py:40-41).  iters receives the inner CG iterations (may be NULL). */
+int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, int* iters,
+                      topo_stream_t stream);
+
+/* xi = A_f^-1 b for an assembled CG1 right-hand side b (the filter of a UFL expression,
+ * FEM_src/pde_solver.py:121-131 with l_arg an expression). */
+int topo_filter_solve(topo_ctx* ctx, const double* b, double* xi, double rtol, int* iters,
+                      topo_stream_t stream);
+
+/* u = K(xi)^-1 f: replaces ElasticityProblem.forward / SmartMumpsSolver.solve
+ * (FEM_src/elasisity_problem.py:168-169, FEM_src/pde_solver.py:106-133).
+ * flags: TOPO_SOLVE_WARM uses u as the initial guess. */
+int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, int flags, int* iters,
+                     topo_stream_t stream);
+
+/* *compliance = int u.f dx + int u.t ds  (FEM_src/elasisity_problem.py:161-166). */
+int topo_compliance(topo_ctx* ctx, const double* u, double* compliance, topo_stream_t stream);
+
+/* b_i = int -r'(xi)(lambda div(u)^2 + 2 mu eps(u):eps(u)) phi_i dx: the right-hand side that
+ * ElasticityProblem.calculate_objective_gradient filters (FEM_src/elasisity_problem.py:134-150). */
+int topo_sensitivity_rhs(topo_ctx* ctx, const double* u, const double* xi, double* b,
+                         topo_stream_t stream);
+
+/* g = A_f^-1 b_s: replaces ElasticityProblem.calculate_objective_gradient
+ * (FEM_src/elasisity_problem.py:134-150). */
+int topo_sensitivity(topo_ctx* ctx, const double* u, const double* xi, double* g, double rtol,
+                     int* iters, topo_stream_t stream);
+
+/* psi = project(psi_prev - alpha g, volume): replaces Solver.step / Solver.project
+ * (src/solver.py:149-194; Newton from c=0 with tol 1e-12, bracketing fallback as
+ * src/utils.py:138-157).  *c receives the multiplier (host pointer, may be NULL). */
+int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double alpha, double volume,
+                  double* psi, double* c, topo_stream_t stream);
+
+/* rho = expit(psi) and *delta = sqrt(int (rho - expit(psi_prev))^2): the design update and
+ * convergence measure of Solver.solve (src/solver.py:262, 284-286).  psi_prev may be NULL
+ * (then *delta is not written); delta is a host pointer. */
+int topo_emd_finish(topo_ctx* ctx, const double* psi, const double* psi_prev, double* rho,
+                    double* delta, topo_stream_t stream);
+
+/* *out = int f dx for a CG1 field: replaces FEMSolver.integrate (FEM_src/solver.py:81-84). */
+int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t stream);
+
+/* y = K(xi) u in FP64 with clamped rows/columns as identity (test hook: the operator of
+ * FEM_src/elasisity_problem.py:104-132 after bc.apply). */
+int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y, topo_stream_t stream);
+
+/* Copy of the pre-assembled load vector (2*n_p2 entries, clamped dofs zero). */
+int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TOPOMAX_GB300_H */

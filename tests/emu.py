@@ -1,0 +1,142 @@
+"""ctypes wrappers around the CPU emulator of the kernel phases (tests only)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from tests.native.build_emulator import load
+
+_E = None
+C_D = ctypes.c_double
+C_I = ctypes.c_int
+P_D = ctypes.POINTER(ctypes.c_double)
+P_I = ctypes.POINTER(ctypes.c_int)
+
+SIDE = {"Left": 1, "Right": 2, "Top": 4, "Bottom": 8}
+
+
+def lib():
+    global _E
+    if _E is None:
+        E = load()
+        E.emu_dir_ints.restype = C_I
+        E.emu_p2_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, C_D, C_D, P_I, P_D, P_D, P_D, C_I]
+        E.emu_p1_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, P_I, P_D, P_D, C_D, C_D, P_D, P_D, C_I]
+        E.emu_transfer.argtypes = [C_I, C_I, C_I, P_I, C_I, C_I, P_I, P_D, P_D, C_I]
+        E.emu_kappa.argtypes = [C_I, C_I, C_D, C_D, P_D, P_D]
+        E.emu_coarsen_kappa.argtypes = [P_D, C_I, C_I, P_D, C_I, C_I]
+        E.emu_build_levels.argtypes = [C_I, C_I, C_I, C_D, C_D, P_I, C_I, C_I, P_I]
+        E.emu_sensitivity.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, C_D, C_D, P_D, P_D, P_D]
+        E.emu_make_dir.argtypes = [C_I, C_I, C_D, C_D, C_I, C_I, P_D, P_I]
+        E.emu_load.argtypes = [C_I, C_I, C_D, C_D, P_I, C_I, C_D, C_D, C_D, C_D, C_D, C_I, P_D, P_D]
+        E.emu_vertex_weights.argtypes = [C_I, C_I, C_D, C_D, P_D]
+        _E = E
+    return _E
+
+
+def dp(a):
+    return None if a is None else a.ctypes.data_as(P_D)
+
+
+def ip(a):
+    return a.ctypes.data_as(P_I)
+
+
+def dir_ints():
+    return lib().emu_dir_ints()
+
+
+def no_dir(NX, NY):
+    d = np.zeros(dir_ints(), np.int32)
+    d[2] = NX
+    d[3] = NY
+    return d
+
+
+def make_dir(nx, ny, hx, hy, sides=(), points=()):
+    mask = 0
+    for s in sides:
+        mask |= SIDE[s]
+    pts = np.array(points, dtype=np.float64).reshape(-1)
+    out = np.zeros(dir_ints(), np.int32)
+    rc = lib().emu_make_dir(nx, ny, hx, hy, mask, len(points), dp(pts) if len(points) else None, ip(out))
+    assert rc == 0
+    return out
+
+
+def p2_apply(nx, ny, hx, hy, lam, mu, p, dirv, xi, u, prec=0, mode=0, pmin=1e-6):
+    y = np.zeros(2 * (2 * nx + 1) * (2 * ny + 1))
+    xi = np.ascontiguousarray(xi, dtype=np.float64)
+    uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    lib().emu_p2_apply(prec, nx, ny, hx, hy, lam, mu, p, pmin, ip(dirv), dp(xi), dp(uu), dp(y), mode)
+    return y
+
+
+def p1_apply(NC, nx, ny, hx, hy, lam, mu, dirv, kK, kM, u, kKc=0.0, kMc=0.0, diag=False):
+    y = np.zeros(NC * (nx + 1) * (ny + 1))
+    u = np.ascontiguousarray(u, dtype=np.float64) if u is not None else None
+    lib().emu_p1_apply(NC, nx, ny, hx, hy, lam, mu, ip(dirv), dp(kK), dp(kM), kKc, kMc, dp(u), dp(y), int(diag))
+    return y
+
+
+def restrict(NC, NXf, NYf, dirf, NXc, NYc, dirc, rf):
+    out = np.zeros(NC * NXc * NYc)
+    lib().emu_transfer(NC, NXf, NYf, ip(dirf), NXc, NYc, ip(dirc), dp(np.ascontiguousarray(rf)), dp(out), 0)
+    return out
+
+
+def prolong(NC, NXf, NYf, dirf, NXc, NYc, dirc, xc):
+    out = np.zeros(NC * NXf * NYf)
+    lib().emu_transfer(NC, NXf, NYf, ip(dirf), NXc, NYc, ip(dirc), dp(np.ascontiguousarray(xc)), dp(out), 1)
+    return out
+
+
+def kappa(nx, ny, p, xi, pmin=1e-6):
+    k = np.zeros(2 * nx * ny)
+    lib().emu_kappa(nx, ny, p, pmin, dp(np.ascontiguousarray(xi)), dp(k))
+    return k
+
+
+def coarsen_kappa(kf, nxf, nyf, nxc, nyc):
+    kc = np.zeros(2 * nxc * nyc)
+    lib().emu_coarsen_kappa(dp(np.ascontiguousarray(kf)), nxf, nyf, dp(kc), nxc, nyc)
+    return kc
+
+
+def build_levels(p2_top, nx, ny, hx, hy, dirv, NC, max_levels=64):
+    w = 6 + dir_ints()
+    out = np.zeros(max_levels * w, np.int32)
+    n = lib().emu_build_levels(int(p2_top), nx, ny, hx, hy, ip(dirv), NC, max_levels, ip(out))
+    levels = []
+    for l in range(n):
+        o = out[l * w:(l + 1) * w]
+        levels.append(dict(p2=bool(o[0]), nx=int(o[1]), ny=int(o[2]), NX=int(o[3]), NY=int(o[4]),
+                           NC=int(o[5]), dir=o[6:].copy()))
+    return levels
+
+
+def sensitivity(nx, ny, hx, hy, lam, mu, p, u, xi, prec=0, pmin=1e-6):
+    b = np.zeros((nx + 1) * (ny + 1))
+    lib().emu_sensitivity(prec, nx, ny, hx, hy, lam, mu, p, pmin, dp(np.ascontiguousarray(u)),
+                          dp(np.ascontiguousarray(xi)), dp(b))
+    return b
+
+
+def load_vector(nx, ny, W, H, dirv, body_force=None, tractions=()):
+    b = np.zeros(2 * (2 * nx + 1) * (2 * ny + 1))
+    tr = np.array([[SIDE[t["side"]], t["center"], t["length"], t["value"][0], t["value"][1]]
+                   for t in tractions], dtype=np.float64).reshape(-1)
+    if body_force is None:
+        bf = (0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    else:
+        bf = (1, body_force["region"]["center"][0], body_force["region"]["center"][1],
+              body_force["region"]["radius"], body_force["value"][0], body_force["value"][1])
+    lib().emu_load(nx, ny, W, H, ip(dirv), *bf, len(tractions), dp(tr) if len(tractions) else None, dp(b))
+    return b
+
+
+def vertex_weights(nx, ny, hx, hy):
+    w = np.zeros((nx + 1) * (ny + 1))
+    lib().emu_vertex_weights(nx, ny, hx, hy, dp(w))
+    return w

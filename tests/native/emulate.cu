@@ -1,0 +1,270 @@
+// CPU emulation of the topomax_gb300 kernels, for the CPU test suite only.
+//
+// The device kernels are written as load / compute / gather phase functions
+// (topo_p2.cuh, topo_p1.cuh) that are __host__ __device__.  This file runs
+// those phases sequentially per tile on the host -- every thread of phase k
+// before any thread of phase k+1, which is exactly the ordering the kernels'
+// __syncthreads give -- so the tiling and index logic can be compared with
+// the FP64 oracle without a GPU.  It is never linked into the product library.
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "topo_mg.h"
+#include "topo_p1.cuh"
+#include "topo_p2.cuh"
+#include "topo_setup.h"
+
+using namespace topo;
+
+namespace {
+constexpr int kDirInts = 5 + 2 * kMaxDirPoints;
+
+Dir dir_from(const int* d) {
+  Dir r;
+  std::memset(&r, 0, sizeof(r));
+  r.x_lo = d[0];
+  r.y_lo = d[1];
+  r.x_hi_from = d[2];
+  r.y_hi_from = d[3];
+  r.npts = d[4];
+  for (int k = 0; k < 2 * kMaxDirPoints; ++k) r.pts[k] = d[5 + k];
+  return r;
+}
+
+void dir_to(const Dir& r, int* d) {
+  d[0] = r.x_lo;
+  d[1] = r.y_lo;
+  d[2] = r.x_hi_from;
+  d[3] = r.y_hi_from;
+  d[4] = r.npts;
+  for (int k = 0; k < 2 * kMaxDirPoints; ++k) d[5 + k] = r.pts[k];
+}
+
+template <class T>
+void p2_run(const P2Params<T>& P, const T* xi, const T* u, T* y, int mode) {
+  auto s = std::make_unique<P2Smem<T>>();
+  const int gx = (P.nx + P2_TX - 1) / P2_TX, gy = (P.ny + P2_TY - 1) / P2_TY;
+  for (int by = 0; by < gy; ++by)
+    for (int bx = 0; bx < gx; ++bx) {
+      std::memset(s.get(), 0xff, sizeof(P2Smem<T>));  // poison: unwritten smem shows up as NaN
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::load(t, P2_THREADS, bx, by, P, mode == 1 ? nullptr : u, xi, *s);
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::compute(t, P2_THREADS, bx, by, P, *s, mode);
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::gather(t, P2_THREADS, bx, by, P, *s, u, y, mode);
+    }
+}
+
+template <class T>
+P2Params<T> p2params(int nx, int ny, double hx, double hy, double lam, double mu, double p, double pmin,
+                     const int* dir) {
+  P2Params<T> P;
+  std::memset(&P, 0, sizeof(P));
+  P.nx = nx;
+  P.ny = ny;
+  P.ihx = T(1.0 / hx);
+  P.ihy = T(1.0 / hy);
+  const double area = 0.5 * hx * hy;
+  P.lamT = T(lam * area);
+  P.mu2T = T(2.0 * mu * area);
+  P.pen = make_penal<T>(p, pmin);
+  P.dir = dir_from(dir);
+  return P;
+}
+}  // namespace
+
+extern "C" {
+
+int emu_dir_ints() { return kDirInts; }
+
+// y = K(xi) u (mode 0) or diag K(xi) (mode 1); prec 0 = FP64, 1 = FP32
+int emu_p2_apply(int prec, int nx, int ny, double hx, double hy, double lam, double mu, double p, double pmin,
+                 const int* dir, const double* xi, const double* u, double* y, int mode) {
+  const size_t nv = size_t(nx + 1) * (ny + 1), nd = size_t(2) * (2 * nx + 1) * (2 * ny + 1);
+  if (prec == 0) {
+    auto P = p2params<double>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
+    p2_run<double>(P, xi, u, y, mode);
+  } else {
+    auto P = p2params<float>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
+    std::vector<float> xf(xi, xi + nv), uf(nd, 0.f), yf(nd, 0.f);
+    if (u) for (size_t i = 0; i < nd; ++i) uf[i] = float(u[i]);
+    p2_run<float>(P, xf.data(), uf.data(), yf.data(), mode);
+    for (size_t i = 0; i < nd; ++i) y[i] = yf[i];
+  }
+  return 0;
+}
+
+int emu_p1_apply(int NC, int nx, int ny, double hx, double hy, double lam, double mu, const int* dir,
+                 const double* kK, const double* kM, double kKc, double kMc, const double* u, double* y, int diag) {
+  const ElemRefs R = make_elem_refs(hx, hy, lam, mu);
+  const int NX = nx + 1, NY = ny + 1;
+  auto fill = [&](auto& P) {
+    P.nx = nx;
+    P.ny = ny;
+    P.dir = dir_from(dir);
+    for (int o = 0; o < 2; ++o) {
+      for (int a = 0; a < 3 * NC; ++a)
+        for (int b = 0; b < 3 * NC; ++b) P.K[o][a][b] = NC == 2 ? R.K2[o][a][b] : R.K1[o][a][b];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) P.Mm[o][a][b] = R.M1[o][a][b];
+    }
+    P.kK = kK;
+    P.kM = kM;
+    P.kK_c = kKc;
+    P.kM_c = kMc;
+  };
+  if (NC == 2) {
+    P1Params<double, 2> P;
+    std::memset(&P, 0, sizeof(P));
+    fill(P);
+    for (int b = 0; b < NY; ++b)
+      for (int a = 0; a < NX; ++a)
+        diag ? P1Kern<double, 2>::node_diag(a, b, P, y) : P1Kern<double, 2>::node_apply(a, b, P, u, y);
+  } else {
+    P1Params<double, 1> P;
+    std::memset(&P, 0, sizeof(P));
+    fill(P);
+    for (int b = 0; b < NY; ++b)
+      for (int a = 0; a < NX; ++a)
+        diag ? P1Kern<double, 1>::node_diag(a, b, P, y) : P1Kern<double, 1>::node_apply(a, b, P, u, y);
+  }
+  return 0;
+}
+
+int emu_transfer(int NC, int NXf, int NYf, const int* dirf, int NXc, int NYc, const int* dirc, const double* in,
+                 double* out, int prolong) {
+  Transfer X;
+  X.NXf = NXf;
+  X.NYf = NYf;
+  X.NXc = NXc;
+  X.NYc = NYc;
+  X.dirf = dir_from(dirf);
+  X.dirc = dir_from(dirc);
+  if (prolong) {
+    for (int b = 0; b < NYf; ++b)
+      for (int a = 0; a < NXf; ++a)
+        NC == 2 ? TransferKern<double, 2>::node_prolong_add(a, b, X, in, out)
+                : TransferKern<double, 1>::node_prolong_add(a, b, X, in, out);
+  } else {
+    for (int J = 0; J < NYc; ++J)
+      for (int I = 0; I < NXc; ++I)
+        NC == 2 ? TransferKern<double, 2>::node_restrict(I, J, X, in, out)
+                : TransferKern<double, 1>::node_restrict(I, J, X, in, out);
+  }
+  return 0;
+}
+
+int emu_kappa(int nx, int ny, double p, double pmin, const double* xi, double* kK) {
+  const Penal<double> pen = make_penal<double>(p, pmin);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i)
+      for (int o = 0; o < 2; ++o) {
+        double xe[3];
+        for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * (nx + 1) + i + p1_off_a(o, k)];
+        kK[(size_t(j) * nx + i) * 2 + o] = tri_kappa(xe, pen);
+      }
+  return 0;
+}
+
+int emu_coarsen_kappa(const double* kf, int nxf, int nyf, double* kc, int nxc, int nyc) {
+  for (int J = 0; J < nyc; ++J)
+    for (int I = 0; I < nxc; ++I)
+      for (int o = 0; o < 2; ++o) kc[(size_t(J) * nxc + I) * 2 + o] = coarsen_kappa(kf, nxf, nyf, I, J, o);
+  return 0;
+}
+
+// per level: p2, nx, ny, NX, NY, NC, dir[kDirInts]
+int emu_build_levels(int p2_top, int nx, int ny, double hx, double hy, const int* dir_top, int NC, int max_levels,
+                     int* out) {
+  const auto v = build_levels(p2_top != 0, nx, ny, hx, hy, dir_from(dir_top), NC);
+  const int n = int(v.size());
+  for (int l = 0; l < n && l < max_levels; ++l) {
+    int* o = out + l * (6 + kDirInts);
+    o[0] = v[l].p2;
+    o[1] = v[l].nx;
+    o[2] = v[l].ny;
+    o[3] = v[l].NX;
+    o[4] = v[l].NY;
+    o[5] = v[l].NC;
+    dir_to(v[l].dir, o + 6);
+  }
+  return n;
+}
+
+int emu_sensitivity(int prec, int nx, int ny, double hx, double hy, double lam, double mu, double p, double pmin,
+                    const double* u, const double* xi, double* b) {
+  const int NX = 2 * nx + 1, VX = nx + 1;
+  const size_t nt = size_t(2) * nx * ny;
+  std::vector<double> tri(3 * nt);
+  const double area = 0.5 * hx * hy;
+  for (size_t t = 0; t < nt; ++t) {
+    const int o = int(t & 1);
+    const size_t cell = t >> 1;
+    const int i = int(cell % nx), j = int(cell / nx);
+    double ue[6][2];
+    for (int k = 0; k < 6; ++k) {
+      const size_t n = size_t(2 * j + p2_off_b(o, k)) * NX + 2 * i + p2_off_a(o, k);
+      ue[k][0] = u[2 * n];
+      ue[k][1] = u[2 * n + 1];
+    }
+    if (prec == 0) {
+      double xe[3], c[3];
+      for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
+      const auto pen = make_penal<double>(p, pmin);
+      if (o == 0) tri_sensitivity<0, double, double>(ue, xe, 1.0 / hx, 1.0 / hy, lam, mu, area, pen, c);
+      else tri_sensitivity<1, double, double>(ue, xe, 1.0 / hx, 1.0 / hy, lam, mu, area, pen, c);
+      for (int k = 0; k < 3; ++k) tri[3 * t + k] = c[k];
+    } else {
+      float xe[3], c[3];
+      for (int k = 0; k < 3; ++k) xe[k] = float(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
+      const auto pen = make_penal<float>(p, pmin);
+      if (o == 0)
+        tri_sensitivity<0, double, float>(ue, xe, 1.0 / hx, 1.0 / hy, float(lam), float(mu), float(area), pen, c);
+      else
+        tri_sensitivity<1, double, float>(ue, xe, 1.0 / hx, 1.0 / hy, float(lam), float(mu), float(area), pen, c);
+      for (int k = 0; k < 3; ++k) tri[3 * t + k] = c[k];
+    }
+  }
+  const size_t nv = size_t(nx + 1) * (ny + 1);
+  for (size_t v = 0; v < nv; ++v) {
+    const int a = int(v % VX), bb = int(v / VX);
+    double s = 0.0;
+    for (int e = 0; e < 6; ++e) {
+      int dci, dcj, o, loc;
+      p1_incidence(e, dci, dcj, o, loc);
+      const int ci = a + dci, cj = bb + dcj;
+      if (ci < 0 || ci >= nx || cj < 0 || cj >= ny) continue;
+      s += tri[3 * ((size_t(cj) * nx + ci) * 2 + o) + loc];
+    }
+    b[v] = s;
+  }
+  return 0;
+}
+
+int emu_make_dir(int nx, int ny, double hx, double hy, int sides, int npts, const double* pts, int* out) {
+  topo_bc_desc bc{sides, npts, pts};
+  Dir d;
+  std::string msg;
+  if (make_p2_dir(nx, ny, hx, hy, &bc, d, msg)) return 1;
+  dir_to(d, out);
+  return 0;
+}
+
+// tr: 5 doubles per traction (side, center, length, vx, vy)
+int emu_load(int nx, int ny, double W, double H, const int* dir, int has_bf, double cx, double cy, double r,
+             double fx, double fy, int ntr, const double* tr, double* b) {
+  std::vector<topo_traction> T(ntr);
+  for (int k = 0; k < ntr; ++k) T[k] = topo_traction{int(tr[5 * k]), tr[5 * k + 1], tr[5 * k + 2], tr[5 * k + 3], tr[5 * k + 4]};
+  topo_load_desc L{has_bf, cx, cy, r, fx, fy, ntr, T.data()};
+  std::vector<double> v;
+  assemble_load(nx, ny, W, H, dir_from(dir), &L, v);
+  std::memcpy(b, v.data(), v.size() * sizeof(double));
+  return 0;
+}
+
+int emu_vertex_weights(int nx, int ny, double hx, double hy, double* w) {
+  const auto v = vertex_weights(nx, ny, hx, hy);
+  std::memcpy(w, v.data(), v.size() * sizeof(double));
+  return 0;
+}
+
+}  // extern "C"

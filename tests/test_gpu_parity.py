@@ -1,0 +1,221 @@
+"""GPU path against the FP64 oracle through the C ABI (needs a CUDA device).
+
+Tolerances: FP64-residual solves run to rtol 1e-12 here, so the displacement
+matches the oracle's direct solve to ~1e-9 relative and the compliance to
+~1e-10; mixed precision (FP32 CG inside FP64 refinement) reaches the same
+refinement target.  The design-loop tests use the parity bar rel <= 1e-6 on
+the compliance history.
+"""
+import numpy as np
+import pytest
+
+from oracle.fem import Design, FEMOracle, Lattice, OracleSolver
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden")
+
+
+def _design(**kw):
+    base = dict(width=2.0, height=1.0, fem_step_size=0.002, penalties=[3.0], volume_fraction=0.5,
+                fixed_sides=["Left"], body_force=None,
+                tractions=[dict(side="Right", center=0.5, length=0.5, value=[0.0, -1.0])],
+                filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)
+    base.update(kw)
+    return Design(**base)
+
+
+def _gpu_problem(d: Design, nx, ny, precision="mixed", rtol=1e-12):
+    import topomax_gb300 as tg
+    from topomax_gb300.designs import parse_design_dict
+    dd = {"Elasticity": {"domain_parameters": dict(width=d.width, height=d.height, fem_step_size=d.fem_step_size,
+                                                   dem_step_size=1.0, penalties=d.penalties,
+                                                   volume_fraction=d.volume_fraction),
+                         "problem_parameters": dict(fixed_sides=d.fixed_sides, body_force=d.body_force,
+                                                    tractions=d.tractions, filter_radius=d.filter_radius,
+                                                    young_modulus=d.young_modulus, poisson_ratio=d.poisson_ratio,
+                                                    fixed_points=d.fixed_points)}}
+    dom, par = parse_design_dict(dd)
+    mesh = tg.RectangleMesh(d.width, d.height, nx, ny)
+    V = tg.FunctionSpace(mesh, "CG", 1)
+    return tg.ElasticityProblem(mesh, V, dom, par, precision=precision, rtol=rtol), V
+
+
+@pytest.mark.parametrize("nx,ny,sides", [(10, 10, ["Bottom"]), (80, 40, ["Left"]), (33, 9, ["Left", "Right", "Top"])])
+def test_operator_and_load_match_oracle(nx, ny, sides):
+    import torch
+    d = _design(fixed_sides=sides)
+    prob, V = _gpu_problem(d, nx, ny)
+    o = FEMOracle(Lattice(d.width, d.height, nx, ny), d)
+    o.set_penalization(3.0)
+    prob.set_penalization(3.0)
+    rng = np.random.default_rng(0)
+    xi = rng.uniform(0.01, 1.0, o.L.n_vertices)
+    u = rng.standard_normal(2 * o.L.n_p2)
+    y = prob.apply_operator(xi, torch.tensor(u, device="cuda")).cpu().numpy()
+    ref = o.apply_state(xi, u)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+    b = prob.load_vector().cpu().numpy()
+    bref = o.load.copy()
+    bref[np.concatenate([2 * o.dirichlet_nodes, 2 * o.dirichlet_nodes + 1])] = 0
+    assert np.max(np.abs(b - bref)) <= 1e-14 * np.max(np.abs(bref))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_filter_matches_oracle(precision):
+    import topomax_gb300 as tg
+    d = _design()
+    nx, ny = 80, 40
+    mesh = tg.RectangleMesh(2.0, 1.0, nx, ny)
+    V = tg.FunctionSpace(mesh, "CG", 1)
+    f = tg.HelmholtzFilter(0.05, V, precision=precision, rtol=1e-12)
+    o = FEMOracle(Lattice(2.0, 1.0, nx, ny), d)
+    rho = np.random.default_rng(1).uniform(0, 1, o.L.n_vertices)
+    xi = f.apply(rho).vector()[:]
+    ref = o.filter_apply(rho)
+    assert np.max(np.abs(xi - ref)) <= 1e-10 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_filter_identity_at_zero_radius(precision):
+    """tests/test_filter.py:25-34: epsilon = 0 leaves rho unchanged."""
+    import topomax_gb300 as tg
+    mesh = tg.RectangleMesh(1.0, 1.0, 10, 10)
+    V = tg.FunctionSpace(mesh, "CG", 1)
+    f = tg.HelmholtzFilter(0.0, V, precision=precision, rtol=1e-14)
+    np.random.seed(198)
+    rho = np.random.random(V.dim())
+    xi = f.apply(rho).vector()[:]
+    assert np.max(np.abs(xi - rho)) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("case", ["cantilever", "triangle"])
+def test_state_compliance_gradient_match_oracle(precision, case):
+    if case == "cantilever":
+        d, nx, ny = _design(), 80, 40
+    else:
+        d = _design(width=1.0, height=1.0, fixed_sides=["Bottom"], tractions=None, filter_radius=0.02,
+                    young_modulus=2.5, poisson_ratio=0.25,
+                    body_force=dict(region=dict(center=[0.5, 0.5], radius=0.05), value=[0.0, -10.0]))
+        nx, ny = 40, 40
+    prob, V = _gpu_problem(d, nx, ny, precision=precision, rtol=1e-12)
+    o = FEMOracle(Lattice(d.width, d.height, nx, ny), d)
+    prob.set_penalization(3.0)
+    o.set_penalization(3.0)
+    rho = np.random.default_rng(2).uniform(0.01, 1.0, o.L.n_vertices)
+    C = prob.calculate_objective(rho)
+    xi_ref = o.filter_apply(rho)
+    u_ref = o.state_solve(xi_ref)
+    C_ref = o.compliance(u_ref)
+    assert abs(C - C_ref) <= 1e-9 * abs(C_ref)
+    u = prob.u.vector()[:]
+    assert np.max(np.abs(u - u_ref)) <= 1e-8 * np.max(np.abs(u_ref))
+    g = prob.calculate_objective_gradient().vector()[:]
+    g_ref = o.gradient(u_ref, xi_ref)
+    tol = 1e-9 if precision == "fp64" else 2e-6
+    assert np.max(np.abs(g - g_ref)) <= tol * np.max(np.abs(g_ref))
+
+
+def test_projection_matches_oracle():
+    import topomax_gb300 as tg
+    d = _design()
+    solver_o = OracleSolver(40, d)
+    rng = np.random.default_rng(4)
+    half = rng.normal(0.0, 3.0, solver_o.lattice.n_vertices)
+    ref = solver_o.project(half, solver_o.volume)
+    from tests.test_gpu_parity import _write_design
+    path = _write_design(d)
+    s = tg.FEMSolver(40, path, verbose=False, save=False)
+    psi = s.project(half, s.volume).cpu().numpy()
+    assert np.max(np.abs(psi - ref)) <= 1e-10
+    assert abs(s.integrate(1.0 / (1.0 + np.exp(-psi))) - s.volume) <= 1e-11
+
+
+def _write_design(d: Design, name="design.json"):
+    import json
+    import tempfile
+    import os
+    dd = {"Elasticity": {"domain_parameters": dict(width=d.width, height=d.height, fem_step_size=d.fem_step_size,
+                                                   dem_step_size=1.0, penalties=d.penalties,
+                                                   volume_fraction=d.volume_fraction),
+                         "problem_parameters": dict(fixed_sides=d.fixed_sides, body_force=d.body_force,
+                                                    tractions=d.tractions, filter_radius=d.filter_radius,
+                                                    young_modulus=d.young_modulus, poisson_ratio=d.poisson_ratio)}}
+    p = os.path.join(tempfile.mkdtemp(), name)
+    with open(p, "w") as f:
+        json.dump(dd, f)
+    return p
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_triangle_known_answer(precision, tmp_path):
+    """tests/test_elasticity_solver.py:30-55: triangle, N=10, objective at k=24."""
+    import json
+    import os
+    import topomax_gb300 as tg
+    gold = json.load(open(os.path.join(GOLDEN, "triangle_N10.json")))
+    s = tg.FEMSolver(10, os.path.join(GOLDEN, "designs", "triangle.json"), data_path=str(tmp_path),
+                     skip_multiple=999, precision=precision, rtol=1e-12, verbose=False)
+    hist = s.solve()[3.0]
+    assert hist["exit_condition"] == "Convergence treshold reached"
+    assert hist["iterations"] == gold["iteration"]
+    obj = hist["objectives"][-1]
+    assert abs(obj - gold["objective"]) <= 1e-6 * abs(gold["objective"])
+    rho = np.sort(s.to_array(s.rho))
+    assert np.max(np.abs(rho - np.array(gold["rho_sorted"]))) <= 1e-5
+    assert os.path.isfile(os.path.join(tmp_path, "FEM", "triangle", "data", "N=10_p=3.0_k=24.dat"))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_cantilever_design_loop_parity(precision):
+    """80x40 cantilever, 20 EMD iterations: compliance history rel <= 1e-6 vs the oracle."""
+    import topomax_gb300 as tg
+    d = _design()
+    so = OracleSolver(40, d, max_iterations=20)
+    ref = so.solve()[0]
+    path = _write_design(d)
+    s = tg.FEMSolver(40, path, precision=precision, rtol=1e-10, verbose=False, save=False, max_iterations=20)
+    hist = s.solve()[3.0]
+    objs = np.array(hist["objectives"])
+    robjs = np.array(ref.objectives)
+    assert len(objs) == len(robjs)
+    assert np.max(np.abs(objs - robjs) / np.abs(robjs)) <= 1e-6
+    assert np.max(np.abs(s.to_array(s.rho) - ref.rho)) <= 1e-5
+
+
+def test_call_order_errors():
+    import topomax_gb300 as tg
+    d = _design()
+    prob, V = _gpu_problem(d, 8, 4)
+    with pytest.raises(ValueError):
+        prob.calculate_objective(np.full(V.dim(), 0.5))        # no penalisation set
+    prob.set_penalization(3.0)
+    with pytest.raises(ValueError):
+        prob.calculate_objective_gradient()                    # before calculate_objective
+    assert np.isnan(prob.calculate_objective(np.full(V.dim(), np.nan)))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_large_grid_properties(precision):
+    """1000x500 (4,006,002 dofs): residual, symmetry and energy identities."""
+    import torch
+    d = _design()
+    prob, V = _gpu_problem(d, 1000, 500, precision=precision, rtol=1e-8)
+    prob.set_penalization(3.0)
+    g = torch.Generator().manual_seed(0)
+    rho = torch.rand(V.dim(), generator=g, dtype=torch.float64) * 0.99 + 0.01
+    C = prob.calculate_objective(rho.numpy())
+    u = prob.u.tensor
+    xi = prob.filtered_rho.tensor
+    b = prob.load_vector()
+    r = b - prob.apply_operator(xi, u)
+    assert (r.norm() / b.norm()).item() <= 1e-8
+    assert abs(C - torch.dot(b, u).item()) <= 1e-12 * abs(C)
+    Ku = prob.apply_operator(xi, u)
+    assert abs(torch.dot(u, Ku).item() - C) <= 1e-7 * abs(C)
+    v = torch.randn(u.numel(), generator=g, dtype=torch.float64).cuda()
+    lhs = torch.dot(v, Ku).item()
+    rhs = torch.dot(u, prob.apply_operator(xi, v)).item()
+    assert abs(lhs - rhs) <= 1e-10 * (abs(lhs) + 1e-300) + 1e-12
+    assert prob.filtered_rho.tensor.min().item() > 0.0

@@ -1,0 +1,216 @@
+"""Kernel phase logic (run on the CPU through the emulator) against the FP64 oracle.
+
+The GPU kernels are load / compute / gather phases shared with the host; here
+they run tile by tile on the CPU so the tiling, halo and index logic is
+checked bit-for-bit-close against the oracle's assembled operators before any
+GPU run.  The same comparisons run on the GPU in ``test_gpu_parity.py``.
+"""
+import numpy as np
+import pytest
+
+from oracle.fem import Design, FEMOracle, Lattice, lame
+from tests import emu
+
+
+def make_design(**kw):
+    base = dict(width=2.0, height=1.0, fem_step_size=0.002, penalties=[3.0], volume_fraction=0.5,
+                fixed_sides=["Left"], body_force=None,
+                tractions=[dict(side="Right", center=0.5, length=0.5, value=[0.0, -1.0])],
+                filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)
+    base.update(kw)
+    return Design(**base)
+
+
+CASES = [
+    # (W, H, nx, ny, sides, p)
+    (1.0, 1.0, 3, 2, ["Left"], 3.0),
+    (1.0, 1.0, 10, 10, ["Bottom"], 3.0),
+    (2.0, 1.0, 33, 9, ["Left", "Right", "Top"], 3.0),      # 2x2 tiles, ragged
+    (2.0, 1.0, 70, 17, [], 3.5),                            # non-integer p, no clamping
+    (3.0, 1.0, 65, 24, ["Bottom", "Right"], 4.0),
+]
+
+
+def _problem(W, H, nx, ny, sides, p, seed=0):
+    d = make_design(width=W, height=H, fixed_sides=sides)
+    L = Lattice(W, H, nx, ny)
+    o = FEMOracle(L, d)
+    o.set_penalization(p)
+    rng = np.random.default_rng(seed)
+    xi = rng.uniform(0.01, 1.0, L.n_vertices)
+    u = rng.standard_normal(2 * L.n_p2)
+    dirv = emu.make_dir(nx, ny, L.hx, L.hy, sides)
+    return d, L, o, xi, u, dirv
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_p2_apply_fp64_matches_oracle(case):
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    y = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u)
+    ref = o.apply_state(xi, u)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", CASES[:3])
+def test_p2_apply_fp32_matches_oracle(case):
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    y = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=1)
+    ref = o.apply_state(xi, u)
+    assert np.max(np.abs(y - ref)) <= 2e-5 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_p2_diag_matches_oracle(case):
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    dg = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, None, mode=1)
+    K = o.stiffness(xi)
+    ref = K.diagonal().copy()
+    dd = np.concatenate([2 * o.dirichlet_nodes, 2 * o.dirichlet_nodes + 1])
+    ref[dd] = 1.0
+    assert np.max(np.abs(dg - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_load_vector_matches_oracle():
+    designs = [
+        make_design(),   # cantilever, traction on the right side
+        make_design(width=1.0, height=1.0, fixed_sides=["Bottom"], tractions=None,
+                    body_force=dict(region=dict(center=[0.5, 0.5], radius=0.05), value=[0.0, -10.0])),
+        make_design(width=3.0, height=1.0, tractions=[
+            dict(side="Top", center=1.5, length=1.0, value=[1.0, -2.0]),
+            dict(side="Bottom", center=2.95, length=0.1, value=[0.5, 0.0]),
+            dict(side="Left", center=0.5, length=1.0, value=[0.0, 3.0])],
+            body_force=dict(region=dict(center=[2.9, 0.5], radius=0.05), value=[0.0, -1.0])),
+    ]
+    for d, (nx, ny) in zip(designs, [(80, 40), (10, 10), (30, 10)]):
+        L = Lattice(d.width, d.height, nx, ny)
+        o = FEMOracle(L, d)
+        dirv = emu.make_dir(nx, ny, L.hx, L.hy, d.fixed_sides)
+        b = emu.load_vector(nx, ny, d.width, d.height, dirv, d.body_force, d.tractions or ())
+        ref = o.load.copy()
+        dd = np.concatenate([2 * o.dirichlet_nodes, 2 * o.dirichlet_nodes + 1])
+        ref[dd] = 0.0
+        assert np.max(np.abs(b - ref)) <= 1e-14 * max(1.0, np.max(np.abs(ref)))
+        tiny = 1e-12 * np.max(np.abs(ref))
+        assert np.count_nonzero(np.abs(b) > tiny) == np.count_nonzero(np.abs(ref) > tiny)
+
+
+def test_vertex_weights_match_oracle():
+    d = make_design()
+    L = Lattice(2.0, 1.0, 12, 7)
+    o = FEMOracle(L, d)
+    w = emu.vertex_weights(12, 7, L.hx, L.hy)
+    assert np.allclose(w, o.vertex_weights, rtol=0, atol=1e-16)
+    assert abs(w.sum() - 2.0) < 1e-13
+
+
+@pytest.mark.parametrize("p", [3.0, 4.0, 3.3])
+def test_sensitivity_rhs_matches_oracle(p):
+    d, L, o, xi, u, dirv = _problem(2.0, 1.0, 20, 9, ["Left"], p, seed=3)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    u = u * 1e-2
+    b = emu.sensitivity(20, 9, L.hx, L.hy, lam, mu, p, u, xi)
+    ref = o.sensitivity_rhs(u, xi)
+    assert np.max(np.abs(b - ref)) <= 1e-12 * np.max(np.abs(ref))
+    b32 = emu.sensitivity(20, 9, L.hx, L.hy, lam, mu, p, u, xi, prec=1)
+    assert np.max(np.abs(b32 - ref)) <= 1e-5 * np.max(np.abs(ref))
+
+
+def test_filter_operator_matches_oracle():
+    d = make_design(filter_radius=0.05)
+    L = Lattice(2.0, 1.0, 40, 20)
+    o = FEMOracle(L, d)
+    x = np.random.default_rng(1).standard_normal(L.n_vertices)
+    dirv = emu.no_dir(41, 21)
+    y = emu.p1_apply(1, 40, 20, L.hx, L.hy, 0.0, 0.0, dirv, None, None, x, kKc=0.05 ** 2, kMc=1.0)
+    ref = o.A_filter @ x
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+    m = emu.p1_apply(1, 40, 20, L.hx, L.hy, 0.0, 0.0, dirv, None, None, x, kKc=0.0, kMc=1.0)
+    assert np.max(np.abs(m - o.M1 @ x)) <= 1e-15
+
+
+def _free_rows(dirv, NX, NY, NC):
+    a, b = np.meshgrid(np.arange(NX), np.arange(NY))
+    a = a.ravel()
+    b = b.ravel()
+    clamped = np.zeros(NX * NY, bool)
+    if dirv[0]:
+        clamped |= a == 0
+    if dirv[1]:
+        clamped |= b == 0
+    clamped |= a >= dirv[2]
+    clamped |= b >= dirv[3]
+    for k in range(dirv[4]):
+        clamped |= (a == dirv[5 + 2 * k]) & (b == dirv[6 + 2 * k])
+    return np.repeat(~clamped, NC)
+
+
+@pytest.mark.parametrize("nx,ny,sides", [(8, 6, ["Left"]), (33, 9, ["Bottom", "Right"]), (12, 12, [])])
+def test_p1_level_is_galerkin_projection_of_p2(nx, ny, sides):
+    """K_P1(kappa) x = P^T K_P2(xi) P x on the free rows (exact Galerkin)."""
+    W, H, p = 2.0, 1.0, 3.0
+    d, L, o, xi, _, dirv = _problem(W, H, nx, ny, sides, p, seed=5)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    lv = emu.build_levels(True, nx, ny, L.hx, L.hy, dirv, 2)
+    f, c = lv[0], lv[1]
+    x1 = np.random.default_rng(7).standard_normal(2 * c["NX"] * c["NY"])
+    x1[~_free_rows(c["dir"], c["NX"], c["NY"], 2)] = 0.0
+    x2 = emu.prolong(2, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], x1)
+    y2 = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, f["dir"], xi, x2)
+    y1 = emu.restrict(2, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], y2)
+    kk = emu.kappa(nx, ny, p, xi)
+    z1 = emu.p1_apply(2, nx, ny, L.hx, L.hy, lam, mu, c["dir"], kk, None, x1)
+    free = _free_rows(c["dir"], c["NX"], c["NY"], 2)
+    assert np.max(np.abs(z1[free] - y1[free])) <= 1e-12 * np.max(np.abs(y1))
+
+
+@pytest.mark.parametrize("NC", [1, 2])
+def test_p1_coarsening_is_galerkin_on_even_grids(NC):
+    nx, ny, hx, hy = 16, 8, 0.125, 0.125
+    rng = np.random.default_rng(11)
+    kf = rng.uniform(1e-3, 1.0, 2 * nx * ny)
+    # the filter's mass coefficient is constant: averaging it is exact Galerkin
+    km = np.ones(2 * nx * ny) if NC == 1 else None
+    dirv = emu.no_dir(nx + 1, ny + 1)
+    if NC == 2:
+        dirv[0] = 1
+    lv = emu.build_levels(False, nx, ny, hx, hy, dirv, NC)
+    f, c = lv[0], lv[1]
+    assert (c["nx"], c["ny"]) == (8, 4)
+    kc = emu.coarsen_kappa(kf, nx, ny, 8, 4)
+    kmc = emu.coarsen_kappa(km, nx, ny, 8, 4) if km is not None else None
+    lam, mu = 0.5, 0.4
+    xc = rng.standard_normal(NC * c["NX"] * c["NY"])
+    free_c = _free_rows(c["dir"], c["NX"], c["NY"], NC)
+    xc[~free_c] = 0.0
+    xf = emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
+    yf = emu.p1_apply(NC, nx, ny, hx, hy, lam, mu, f["dir"], kf, km, xf)
+    yc = emu.restrict(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], yf)
+    zc = emu.p1_apply(NC, 8, 4, 2 * hx, 2 * hy, lam, mu, c["dir"], kc, kmc, xc)
+    assert np.max(np.abs(zc[free_c] - yc[free_c])) <= 1e-12 * np.max(np.abs(yc))
+
+
+def test_level_chain_shapes():
+    dirv = emu.make_dir(1000, 500, 0.002, 0.002, ["Left"])
+    lv = emu.build_levels(True, 1000, 500, 0.002, 0.002, dirv, 2)
+    dims = [(l["nx"], l["ny"]) for l in lv]
+    assert dims[0] == (1000, 500) and lv[0]["p2"] and not lv[1]["p2"]
+    assert dims[1] == (1000, 500)
+    assert dims[-1] == (4, 2) and 2 * lv[-1]["NX"] * lv[-1]["NY"] <= 64
+    assert all(l["dir"][0] == 1 for l in lv)          # left side stays clamped
+    # odd sizes pad: 125 -> 63
+    assert (125, 63) in dims
+    # a clamped right side on an odd level clamps the last two coarse columns
+    dr = emu.make_dir(10, 10, 0.1, 0.1, ["Right"])
+    lv = emu.build_levels(True, 10, 10, 0.1, 0.1, dr, 2)
+    p1 = lv[1]
+    assert p1["dir"][2] == 10
+    c = lv[2]                                         # 10 cells -> 5
+    assert c["nx"] == 5 and c["dir"][2] == 5
+    c2 = lv[3]                                        # 5 cells -> 3 (padded)
+    assert c2["nx"] == 3 and c2["dir"][2] == 2

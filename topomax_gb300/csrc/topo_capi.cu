@@ -1,0 +1,780 @@
+// C ABI of the topomax GB300 design loop: problem context, load assembly,
+// iterative refinement, sensitivity and the entropic-mirror-descent update.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "topomax_gb300.h"
+#include "topo_mg_impl.cuh"
+#include "topo_setup.h"
+
+namespace topo {
+extern template class MG<float>;
+extern template class MG<double>;
+}  // namespace topo
+
+using namespace topo;
+
+namespace {
+
+constexpr int kFilterMaxIt = 200;
+constexpr int kStateMaxIt = 500;
+constexpr int kMaxOuter = 30;
+
+struct NewtonState {
+  double c;
+  double f, fp;
+  int done, ok, iters, pad;
+};
+
+__device__ __forceinline__ double expit_d(double x) { return 1.0 / (1.0 + exp(-x)); }
+
+// ---------------------------------------------------------------------------
+// design-level kernels
+// ---------------------------------------------------------------------------
+__global__ void k_kappa_p2(int nx, int ny, Penal<double> pen, const double* __restrict__ xi,
+                           double* __restrict__ kK) {
+  const size_t nt = size_t(2) * nx * ny;
+  const int VX = nx + 1;
+  TOPO_GRID_STRIDE(t, nt) {
+    const int o = int(t & 1);
+    const size_t cell = t >> 1;
+    const int i = int(cell % nx), j = int(cell / nx);
+    double xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
+    kK[t] = tri_kappa(xe, pen);
+  }
+}
+
+__global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
+                                int nxc, int nyc) {
+  const size_t nt = size_t(2) * nxc * nyc;
+  TOPO_GRID_STRIDE(t, nt) {
+    const int o = int(t & 1);
+    const size_t cell = t >> 1;
+    kc[t] = coarsen_kappa(kf, nxf, nyf, int(cell % nxc), int(cell / nxc), o);
+  }
+}
+
+template <class TQ>
+__global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu, TQ area, Penal<TQ> pen,
+                           const double* __restrict__ u, const double* __restrict__ xi, TQ* __restrict__ out) {
+  const size_t nt = size_t(2) * nx * ny;
+  const int VX = nx + 1, NX = 2 * nx + 1;
+  TOPO_GRID_STRIDE(t, nt) {
+    const int o = int(t & 1);
+    const size_t cell = t >> 1;
+    const int i = int(cell % nx), j = int(cell / nx);
+    double ue[6][2];
+    for (int k = 0; k < 6; ++k) {
+      const size_t n = size_t(2 * j + p2_off_b(o, k)) * NX + 2 * i + p2_off_a(o, k);
+      ue[k][0] = u[2 * n];
+      ue[k][1] = u[2 * n + 1];
+    }
+    TQ xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = TQ(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
+    TQ c[3];
+    if (o == 0) tri_sensitivity<0, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+    else tri_sensitivity<1, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+    out[3 * t] = c[0];
+    out[3 * t + 1] = c[1];
+    out[3 * t + 2] = c[2];
+  }
+}
+
+template <class TQ>
+__global__ void k_vertex_gather3(int nx, int ny, const TQ* __restrict__ tri3, double* __restrict__ b) {
+  const int VX = nx + 1;
+  const size_t nv = size_t(nx + 1) * (ny + 1);
+  TOPO_GRID_STRIDE(v, nv) {
+    const int a = int(v % VX), bb = int(v / VX);
+    double s = 0.0;
+    for (int e = 0; e < 6; ++e) {
+      int dci, dcj, o, loc;
+      p1_incidence(e, dci, dcj, o, loc);
+      const int ci = a + dci, cj = bb + dcj;
+      if (ci < 0 || ci >= nx || cj < 0 || cj >= ny) continue;
+      const size_t t = (size_t(cj) * nx + ci) * 2 + o;
+      s += double(tri3[3 * t + loc]);
+    }
+    b[v] = s;
+  }
+}
+
+__global__ void k_emd_half(const double* __restrict__ psi_prev, const double* __restrict__ g, double alpha,
+                           double* __restrict__ half, size_t n) {
+  TOPO_GRID_STRIDE(i, n) half[i] = psi_prev[i] - alpha * g[i];
+}
+
+// One Newton step of  F(c) = int expit(half + c) - volume = 0  (src/solver.py:149-186,
+// scipy newton semantics: stop when |c_new - c| < tol).
+__global__ void k_newton(const double* __restrict__ half, const double* __restrict__ w, size_t n, double volume,
+                         double tol, int maxit, double* partials, unsigned* counter, NewtonState* st) {
+  if (st->done) return;
+  const double c = st->c;
+  double v[2] = {0.0, 0.0};
+  TOPO_GRID_STRIDE(i, n) {
+    const double e = expit_d(half[i] + c);
+    v[0] += w[i] * e;
+    v[1] += w[i] * (e * (1.0 - e));
+  }
+  double tot[2];
+  if (finish_reduction<2>(v, partials, counter, tot)) {
+    const double f = tot[0] - volume, fp = tot[1];
+    st->f = f;
+    st->fp = fp;
+    st->iters += 1;
+    if (f == 0.0) {
+      st->done = 1;
+      st->ok = 1;
+    } else if (fp == 0.0 || !isfinite(f) || !isfinite(fp)) {
+      st->done = 1;
+      st->ok = 0;
+    } else {
+      const double p = c - f / fp;
+      if (!isfinite(p)) {
+        st->done = 1;
+        st->ok = 0;
+      } else if (fabs(p - c) < tol) {
+        st->c = p;
+        st->done = 1;
+        st->ok = 1;
+      } else {
+        st->c = p;
+        if (st->iters >= maxit) {
+          st->done = 1;
+          st->ok = 0;
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_eval_volume(const double* __restrict__ half, const double* __restrict__ w, size_t n, double c,
+                              double* partials, unsigned* counter, double* out) {
+  double v[1] = {0.0};
+  TOPO_GRID_STRIDE(i, n) v[0] += w[i] * expit_d(half[i] + c);
+  double tot[1];
+  if (finish_reduction<1>(v, partials, counter, tot)) out[0] = tot[0];
+}
+
+__global__ void k_emd_final(const double* __restrict__ half, const NewtonState* st, const double* cfix,
+                            double* __restrict__ psi, size_t n) {
+  const double c = cfix ? *cfix : st->c;
+  TOPO_GRID_STRIDE(i, n) psi[i] = half[i] + c;
+}
+
+__global__ void k_emd_finish(const double* __restrict__ psi, const double* __restrict__ psi_prev,
+                             const double* __restrict__ w, double* __restrict__ rho, size_t n, double* partials,
+                             unsigned* counter, double* out) {
+  double v[1] = {0.0};
+  TOPO_GRID_STRIDE(i, n) {
+    const double r = expit_d(psi[i]);
+    if (rho) rho[i] = r;
+    if (psi_prev) {
+      const double d = r - expit_d(psi_prev[i]);
+      v[0] += w[i] * d * d;
+    }
+  }
+  if (!psi_prev) return;
+  double tot[1];
+  if (finish_reduction<1>(v, partials, counter, tot)) out[0] = tot[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct topo_ctx {
+  int device = 0;
+  int sms = 148;
+  int precision = TOPO_PREC_MIXED;
+  bool has_state = false;
+  int nx = 0, ny = 0;
+  double W = 0, H = 0, hx = 0, hy = 0;
+  double E = 0, nu = 0, lmbda = 0, mu = 0, eps = 0, pmin = 1e-6;
+  bool penal_set = false;
+  double p = 0;
+  Dir dir_p2{};
+  Arena arena;
+  Reducer red;
+  std::string err;
+  size_t nv = 0, nn2 = 0;
+  double* vw = nullptr;
+  double* load = nullptr;
+  // state hierarchy
+  std::vector<LevelSpec> sspec;
+  std::vector<ElemRefs> srefs;
+  std::vector<double*> skK;
+  MG<float> smg32;
+  MG<double> smg64;
+  float* xi32 = nullptr;
+  double* r64 = nullptr;
+  double* y64 = nullptr;
+  float* d32 = nullptr;
+  // filter hierarchy
+  std::vector<LevelSpec> fspec;
+  std::vector<ElemRefs> frefs;
+  std::vector<double*> fkK, fkM;
+  MG<float> fmg32;
+  MG<double> fmg64;
+  double* fb64 = nullptr;
+  double* fr64 = nullptr;
+  double* fy64 = nullptr;
+  float* fd32 = nullptr;
+  // sensitivity / design scratch
+  void* sens_tri = nullptr;
+  double* half = nullptr;
+  NewtonState* nstate = nullptr;
+  double* cfix = nullptr;
+
+  ~topo_ctx() {
+    if (red.host) cudaFreeHost(red.host);
+  }
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_check(const char* where) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TOPO_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+    return TOPO_OK;
+  }
+  int grid(size_t n) const { return vec_grid(n, sms); }
+
+  template <class T>
+  P2Params<T> p2params() const {
+    P2Params<T> P;
+    std::memset(&P, 0, sizeof(P));
+    P.nx = nx;
+    P.ny = ny;
+    P.ihx = T(1.0 / hx);
+    P.ihy = T(1.0 / hy);
+    const double area = 0.5 * hx * hy;
+    P.lamT = T(lmbda * area);
+    P.mu2T = T(2.0 * mu * area);
+    P.pen = make_penal<T>(p, pmin);
+    P.dir = dir_p2;
+    return P;
+  }
+
+  double dot64(const double* a, const double* b, size_t n, cudaStream_t s) {
+    k_dot<double, double><<<red.blocks, kVecThreads, 0, s>>>(a, b, n, red.partials, red.counter, red.out);
+    cudaMemcpyAsync(red.host, red.out, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return red.host[0];
+  }
+};
+
+namespace {
+
+
+int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
+  if (!g || g->nx < 1 || g->ny < 1 || !(g->width > 0) || !(g->height > 0))
+    return C->fail(TOPO_ERR_ARG, "invalid grid description");
+  if (precision != TOPO_PREC_FP64 && precision != TOPO_PREC_MIXED)
+    return C->fail(TOPO_ERR_ARG, "unknown precision mode %d", precision);
+  if (size_t(2 * g->nx + 1) * size_t(2 * g->ny + 1) > (size_t(1) << 31))
+    return C->fail(TOPO_ERR_ARG, "grid too large");
+  if (cudaGetDevice(&C->device) != cudaSuccess) return C->fail(TOPO_ERR_CUDA, "no CUDA device");
+  cudaDeviceGetAttribute(&C->sms, cudaDevAttrMultiProcessorCount, C->device);
+  C->precision = precision;
+  C->nx = g->nx;
+  C->ny = g->ny;
+  C->W = g->width;
+  C->H = g->height;
+  C->hx = g->width / g->nx;
+  C->hy = g->height / g->ny;
+  C->nv = size_t(g->nx + 1) * (g->ny + 1);
+  C->nn2 = size_t(2 * g->nx + 1) * (2 * g->ny + 1);
+  C->red.init(C->arena, C->sms);
+  const std::vector<double> w = vertex_weights(C->nx, C->ny, C->hx, C->hy);
+  C->vw = C->arena.alloc_n<double>(C->nv);
+  if (!C->vw) return C->fail(TOPO_ERR_CUDA, "out of device memory");
+  cudaMemcpy(C->vw, w.data(), C->nv * sizeof(double), cudaMemcpyHostToDevice);
+  C->half = C->arena.alloc_n<double>(C->nv);
+  C->nstate = C->arena.alloc_n<NewtonState>(1);
+  C->cfix = C->arena.alloc_n<double>(1);
+  return TOPO_OK;
+}
+
+int init_filter(topo_ctx* C, double eps) {
+  C->eps = eps;
+  const Dir nd = no_dir(C->nx + 1, C->ny + 1);
+  C->fspec = build_levels(false, C->nx, C->ny, C->hx, C->hy, nd, 1);
+  const int L = int(C->fspec.size());
+  C->frefs.resize(L);
+  C->fkK.resize(L);
+  C->fkM.resize(L);
+  for (int l = 0; l < L; ++l) {
+    C->frefs[l] = make_elem_refs(C->fspec[l].hx, C->fspec[l].hy, 0.0, 0.0);
+    C->fkK[l] = C->arena.alloc_n<double>(C->fspec[l].ntri());
+    C->fkM[l] = C->arena.alloc_n<double>(C->fspec[l].ntri());
+  }
+  cudaStream_t s = 0;
+  k_fill<double><<<C->grid(C->fspec[0].ntri()), kVecThreads, 0, s>>>(C->fkK[0], eps * eps, C->fspec[0].ntri());
+  k_fill<double><<<C->grid(C->fspec[0].ntri()), kVecThreads, 0, s>>>(C->fkM[0], 1.0, C->fspec[0].ntri());
+  for (int l = 1; l < L; ++l) {
+    const LevelSpec &F = C->fspec[l - 1], &Cc = C->fspec[l];
+    k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->fkK[l - 1], F.nx, F.ny, C->fkK[l], Cc.nx, Cc.ny);
+    k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->fkM[l - 1], F.nx, F.ny, C->fkM[l], Cc.nx, Cc.ny);
+  }
+  std::vector<const double*> kK(C->fkK.begin(), C->fkK.end()), kM(C->fkM.begin(), C->fkM.end());
+  C->fb64 = C->arena.alloc_n<double>(C->nv);
+  C->fr64 = C->arena.alloc_n<double>(C->nv);
+  C->fy64 = C->arena.alloc_n<double>(C->nv);
+  int st;
+  if (C->precision == TOPO_PREC_MIXED) {
+    C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
+    C->fmg32.set_coefficients(kK, kM);
+    C->fd32 = C->arena.alloc_n<float>(C->nv);
+    if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
+    st = C->fmg32.setup(s);
+  } else {
+    C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
+    C->fmg64.set_coefficients(kK, kM);
+    if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
+    st = C->fmg64.setup(s);
+  }
+  if (st) return C->fail(st == -5 ? TOPO_ERR_CUDA : TOPO_ERR_NOT_CONVERGED, "filter multigrid set-up failed (%d)", st);
+  return C->cuda_check("filter set-up");
+}
+
+// FP64 filter operator y = (eps^2 K1 + M1) x  (or M1 x when stiff == 0)
+void filter_apply64(topo_ctx* C, const double* x, double* y, bool stiff, cudaStream_t s) {
+  auto P = make_p1<double, 1>(C->fspec[0], C->frefs[0], nullptr, nullptr);
+  P.kK_c = stiff ? C->eps * C->eps : 0.0;
+  P.kM_c = 1.0;
+  k_p1_apply<double, 1><<<C->grid(C->nv), kVecThreads, 0, s>>>(P, x, y);
+}
+
+// Iterative refinement: FP32 multigrid CG inside an FP64 residual loop.
+template <class Apply64>
+int ir_solve(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, double* x, bool warm, size_t n,
+             double rtol, double* r64, double* y64, float* d32, int maxit, SolveStats& st, cudaStream_t s) {
+  const int g = C->grid(n);
+  st = SolveStats{};
+  if (!warm) k_fill<double><<<g, kVecThreads, 0, s>>>(x, 0.0, n);
+  const double bn = std::sqrt(C->dot64(b, b, n, s));
+  if (!std::isfinite(bn)) return C->fail(TOPO_ERR_NAN, "non-finite right-hand side");
+  if (bn == 0.0) {
+    k_fill<double><<<g, kVecThreads, 0, s>>>(x, 0.0, n);
+    return TOPO_OK;
+  }
+  float* r32 = mg.scratch0(4);
+  for (int outer = 0; outer <= kMaxOuter; ++outer) {
+    apply64(x, y64, s);
+    k_sub<double><<<g, kVecThreads, 0, s>>>(r64, b, y64, n);
+    const double rn = std::sqrt(C->dot64(r64, r64, n, s));
+    st.relres = rn / bn;
+    st.outer = outer;
+    if (!std::isfinite(rn)) return C->fail(TOPO_ERR_NAN, "non-finite residual");
+    if (rn <= rtol * bn) return TOPO_OK;
+    if (outer == kMaxOuter) break;
+    k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, r64, 1.0 / rn, n);
+    const double inner = std::min(0.1, std::max(1e-5, 0.3 * rtol * bn / rn));
+    SolveStats is;
+    const int rc = mg.pcg(r32, d32, false, inner, maxit, is, s);
+    st.iterations += is.iterations;
+    if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
+    if (rc != 0 && !(is.relres < 0.5)) return C->fail(TOPO_ERR_NOT_CONVERGED, "inner solve stalled (relres %.3g)", is.relres);
+    k_add_scaled<double, float><<<g, kVecThreads, 0, s>>>(x, rn, d32, n);
+  }
+  return C->fail(TOPO_ERR_NOT_CONVERGED, "refinement did not reach rtol %.3g (relres %.3g)", rtol, st.relres);
+}
+
+int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int* iters, cudaStream_t s) {
+  SolveStats st;
+  int rc;
+  if (C->precision == TOPO_PREC_MIXED) {
+    auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
+    rc = ir_solve(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fr64, C->fy64, C->fd32, kFilterMaxIt, st, s);
+  } else {
+    rc = C->fmg64.pcg(b, xi, false, rtol, kFilterMaxIt, st, s);
+    if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
+    else if (rc) rc = C->fail(TOPO_ERR_NOT_CONVERGED, "filter CG did not converge (relres %.3g)", st.relres);
+  }
+  if (iters) *iters = st.iterations;
+  if (rc) return rc;
+  return C->cuda_check("filter solve");
+}
+
+int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
+  const int L = int(C->sspec.size());
+  Penal<double> pen = make_penal<double>(C->p, C->pmin);
+  k_kappa_p2<<<C->grid(C->sspec[1].ntri()), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->skK[1]);
+  for (int l = 2; l < L; ++l) {
+    const LevelSpec &F = C->sspec[l - 1], &Cc = C->sspec[l];
+    k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->skK[l - 1], F.nx, F.ny, C->skK[l], Cc.nx, Cc.ny);
+  }
+  int st;
+  if (C->precision == TOPO_PREC_MIXED) {
+    k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
+    C->smg32.set_p2(C->p2params<float>(), C->xi32);
+    st = C->smg32.setup(s);
+  } else {
+    C->smg64.set_p2(C->p2params<double>(), xi);
+    st = C->smg64.setup(s);
+  }
+  if (st == -5) return C->fail(TOPO_ERR_CUDA, "state set-up: CUDA error");
+  if (st) return C->fail(TOPO_ERR_NOT_CONVERGED, "state set-up: coarse operator not positive definite");
+  return TOPO_OK;
+}
+
+template <class F>
+int guarded(topo_ctx* C, F&& f) {
+  if (!C) return TOPO_ERR_ARG;
+  try {
+    C->err.clear();
+    return f();
+  } catch (const std::exception& e) {
+    return C->fail(TOPO_ERR_CUDA, "exception: %s", e.what());
+  } catch (...) {
+    return C->fail(TOPO_ERR_CUDA, "unknown exception");
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// exported entry points
+// ---------------------------------------------------------------------------
+extern "C" {
+
+topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, const topo_bc_desc* bc,
+                      const topo_load_desc* load, int precision, int* status) {
+  topo_ctx* C = nullptr;
+  int rc = TOPO_OK;
+  try {
+    C = new topo_ctx();
+    rc = init_common(C, grid, precision);
+    if (!rc && !mat) rc = C->fail(TOPO_ERR_ARG, "material description missing");
+    if (!rc) {
+      if (!(mat->poisson_ratio < 0.5) || !(mat->young_modulus > 0) || !(mat->filter_radius >= 0))
+        rc = C->fail(TOPO_ERR_ARG, "invalid material parameters");
+    }
+    if (!rc) {
+      C->has_state = true;
+      C->E = mat->young_modulus;
+      C->nu = mat->poisson_ratio;
+      C->mu = C->E / (2 * (1 + C->nu));                 // FEM_src/elasisity_problem.py:97-99
+      C->lmbda = C->mu * C->nu / (0.5 - C->nu);
+      C->pmin = mat->penal_min > 0 ? mat->penal_min : 1e-6;
+      std::string msg;
+      if (make_p2_dir(C->nx, C->ny, C->hx, C->hy, bc, C->dir_p2, msg)) rc = C->fail(TOPO_ERR_ARG, "%s", msg.c_str());
+    }
+    if (!rc && load) {
+      if (load->n_tractions < 0 || (load->n_tractions > 0 && !load->tractions))
+        rc = C->fail(TOPO_ERR_ARG, "invalid traction list");
+      for (int k = 0; !rc && k < load->n_tractions; ++k) {
+        const int sd = load->tractions[k].side;
+        if (sd != TOPO_SIDE_LEFT && sd != TOPO_SIDE_RIGHT && sd != TOPO_SIDE_TOP && sd != TOPO_SIDE_BOTTOM)
+          rc = C->fail(TOPO_ERR_ARG, "Malformed side: %d", sd);
+      }
+    }
+    if (!rc) {
+      std::vector<double> b;
+      assemble_load(C->nx, C->ny, C->W, C->H, C->dir_p2, load, b);
+      C->load = C->arena.alloc_n<double>(b.size());
+      if (!C->load) rc = C->fail(TOPO_ERR_CUDA, "out of device memory");
+      else cudaMemcpy(C->load, b.data(), b.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (!rc) {
+      C->sspec = build_levels(true, C->nx, C->ny, C->hx, C->hy, C->dir_p2, 2);
+      const int L = int(C->sspec.size());
+      C->srefs.resize(L);
+      C->skK.assign(L, nullptr);
+      for (int l = 0; l < L; ++l) {
+        C->srefs[l] = make_elem_refs(C->sspec[l].hx, C->sspec[l].hy, C->lmbda, C->mu);
+        if (l > 0) C->skK[l] = C->arena.alloc_n<double>(C->sspec[l].ntri());
+      }
+      std::vector<const double*> kK(C->skK.begin(), C->skK.end()), kM(L, nullptr);
+      const size_t n = 2 * C->nn2;
+      C->r64 = C->arena.alloc_n<double>(n);
+      C->y64 = C->arena.alloc_n<double>(n);
+      if (precision == TOPO_PREC_MIXED) {
+        C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg32.set_coefficients(kK, kM);
+        C->xi32 = C->arena.alloc_n<float>(C->nv);
+        C->d32 = C->arena.alloc_n<float>(n);
+        C->sens_tri = C->arena.alloc_n<float>(size_t(3) * C->sspec[0].ntri());
+      } else {
+        C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg64.set_coefficients(kK, kM);
+        C->sens_tri = C->arena.alloc_n<double>(size_t(3) * C->sspec[0].ntri());
+      }
+      if (C->arena.failed()) rc = C->fail(TOPO_ERR_CUDA, "out of device memory");
+    }
+    if (!rc) rc = init_filter(C, mat->filter_radius);
+  } catch (...) {
+    rc = TOPO_ERR_CUDA;
+  }
+  if (status) *status = rc;
+  if (rc) {
+    if (C && status) {
+      // keep the message reachable through a failed create: print it
+      std::fprintf(stderr, "topo_create: %s\n", C->err.c_str());
+    }
+    delete C;
+    return nullptr;
+  }
+  return C;
+}
+
+topo_ctx* topo_create_filter(const topo_grid_desc* grid, double epsilon, int precision, int* status) {
+  topo_ctx* C = nullptr;
+  int rc = TOPO_OK;
+  try {
+    C = new topo_ctx();
+    rc = init_common(C, grid, precision);
+    if (!rc && !(epsilon >= 0)) rc = C->fail(TOPO_ERR_ARG, "invalid filter radius");
+    if (!rc) rc = init_filter(C, epsilon);
+  } catch (...) {
+    rc = TOPO_ERR_CUDA;
+  }
+  if (status) *status = rc;
+  if (rc) {
+    if (C) std::fprintf(stderr, "topo_create_filter: %s\n", C->err.c_str());
+    delete C;
+    return nullptr;
+  }
+  return C;
+}
+
+void topo_destroy(topo_ctx* ctx) { delete ctx; }
+
+const char* topo_last_error(const topo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs) {
+  if (!ctx) return TOPO_ERR_ARG;
+  if (n_vertices) *n_vertices = int64_t(ctx->nv);
+  if (n_dofs) *n_dofs = int64_t(2 * ctx->nn2);
+  return TOPO_OK;
+}
+
+int topo_set_penalization(topo_ctx* ctx, double p) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context has no penaliser");
+    if (!std::isfinite(p)) return ctx->fail(TOPO_ERR_ARG, "non-finite penalisation");
+    ctx->p = p;
+    ctx->penal_set = true;
+    return TOPO_OK;
+  });
+}
+
+int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, int* iters, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!f || !xi || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid filter arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    filter_apply64(ctx, f, ctx->fb64, false, s);
+    return filter_solve_impl(ctx, ctx->fb64, xi, rtol, iters, s);
+  });
+}
+
+int topo_filter_solve(topo_ctx* ctx, const double* b, double* xi, double rtol, int* iters, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!b || !xi || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid filter arguments");
+    return filter_solve_impl(ctx, b, xi, rtol, iters, reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, int flags, int* iters,
+                     topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
+    if (!xi || !u || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid state-solve arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int rc = state_setup(ctx, xi, s);
+    if (rc) return rc;
+    const size_t n = 2 * ctx->nn2;
+    const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
+    SolveStats st;
+    if (ctx->precision == TOPO_PREC_MIXED) {
+      P2Params<double> P64 = ctx->p2params<double>();
+      auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
+      rc = ir_solve(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->r64, ctx->y64, ctx->d32, kStateMaxIt,
+                    st, s);
+    } else {
+      rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, kStateMaxIt, st, s);
+      if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");
+      else if (rc) rc = ctx->fail(TOPO_ERR_NOT_CONVERGED, "state CG did not converge (relres %.3g)", st.relres);
+    }
+    if (iters) *iters = st.iterations;
+    if (rc) return rc;
+    return ctx->cuda_check("state solve");
+  });
+}
+
+int topo_compliance(topo_ctx* ctx, const double* u, double* compliance, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!u || !compliance) return ctx->fail(TOPO_ERR_ARG, "invalid compliance arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    k_dot<double, double><<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->load, u, 2 * ctx->nn2, ctx->red.partials,
+                                                                ctx->red.counter, compliance);
+    return ctx->cuda_check("compliance");
+  });
+}
+
+int topo_sensitivity_rhs(topo_ctx* ctx, const double* u, const double* xi, double* b, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
+    if (!u || !xi || !b) return ctx->fail(TOPO_ERR_ARG, "invalid sensitivity arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t nt = size_t(2) * ctx->nx * ctx->ny;
+    const double area = 0.5 * ctx->hx * ctx->hy;
+    if (ctx->precision == TOPO_PREC_MIXED) {
+      float* tri = static_cast<float*>(ctx->sens_tri);
+      k_sens_tri<float><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
+                                                               float(ctx->lmbda), float(ctx->mu), float(area),
+                                                               make_penal<float>(ctx->p, ctx->pmin), u, xi, tri);
+      k_vertex_gather3<float><<<ctx->grid(ctx->nv), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, tri, b);
+    } else {
+      double* tri = static_cast<double*>(ctx->sens_tri);
+      k_sens_tri<double><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
+                                                                ctx->lmbda, ctx->mu, area,
+                                                                make_penal<double>(ctx->p, ctx->pmin), u, xi, tri);
+      k_vertex_gather3<double><<<ctx->grid(ctx->nv), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, tri, b);
+    }
+    return ctx->cuda_check("sensitivity");
+  });
+}
+
+int topo_sensitivity(topo_ctx* ctx, const double* u, const double* xi, double* g, double rtol, int* iters,
+                     topo_stream_t stream) {
+  int rc = topo_sensitivity_rhs(ctx, u, xi, ctx ? ctx->fb64 : nullptr, stream);
+  if (rc) return rc;
+  return guarded(ctx, [&]() {
+    if (!g || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid sensitivity arguments");
+    return filter_solve_impl(ctx, ctx->fb64, g, rtol, iters, reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double alpha, double volume, double* psi,
+                  double* c_out, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!psi_prev || !g || !psi || !std::isfinite(alpha) || !std::isfinite(volume))
+      return ctx->fail(TOPO_ERR_ARG, "invalid step arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t n = ctx->nv;
+    k_emd_half<<<ctx->grid(n), kVecThreads, 0, s>>>(psi_prev, g, alpha, ctx->half, n);
+    NewtonState init{};
+    init.c = 0.0;
+    cudaMemcpyAsync(ctx->nstate, &init, sizeof(init), cudaMemcpyHostToDevice, s);
+    NewtonState hs{};
+    const int maxit = 50;  // scipy.optimize.newton default
+    for (int launched = 0; launched < maxit;) {
+      const int chunk = std::min(8, maxit - launched);
+      for (int k = 0; k < chunk; ++k)
+        k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
+                                                          ctx->red.partials, ctx->red.counter, ctx->nstate);
+      launched += chunk;
+      cudaMemcpyAsync(&hs, ctx->nstate, sizeof(hs), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return ctx->cuda_check("projection");
+      if (hs.done) break;
+    }
+    double c = hs.c;
+    if (!(hs.done && hs.ok)) {
+      // bracketing fallback (src/utils.py:138-157): grow [-r, r] from 2 while r <= 2000
+      auto F = [&](double cc) {
+        k_eval_volume<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, cc, ctx->red.partials,
+                                                                ctx->red.counter, ctx->red.out);
+        cudaMemcpyAsync(ctx->red.host, ctx->red.out, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        return ctx->red.host[0] - volume;
+      };
+      double r = 2.0, lo = 0, hi = 0, flo = 0, fhi = 0;
+      bool found = false;
+      while (r <= 2000.0) {
+        flo = F(-r);
+        fhi = F(r);
+        if (std::isfinite(flo) && std::isfinite(fhi) && ((flo <= 0 && fhi >= 0) || (flo >= 0 && fhi <= 0))) {
+          found = true;
+          lo = -r;
+          hi = r;
+          break;
+        }
+        r *= 2;
+      }
+      if (!found) return ctx->fail(TOPO_ERR_PROJECTION, "Projection failed to converge");
+      if (flo == 0) c = lo;
+      else if (fhi == 0) c = hi;
+      else {
+        for (int it = 0; it < 200 && hi - lo > 2e-12; ++it) {
+          const double mid = 0.5 * (lo + hi), fm = F(mid);
+          if (fm == 0) { lo = hi = mid; break; }
+          if ((fm < 0) == (flo < 0)) { lo = mid; flo = fm; }
+          else hi = mid;
+        }
+        c = 0.5 * (lo + hi);
+      }
+      cudaMemcpyAsync(ctx->cfix, &c, sizeof(double), cudaMemcpyHostToDevice, s);
+      k_emd_final<<<ctx->grid(n), kVecThreads, 0, s>>>(ctx->half, ctx->nstate, ctx->cfix, psi, n);
+    } else {
+      k_emd_final<<<ctx->grid(n), kVecThreads, 0, s>>>(ctx->half, ctx->nstate, nullptr, psi, n);
+    }
+    if (c_out) *c_out = c;
+    return ctx->cuda_check("projection");
+  });
+}
+
+int topo_emd_finish(topo_ctx* ctx, const double* psi, const double* psi_prev, double* rho, double* delta,
+                    topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!psi) return ctx->fail(TOPO_ERR_ARG, "invalid arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    k_emd_finish<<<ctx->red.blocks, kVecThreads, 0, s>>>(psi, psi_prev, ctx->vw, rho, ctx->nv, ctx->red.partials,
+                                                         ctx->red.counter, ctx->red.out);
+    if (psi_prev && delta) {
+      cudaMemcpyAsync(ctx->red.host, ctx->red.out, sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      *delta = std::sqrt(ctx->red.host[0]);
+    }
+    return ctx->cuda_check("design update");
+  });
+}
+
+int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!f || !out) return ctx->fail(TOPO_ERR_ARG, "invalid integrate arguments");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    k_dot<double, double><<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->vw, f, ctx->nv, ctx->red.partials,
+                                                                ctx->red.counter, out);
+    return ctx->cuda_check("integrate");
+  });
+}
+
+int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
+    if (!xi || !u || !y) return ctx->fail(TOPO_ERR_ARG, "invalid apply arguments");
+    p2_apply_f64(ctx->p2params<double>(), xi, u, y, reinterpret_cast<cudaStream_t>(stream));
+    return ctx->cuda_check("apply");
+  });
+}
+
+int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!b) return ctx->fail(TOPO_ERR_ARG, "null output");
+    cudaMemcpyAsync(b, ctx->load, 2 * ctx->nn2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                    reinterpret_cast<cudaStream_t>(stream));
+    return ctx->cuda_check("load vector");
+  });
+}
+
+}  // extern "C"

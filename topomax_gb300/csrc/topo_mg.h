@@ -1,0 +1,150 @@
+// Geometric multigrid-preconditioned CG on the structured lattice.
+//
+// Level 0 is either the matrix-free P2 elasticity operator (state solve) or
+// a P1 operator (Helmholtz filter).  Every coarser level is a P1 operator with
+// per-triangle coefficients (see topo_p1.cuh); the coarsest level (at most
+// kCoarseMaxDofs unknowns) is solved with a dense inverse formed on the GPU.
+// Smoothing: Chebyshev polynomials in D^-1 A with eigenvalue bounds from a
+// power iteration at set-up.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "topo_common.cuh"
+#include "topo_p2.cuh"
+
+namespace topo {
+
+constexpr int kCoarseMaxDofs = 64;
+
+// Device memory owner: everything allocated here is freed with the arena.
+class Arena {
+ public:
+  Arena() = default;
+  Arena(const Arena&) = delete;
+  Arena& operator=(const Arena&) = delete;
+  ~Arena();
+  void* alloc(size_t bytes);
+  template <class T>
+  T* alloc_n(size_t n) { return static_cast<T*>(alloc(n * sizeof(T))); }
+  size_t bytes() const { return bytes_; }
+  bool failed() const { return failed_; }
+
+ private:
+  std::vector<void*> ptrs_;
+  size_t bytes_ = 0;
+  bool failed_ = false;
+};
+
+struct LevelSpec {
+  bool p2 = false;  // P2 elasticity level (only level 0 of the state hierarchy)
+  int nx = 0, ny = 0;
+  int NX = 0, NY = 0, NC = 1;
+  double hx = 0, hy = 0;
+  Dir dir{};
+  size_t nn() const { return size_t(NX) * NY; }
+  size_t ndof() const { return nn() * NC; }
+  size_t ntri() const { return size_t(2) * nx * ny; }
+};
+
+Dir coarsen_dir(const Dir& f, int NXf, int NYf, int NXc, int NYc);
+std::vector<LevelSpec> build_levels(bool p2_top, int nx, int ny, double hx, double hy,
+                                    const Dir& top, int NC);
+
+// Unit-coefficient P1 element matrices of one level.
+struct ElemRefs {
+  double K2[2][6][6];  // elasticity (lambda, mu given)
+  double K1[2][3][3];  // Laplacian
+  double M1[2][3][3];  // mass
+};
+ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu);
+
+// Reduction scratch shared by one stream.
+struct Reducer {
+  double* partials = nullptr;  // [blocks * 4]
+  unsigned* counter = nullptr;
+  double* out = nullptr;       // device scalars [16]
+  double* host = nullptr;      // pinned mirror [16]
+  int sms = 148;
+  int blocks = 0;
+  void init(Arena& a, int sms);
+};
+
+struct SolveStats {
+  int iterations = 0;       // inner CG iterations (sum)
+  int outer = 0;            // refinement steps
+  double relres = 0.0;      // final relative residual (in the solve's precision)
+  int status = 0;
+};
+
+template <class T>
+class MG {
+ public:
+  // coefficient masters (double, per P1 level; index by level) are owned by
+  // the caller and must outlive the MG object.
+  void init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, double lmbda, double mu,
+            Arena& arena, Reducer* red);
+  // level-0 P2 parameters; xi points to the design in precision T
+  void set_p2(const P2Params<T>& p, const T* xi) { p2_ = p; xi_ = xi; }
+  // kK/kM masters per level (entries for P2 level ignored; nullptr allowed)
+  void set_coefficients(const std::vector<const double*>& kK, const std::vector<const double*>& kM) {
+    kK64_ = kK;
+    kM64_ = kM;
+  }
+  // constant mass coefficient on level 0 when it is P1 (filter)
+  int setup(cudaStream_t s);  // diagonals, eigen bounds, coarse inverse
+  void apply(int l, const T* x, T* y, cudaStream_t s);
+  void vcycle(const T* b, T* x, cudaStream_t s);
+  // preconditioned CG on level 0: solves A x = b to ||r|| <= rtol ||b||
+  // (x used as initial guess when x_nonzero)
+  int pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s);
+  const LevelSpec& spec(int l) const { return specs_[l]; }
+  int levels() const { return int(specs_.size()); }
+  double lmax(int l) const { return lv_[l].lmax; }
+  // device scratch vectors of level 0 (n dofs), free for callers between solves
+  T* scratch0(int k) { return pcg_[k]; }
+
+  int cheb_degree = 2;
+  double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
+  int power_iters = 12;
+
+ private:
+  struct Lev {
+    T *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *t = nullptr;
+    T* diag = nullptr;
+    T* dinv = nullptr;
+    T* kK = nullptr;
+    T* kM = nullptr;
+    double lmax = 1.0;
+  };
+  void vcycle_level(int l, cudaStream_t s);
+  void smooth(int l, const T* b, T* x, bool xzero, cudaStream_t s);
+  void restrict_to(int l, const T* rf, T* bc, cudaStream_t s);
+  void prolong_add(int l, const T* xc, T* xf, cudaStream_t s);
+  double dot(const T* a, const T* b, size_t n, cudaStream_t s);  // synchronising
+  void diag_of(int l, T* d, cudaStream_t s);
+  double estimate_lmax(int l, cudaStream_t s);
+
+  std::vector<LevelSpec> specs_;
+  std::vector<Lev> lv_;
+  const ElemRefs* refs_ = nullptr;
+  std::vector<const double*> kK64_, kM64_;
+  double lmbda_ = 0, mu_ = 0;
+  P2Params<T> p2_{};
+  const T* xi_ = nullptr;
+  T* cinv_ = nullptr;  // dense coarsest inverse
+  int* cstat_ = nullptr;
+  T* pcg_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  Reducer* red_ = nullptr;
+  int sms_ = 148;
+};
+
+// y = A x for the FP64 P2 operator (used for refinement residuals)
+void p2_apply_f64(const P2Params<double>& p, const double* xi, const double* x, double* y,
+                  cudaStream_t s);
+void p2_apply_f32(const P2Params<float>& p, const float* xi, const float* x, float* y,
+                  cudaStream_t s);
+
+}  // namespace topo

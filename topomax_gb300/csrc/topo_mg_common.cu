@@ -1,0 +1,154 @@
+// Precision-independent parts of the multigrid set-up.
+#include <algorithm>
+#include <cstring>
+
+#include "topo_mg.h"
+
+namespace topo {
+
+Arena::~Arena() {
+  for (void* p : ptrs_) cudaFree(p);
+}
+
+void* Arena::alloc(size_t bytes) {
+  void* p = nullptr;
+  const size_t b = std::max<size_t>(bytes, 16);
+  if (cudaMalloc(&p, b) != cudaSuccess) {
+    failed_ = true;
+    return nullptr;
+  }
+  cudaMemset(p, 0, b);
+  ptrs_.push_back(p);
+  bytes_ += b;
+  return p;
+}
+
+static void add_point(Dir& d, int a, int b, int NX, int NY) {
+  if (a < 0 || b < 0 || a >= NX || b >= NY) return;
+  for (int k = 0; k < d.npts; ++k)
+    if (d.pts[2 * k] == a && d.pts[2 * k + 1] == b) return;
+  if (d.npts < kMaxDirPoints) {
+    d.pts[2 * d.npts] = a;
+    d.pts[2 * d.npts + 1] = b;
+    ++d.npts;
+  }
+}
+
+// Coarse node I is clamped when its hat function is non-zero at a clamped
+// fine node (fine columns 2I-1..2I+1), so the coarse space stays inside the
+// fine space of functions vanishing on the clamped nodes.
+Dir coarsen_dir(const Dir& f, int NXf, int NYf, int NXc, int NYc) {
+  Dir c;
+  std::memset(&c, 0, sizeof(c));
+  c.x_lo = f.x_lo;
+  c.y_lo = f.y_lo;
+  c.x_hi_from = (f.x_hi_from >= NXf) ? NXc : f.x_hi_from / 2;
+  c.y_hi_from = (f.y_hi_from >= NYf) ? NYc : f.y_hi_from / 2;
+  for (int k = 0; k < f.npts; ++k) {
+    const int a = f.pts[2 * k], b = f.pts[2 * k + 1];
+    const int pa = a & 1, pb = b & 1;
+    if (!pa && !pb) {
+      add_point(c, a / 2, b / 2, NXc, NYc);
+    } else if (pa && !pb) {
+      add_point(c, (a - 1) / 2, b / 2, NXc, NYc);
+      add_point(c, (a + 1) / 2, b / 2, NXc, NYc);
+    } else if (!pa && pb) {
+      add_point(c, a / 2, (b - 1) / 2, NXc, NYc);
+      add_point(c, a / 2, (b + 1) / 2, NXc, NYc);
+    } else {
+      add_point(c, (a - 1) / 2, (b - 1) / 2, NXc, NYc);
+      add_point(c, (a + 1) / 2, (b + 1) / 2, NXc, NYc);
+    }
+  }
+  return c;
+}
+
+std::vector<LevelSpec> build_levels(bool p2_top, int nx, int ny, double hx, double hy, const Dir& top, int NC) {
+  std::vector<LevelSpec> v;
+  LevelSpec L;
+  if (p2_top) {
+    L.p2 = true;
+    L.nx = nx;
+    L.ny = ny;
+    L.NX = 2 * nx + 1;
+    L.NY = 2 * ny + 1;
+    L.NC = 2;
+    L.hx = hx;
+    L.hy = hy;
+    L.dir = top;
+    v.push_back(L);
+    LevelSpec P;
+    P.p2 = false;
+    P.nx = nx;
+    P.ny = ny;
+    P.NX = nx + 1;
+    P.NY = ny + 1;
+    P.NC = 2;
+    P.hx = hx;
+    P.hy = hy;
+    P.dir = coarsen_dir(top, L.NX, L.NY, P.NX, P.NY);
+    v.push_back(P);
+  } else {
+    L.p2 = false;
+    L.nx = nx;
+    L.ny = ny;
+    L.NX = nx + 1;
+    L.NY = ny + 1;
+    L.NC = NC;
+    L.hx = hx;
+    L.hy = hy;
+    L.dir = top;
+    v.push_back(L);
+  }
+  while (v.back().ndof() > size_t(kCoarseMaxDofs) && (v.back().nx > 1 || v.back().ny > 1)) {
+    const LevelSpec& F = v.back();
+    LevelSpec C;
+    C.p2 = false;
+    C.nx = (F.nx + 1) / 2;
+    C.ny = (F.ny + 1) / 2;
+    C.NX = C.nx + 1;
+    C.NY = C.ny + 1;
+    C.NC = F.NC;
+    C.hx = 2 * F.hx;
+    C.hy = 2 * F.hy;
+    C.dir = coarsen_dir(F.dir, F.NX, F.NY, C.NX, C.NY);
+    v.push_back(C);
+  }
+  return v;
+}
+
+ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu) {
+  ElemRefs R;
+  std::memset(&R, 0, sizeof(R));
+  const double area = 0.5 * hx * hy;
+  // barycentric gradients, orientation 0: (v0,v1,v3), 1: (v0,v2,v3)
+  const double G[2][3][2] = {{{-1 / hx, 0}, {1 / hx, -1 / hy}, {0, 1 / hy}},
+                             {{0, -1 / hy}, {-1 / hx, 1 / hy}, {1 / hx, 0}}};
+  for (int o = 0; o < 2; ++o) {
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) {
+        const double gg = G[o][k][0] * G[o][l][0] + G[o][k][1] * G[o][l][1];
+        R.K1[o][k][l] = area * gg;
+        R.M1[o][k][l] = area / 12.0 * (k == l ? 2.0 : 1.0);
+        for (int c = 0; c < 2; ++c)
+          for (int d = 0; d < 2; ++d) {
+            // K[(k,c),(l,d)] = lam dc(lk) dd(ll) + mu dcd grad lk.grad ll + mu dc(ll) dd(lk)
+            double v = lmbda * G[o][k][c] * G[o][l][d] + mu * G[o][l][c] * G[o][k][d];
+            if (c == d) v += mu * gg;
+            R.K2[o][2 * k + c][2 * l + d] = area * v;
+          }
+      }
+  }
+  return R;
+}
+
+void Reducer::init(Arena& a, int nsms) {
+  sms = nsms;
+  blocks = nsms * 8;
+  partials = a.alloc_n<double>(size_t(blocks) * 4);
+  counter = a.alloc_n<unsigned>(1);
+  out = a.alloc_n<double>(16);
+  cudaMallocHost(&host, 16 * sizeof(double));
+}
+
+}  // namespace topo

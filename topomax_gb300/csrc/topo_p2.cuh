@@ -1,0 +1,355 @@
+// Matrix-free vector-P2 SIMP elasticity operator on the structured lattice.
+//
+// Restates the bilinear form of FEM_src/elasisity_problem.py:104-132,
+//   a(u,v) = (r(xi) [lambda div(u) I + 2 mu eps(u)], eps(v)) dx,
+// integrated with the 7-point degree-5 rule.  Per triangle the displacement
+// gradient is linear, so with vertex values G_k of grad(u) and the
+// r-weighted mass matrix M_kl = sum_q w_q r(xi_q) lam_qk lam_ql the quadrature
+// sum becomes   y_(m,c) = sum_k (S_k gradN_m(v_k))_c,   S_k = sum_l M_kl sigma(G_l),
+// which is algebraically identical to the quadrature of the assembled form.
+//
+// The kernels are split into load / compute / gather phases (separated by
+// __syncthreads on the GPU) so the test emulator can run the same phases on
+// the CPU.
+#pragma once
+
+#include "topo_common.cuh"
+
+namespace topo {
+
+template <class T>
+struct P2Params {
+  int nx, ny;     // cells
+  T ihx, ihy;     // 1/hx, 1/hy
+  T lamT, mu2T;   // lambda*|T|, 2*mu*|T|
+  Penal<T> pen;
+  Dir dir;        // on the (2nx+1)x(2ny+1) node lattice
+};
+
+// r-weighted P1 mass matrix of one triangle, packed [00,11,22,01,02,12].
+template <class T>
+TOPO_HD void tri_rmass(const T (&xi)[3], const Penal<T>& pen, T (&M)[6]) {
+  for (int k = 0; k < 6; ++k) M[k] = T(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int q = 0; q < Rule7::n; ++q) {
+    const T l0 = T(Rule7::lam(q, 0)), l1 = T(Rule7::lam(q, 1)), l2 = T(Rule7::lam(q, 2));
+    const T x = l0 * xi[0] + l1 * xi[1] + l2 * xi[2];
+    const T wr = T(Rule7::w(q)) * pen.r(x);
+    M[0] += wr * (l0 * l0);
+    M[1] += wr * (l1 * l1);
+    M[2] += wr * (l2 * l2);
+    M[3] += wr * (l0 * l1);
+    M[4] += wr * (l0 * l2);
+    M[5] += wr * (l1 * l2);
+  }
+}
+
+// S * g_I for symmetric S = (xx, yy, xy); g in units of (ihx, ihy).
+template <int O, int I, class T>
+TOPO_HD void sg(const T (&s)[3], T ihx, T ihy, T& ox, T& oy) {
+  if constexpr (O == 0) {
+    if constexpr (I == 0) { ox = -s[0] * ihx; oy = -s[2] * ihx; }
+    else if constexpr (I == 1) { ox = s[0] * ihx - s[2] * ihy; oy = s[2] * ihx - s[1] * ihy; }
+    else { ox = s[2] * ihy; oy = s[1] * ihy; }
+  } else {
+    if constexpr (I == 0) { ox = -s[2] * ihy; oy = -s[1] * ihy; }
+    else if constexpr (I == 1) { ox = s[2] * ihy - s[0] * ihx; oy = s[1] * ihy - s[2] * ihx; }
+    else { ox = s[0] * ihx; oy = s[2] * ihx; }
+  }
+}
+
+// Vertex gradients G[k] = grad(u)(v_k) = [[ux_x, ux_y],[uy_x, uy_y]] of the P2
+// field with local node values u (order A,B,C,mid(BC),mid(AC),mid(AB)).
+template <int O, class T, class TU>
+TOPO_HD void p2_vertex_grads(const TU (&u)[6][2], T ihx, T ihy, T (&G)[3][2][2]) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int c = 0; c < 2; ++c) {
+    // W[k][i]: coefficient of g_i in grad(u)(v_k), component c
+    const TU w00 = TU(3) * u[0][c], w01 = TU(4) * u[5][c] - u[1][c], w02 = TU(4) * u[4][c] - u[2][c];
+    const TU w10 = TU(4) * u[5][c] - u[0][c], w11 = TU(3) * u[1][c], w12 = TU(4) * u[3][c] - u[2][c];
+    const TU w20 = TU(4) * u[4][c] - u[0][c], w21 = TU(4) * u[3][c] - u[1][c], w22 = TU(3) * u[2][c];
+    if constexpr (O == 0) {
+      G[0][c][0] = T(w01 - w00) * ihx; G[0][c][1] = T(w02 - w01) * ihy;
+      G[1][c][0] = T(w11 - w10) * ihx; G[1][c][1] = T(w12 - w11) * ihy;
+      G[2][c][0] = T(w21 - w20) * ihx; G[2][c][1] = T(w22 - w21) * ihy;
+    } else {
+      G[0][c][0] = T(w02 - w01) * ihx; G[0][c][1] = T(w01 - w00) * ihy;
+      G[1][c][0] = T(w12 - w11) * ihx; G[1][c][1] = T(w11 - w10) * ihy;
+      G[2][c][0] = T(w22 - w21) * ihx; G[2][c][1] = T(w21 - w20) * ihy;
+    }
+  }
+}
+
+// y = K_T u for one triangle of orientation O.
+template <int O, class T>
+TOPO_HD void tri_apply(const T (&u)[6][2], const T (&xi)[3], const P2Params<T>& P, T (&y)[6][2]) {
+  T M[6];
+  tri_rmass(xi, P.pen, M);
+  T G[3][2][2];
+  p2_vertex_grads<O>(u, P.ihx, P.ihy, G);
+  const T muT = T(0.5) * P.mu2T;
+  T sig[3][3];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int k = 0; k < 3; ++k) {
+    const T exx = G[k][0][0], eyy = G[k][1][1];
+    const T tr = exx + eyy;
+    sig[k][0] = P.lamT * tr + P.mu2T * exx;
+    sig[k][1] = P.lamT * tr + P.mu2T * eyy;
+    sig[k][2] = muT * (G[k][0][1] + G[k][1][0]);
+  }
+  T S[3][3];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int c = 0; c < 3; ++c) {
+    S[0][c] = M[0] * sig[0][c] + M[3] * sig[1][c] + M[4] * sig[2][c];
+    S[1][c] = M[3] * sig[0][c] + M[1] * sig[1][c] + M[5] * sig[2][c];
+    S[2][c] = M[4] * sig[0][c] + M[5] * sig[1][c] + M[2] * sig[2][c];
+  }
+  // vertex nodes: (4 S_i - sum S) g_i
+  T Q[3][3];
+  for (int c = 0; c < 3; ++c) {
+    const T tot = S[0][c] + S[1][c] + S[2][c];
+    Q[0][c] = T(4) * S[0][c] - tot;
+    Q[1][c] = T(4) * S[1][c] - tot;
+    Q[2][c] = T(4) * S[2][c] - tot;
+  }
+  sg<O, 0>(Q[0], P.ihx, P.ihy, y[0][0], y[0][1]);
+  sg<O, 1>(Q[1], P.ihx, P.ihy, y[1][0], y[1][1]);
+  sg<O, 2>(Q[2], P.ihx, P.ihy, y[2][0], y[2][1]);
+  // edge nodes: 4 (S_i g_j + S_j g_i)
+  T ax, ay, bx, by;
+  sg<O, 2>(S[1], P.ihx, P.ihy, ax, ay);
+  sg<O, 1>(S[2], P.ihx, P.ihy, bx, by);
+  y[3][0] = T(4) * (ax + bx); y[3][1] = T(4) * (ay + by);
+  sg<O, 2>(S[0], P.ihx, P.ihy, ax, ay);
+  sg<O, 0>(S[2], P.ihx, P.ihy, bx, by);
+  y[4][0] = T(4) * (ax + bx); y[4][1] = T(4) * (ay + by);
+  sg<O, 1>(S[0], P.ihx, P.ihy, ax, ay);
+  sg<O, 0>(S[1], P.ihx, P.ihy, bx, by);
+  y[5][0] = T(4) * (ax + bx); y[5][1] = T(4) * (ay + by);
+}
+
+// Diagonal of K_T for one triangle.
+template <class T>
+TOPO_HD void tri_diag(int o, const T (&xi)[3], const P2Params<T>& P, T (&d)[6][2]) {
+  T M[6];
+  tri_rmass(xi, P.pen, M);
+  const int gxs_[2][3] = {{-1, 1, 0}, {0, -1, 1}};
+  const int gys_[2][3] = {{0, -1, 1}, {-1, 1, 0}};
+  const T lmT = P.lamT + P.mu2T, muT = T(0.5) * P.mu2T;
+  for (int m = 0; m < 6; ++m) {
+    T vx[3], vy[3];
+    for (int k = 0; k < 3; ++k) {
+      int cx, cy;  // gradient of N_m at vertex k in units of (ihx, ihy)
+      if (m < 3) {
+        const int f = (k == m) ? 3 : -1;
+        cx = f * gxs_[o][m];
+        cy = f * gys_[o][m];
+      } else {
+        const int i = (m == 3) ? 1 : 0, j = (m == 5) ? 1 : 2;  // edge (i,j)
+        cx = 0; cy = 0;
+        if (k == i) { cx += 4 * gxs_[o][j]; cy += 4 * gys_[o][j]; }
+        if (k == j) { cx += 4 * gxs_[o][i]; cy += 4 * gys_[o][i]; }
+      }
+      vx[k] = T(cx) * P.ihx;
+      vy[k] = T(cy) * P.ihy;
+    }
+    const T qx = M[0] * vx[0] * vx[0] + M[1] * vx[1] * vx[1] + M[2] * vx[2] * vx[2] +
+                 T(2) * (M[3] * vx[0] * vx[1] + M[4] * vx[0] * vx[2] + M[5] * vx[1] * vx[2]);
+    const T qy = M[0] * vy[0] * vy[0] + M[1] * vy[1] * vy[1] + M[2] * vy[2] * vy[2] +
+                 T(2) * (M[3] * vy[0] * vy[1] + M[4] * vy[0] * vy[2] + M[5] * vy[1] * vy[2]);
+    d[m][0] = lmT * qx + muT * qy;
+    d[m][1] = lmT * qy + muT * qx;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tiled kernel phases
+// ---------------------------------------------------------------------------
+constexpr int P2_TX = 32;  // owned cells per tile in x
+constexpr int P2_TY = 8;   // owned cells per tile in y
+constexpr int P2_THREADS = 256;
+
+struct P2Tile {
+  static constexpr int CX = P2_TX + 1, CY = P2_TY + 1;  // computed cells (1-cell halo at low side)
+  static constexpr int NTX = 2 * CX + 1, NTY = 2 * CY + 1;
+  static constexpr int VX = CX + 1, VY = CY + 1;
+  static constexpr int NTRI = CX * CY * 2;
+};
+
+template <class T>
+struct P2Smem {
+  T u[P2Tile::NTY][P2Tile::NTX][2];
+  T xi[P2Tile::VY][P2Tile::VX];
+  T out[P2Tile::NTRI][12];
+};
+
+template <class T>
+struct P2Kern {
+  using Smem = P2Smem<T>;
+
+  TOPO_HD static void load(int tid, int nt, int bx, int by, const P2Params<T>& P,
+                           const T* u, const T* xi, Smem& s) {
+    const int i0 = bx * P2_TX, j0 = by * P2_TY;
+    const int A0 = 2 * (i0 - 1), B0 = 2 * (j0 - 1);
+    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+    if (u) {
+      for (int idx = tid; idx < P2Tile::NTX * P2Tile::NTY; idx += nt) {
+        const int al = idx % P2Tile::NTX, bl = idx / P2Tile::NTX;
+        const int a = A0 + al, b = B0 + bl;
+        T v0 = T(0), v1 = T(0);
+        if (a >= 0 && a < NX && b >= 0 && b < NY && !is_clamped(P.dir, a, b)) {
+          const size_t n = size_t(b) * NX + a;
+          v0 = u[2 * n];
+          v1 = u[2 * n + 1];
+        }
+        s.u[bl][al][0] = v0;
+        s.u[bl][al][1] = v1;
+      }
+    }
+    const int VXg = P.nx + 1, VYg = P.ny + 1;
+    for (int idx = tid; idx < P2Tile::VX * P2Tile::VY; idx += nt) {
+      const int il = idx % P2Tile::VX, jl = idx / P2Tile::VX;
+      const int i = i0 - 1 + il, j = j0 - 1 + jl;
+      s.xi[jl][il] = (i >= 0 && i < VXg && j >= 0 && j < VYg) ? xi[size_t(j) * VXg + i] : T(0);
+    }
+  }
+
+  // mode 0: operator apply, mode 1: diagonal
+  TOPO_HD static void compute(int tid, int nt, int bx, int by, const P2Params<T>& P, Smem& s,
+                              int mode) {
+    const int i0 = bx * P2_TX, j0 = by * P2_TY;
+    for (int t = tid; t < P2Tile::NTRI; t += nt) {
+      const int o = t & 1, cell = t >> 1;
+      const int ci = cell % P2Tile::CX, cj = cell / P2Tile::CX;
+      const int ig = i0 - 1 + ci, jg = j0 - 1 + cj;
+      T y[6][2];
+      if (ig < 0 || ig >= P.nx || jg < 0 || jg >= P.ny) {
+        for (int k = 0; k < 6; ++k) y[k][0] = y[k][1] = T(0);
+      } else {
+        T xe[3];
+        for (int k = 0; k < 3; ++k) xe[k] = s.xi[cj + p1_off_b(o, k)][ci + p1_off_a(o, k)];
+        if (mode == 1) {
+          tri_diag(o, xe, P, y);
+        } else {
+          T ue[6][2];
+          for (int k = 0; k < 6; ++k) {
+            const int al = 2 * ci + p2_off_a(o, k), bl = 2 * cj + p2_off_b(o, k);
+            ue[k][0] = s.u[bl][al][0];
+            ue[k][1] = s.u[bl][al][1];
+          }
+          if (o == 0) tri_apply<0>(ue, xe, P, y);
+          else tri_apply<1>(ue, xe, P, y);
+        }
+      }
+      for (int k = 0; k < 6; ++k) {
+        s.out[t][2 * k] = y[k][0];
+        s.out[t][2 * k + 1] = y[k][1];
+      }
+    }
+  }
+
+  TOPO_HD static T tri_val(const Smem& s, int ci, int cj, int o, int k, int c) {
+    if (ci < 0 || ci >= P2Tile::CX || cj < 0 || cj >= P2Tile::CY) return T(0);
+    return s.out[(cj * P2Tile::CX + ci) * 2 + o][2 * k + c];
+  }
+
+  // Sum the per-triangle results onto the tile's owned nodes.
+  // mode 0: y = K u (clamped rows copy u);  mode 1: y = diag (clamped rows 1).
+  TOPO_HD static void gather(int tid, int nt, int bx, int by, const P2Params<T>& P,
+                             const Smem& s, const T* u, T* y, int mode) {
+    const int i0 = bx * P2_TX, j0 = by * P2_TY;
+    const int NX = 2 * P.nx + 1;
+    const int a_beg = 2 * i0, b_beg = 2 * j0;
+    const int a_end = (i0 + P2_TX >= P.nx) ? 2 * P.nx + 1 : 2 * (i0 + P2_TX);
+    const int b_end = (j0 + P2_TY >= P.ny) ? 2 * P.ny + 1 : 2 * (j0 + P2_TY);
+    const int na = a_end - a_beg, nb = b_end - b_beg;
+    for (int idx = tid; idx < na * nb; idx += nt) {
+      const int a = a_beg + idx % na, b = b_beg + idx / na;
+      const int al = a - 2 * (i0 - 1), bl = b - 2 * (j0 - 1);
+      const int I = al >> 1, J = bl >> 1, pa = al & 1, pb = bl & 1;
+      const size_t n = size_t(b) * NX + a;
+      T r[2];
+      for (int c = 0; c < 2; ++c) {
+        T v;
+        if (!pa && !pb) {
+          v = tri_val(s, I - 1, J - 1, 0, 2, c) + tri_val(s, I - 1, J - 1, 1, 2, c) +
+              tri_val(s, I, J - 1, 1, 1, c) + tri_val(s, I - 1, J, 0, 1, c) +
+              tri_val(s, I, J, 0, 0, c) + tri_val(s, I, J, 1, 0, c);
+        } else if (pa && !pb) {
+          v = tri_val(s, I, J, 0, 5, c) + tri_val(s, I, J - 1, 1, 3, c);
+        } else if (!pa && pb) {
+          v = tri_val(s, I, J, 1, 5, c) + tri_val(s, I - 1, J, 0, 3, c);
+        } else {
+          v = tri_val(s, I, J, 0, 4, c) + tri_val(s, I, J, 1, 4, c);
+        }
+        r[c] = v;
+      }
+      if (is_clamped(P.dir, a, b)) {
+        if (mode == 1) { r[0] = T(1); r[1] = T(1); }
+        else { r[0] = u[2 * n]; r[1] = u[2 * n + 1]; }
+      }
+      y[2 * n] = r[0];
+      y[2 * n + 1] = r[1];
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// per-triangle kernels (no tiling)
+// ---------------------------------------------------------------------------
+
+// kappa_T = (1/|T|) int_T r(xi) with the 7-point rule: the Galerkin P1
+// coefficient of the P2 operator (P1 strains are constant per triangle).
+template <class T>
+TOPO_HD T tri_kappa(const T (&xi)[3], const Penal<T>& pen) {
+  T s = T(0);
+  for (int q = 0; q < Rule7::n; ++q) {
+    const T x = T(Rule7::lam(q, 0)) * xi[0] + T(Rule7::lam(q, 1)) * xi[1] + T(Rule7::lam(q, 2)) * xi[2];
+    s += T(Rule7::w(q)) * pen.r(x);
+  }
+  return s;
+}
+
+// Sensitivity moments c_k = int_T s phi_k, s = -r'(xi)(lambda div(u)^2 + 2 mu eps:eps)
+// (FEM_src/elasisity_problem.py:146-149) with the 12-point rule.  The vertex
+// gradients are formed in TG from the nodal values (this carries the
+// cancellation), the quadrature runs in TQ.
+template <int O, class TG, class TQ>
+TOPO_HD void tri_sensitivity(const TG (&u)[6][2], const TQ (&xi)[3], TG ihx, TG ihy, TQ lam,
+                             TQ mu, TQ area, const Penal<TQ>& pen, TQ (&c)[3]) {
+  TG Gd[3][2][2];
+  p2_vertex_grads<O>(u, ihx, ihy, Gd);
+  TQ G[3][2][2];
+  for (int k = 0; k < 3; ++k)
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 2; ++b) G[k][a][b] = TQ(Gd[k][a][b]);
+  c[0] = c[1] = c[2] = TQ(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int q = 0; q < Rule12::n; ++q) {
+    const TQ l0 = TQ(Rule12::lam(q, 0)), l1 = TQ(Rule12::lam(q, 1)), l2 = TQ(Rule12::lam(q, 2));
+    const TQ gxx = l0 * G[0][0][0] + l1 * G[1][0][0] + l2 * G[2][0][0];
+    const TQ gxy = l0 * G[0][0][1] + l1 * G[1][0][1] + l2 * G[2][0][1];
+    const TQ gyx = l0 * G[0][1][0] + l1 * G[1][1][0] + l2 * G[2][1][0];
+    const TQ gyy = l0 * G[0][1][1] + l1 * G[1][1][1] + l2 * G[2][1][1];
+    const TQ dv = gxx + gyy;
+    const TQ exy = TQ(0.5) * (gxy + gyx);
+    const TQ ee = gxx * gxx + gyy * gyy + TQ(2) * exy * exy;
+    const TQ x = l0 * xi[0] + l1 * xi[1] + l2 * xi[2];
+    const TQ sq = -pen.dr(x) * (lam * dv * dv + TQ(2) * mu * ee) * (TQ(Rule12::w(q)) * area);
+    c[0] += sq * l0;
+    c[1] += sq * l1;
+    c[2] += sq * l2;
+  }
+}
+
+}  // namespace topo

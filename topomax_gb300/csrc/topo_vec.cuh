@@ -1,0 +1,174 @@
+// Element-wise vector kernels and deterministic grid reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <type_traits>
+#include "topo_common.cuh"
+
+namespace topo {
+
+constexpr int kVecThreads = 256;
+
+inline int vec_grid(size_t n, int sms) {
+  size_t b = (n + kVecThreads - 1) / kVecThreads;
+  size_t cap = size_t(sms) * 8;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return int(b);
+}
+
+#define TOPO_GRID_STRIDE(i, n) \
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (n); i += size_t(gridDim.x) * blockDim.x)
+
+template <class T>
+__global__ void k_fill(T* x, T v, size_t n) { TOPO_GRID_STRIDE(i, n) x[i] = v; }
+
+template <class TD, class TS>
+__global__ void k_convert(TD* __restrict__ d, const TS* __restrict__ s, double scale, size_t n) {
+  TOPO_GRID_STRIDE(i, n) d[i] = TD(double(s[i]) * scale);
+}
+
+// y += a x
+template <class T>
+__global__ void k_axpy(T* __restrict__ y, T a, const T* __restrict__ x, size_t n) {
+  TOPO_GRID_STRIDE(i, n) y[i] += a * x[i];
+}
+
+// p = z + b p
+template <class T>
+__global__ void k_xpby(T* __restrict__ p, const T* __restrict__ z, T b, size_t n) {
+  TOPO_GRID_STRIDE(i, n) p[i] = z[i] + b * p[i];
+}
+
+// r = b - y
+template <class T>
+__global__ void k_sub(T* __restrict__ r, const T* __restrict__ b, const T* __restrict__ y, size_t n) {
+  TOPO_GRID_STRIDE(i, n) r[i] = b[i] - y[i];
+}
+
+// u += s * d  (d in lower precision)
+template <class TU, class TD>
+__global__ void k_add_scaled(TU* __restrict__ u, double s, const TD* __restrict__ d, size_t n) {
+  TOPO_GRID_STRIDE(i, n) u[i] += TU(s * double(d[i]));
+}
+
+template <class T>
+__global__ void k_mul(T* __restrict__ y, const T* __restrict__ a, const T* __restrict__ x, size_t n) {
+  TOPO_GRID_STRIDE(i, n) y[i] = a[i] * x[i];
+}
+
+template <class T>
+__global__ void k_scale(T* __restrict__ x, T a, size_t n) { TOPO_GRID_STRIDE(i, n) x[i] *= a; }
+
+template <class T>
+__global__ void k_recip(T* __restrict__ x, size_t n) {
+  TOPO_GRID_STRIDE(i, n) x[i] = T(1) / x[i];
+}
+
+// Chebyshev smoother pieces (preconditioner Dinv).
+// first step: d = c0 * Dinv r ; x = (xzero ? 0 : x) + d
+template <class T>
+__global__ void k_cheb_first(const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ d,
+                             T* __restrict__ x, T c0, int xzero, size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    const T di = c0 * dinv[i] * r[i];
+    d[i] = di;
+    x[i] = xzero ? di : x[i] + di;
+  }
+}
+// later steps: r -= t ; d = c1 d + c2 Dinv r ; x += d
+template <class T>
+__global__ void k_cheb_next(T* __restrict__ r, const T* __restrict__ t, const T* __restrict__ dinv,
+                            T* __restrict__ d, T* __restrict__ x, T c1, T c2, size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    const T ri = r[i] - t[i];
+    r[i] = ri;
+    const T di = c1 * d[i] + c2 * dinv[i] * ri;
+    d[i] = di;
+    x[i] += di;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reductions: per-block partial sums, the last block to finish adds the
+// partials in block order (deterministic) and stores the result.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+// Finishes a reduction of NV values per block.  Returns true in thread 0 of
+// the last block, with the totals in tot[].
+template <int NV>
+__device__ bool finish_reduction(const double (&v)[NV], double* partials, unsigned* counter,
+                                 double (&tot)[NV]) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  for (int k = 0; k < NV; ++k) {
+    const double s = block_sum(v[k], sh);
+    if (threadIdx.x == 0) partials[size_t(blockIdx.x) * NV + k] = s;
+  }
+  __threadfence();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      s += ((volatile double*)partials)[size_t(b) * NV + k];
+    // fixed-order combine: strided per-thread sums then a tree
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) tot[k] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return threadIdx.x == 0;
+}
+
+// out[0] = sum a_i b_i (or sum a_i^2 when b == nullptr)
+template <class TA, class TB>
+__global__ void k_dot(const TA* __restrict__ a, const TB* __restrict__ b, size_t n, double* partials,
+                      unsigned* counter, double* out) {
+  // per-thread partial in the input precision (a handful of terms), then FP64
+  using Acc = typename std::conditional<sizeof(TA) == 4 && sizeof(TB) == 4, float, double>::type;
+  Acc acc = Acc(0);
+  TOPO_GRID_STRIDE(i, n) acc += b ? Acc(a[i]) * Acc(b[i]) : Acc(a[i]) * Acc(a[i]);
+  double v[1] = {double(acc)};
+  double tot[1];
+  if (finish_reduction<1>(v, partials, counter, tot)) out[0] = tot[0];
+}
+
+// two dots at once: out[0] = a.b, out[1] = c.d
+template <class T>
+__global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
+                       const T* __restrict__ d, size_t n, double* partials, unsigned* counter,
+                       double* out) {
+  double v[2] = {0.0, 0.0};
+  TOPO_GRID_STRIDE(i, n) {
+    v[0] += double(a[i]) * double(b[i]);
+    v[1] += double(c[i]) * double(d[i]);
+  }
+  double tot[2];
+  if (finish_reduction<2>(v, partials, counter, tot)) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+}  // namespace topo

@@ -1,0 +1,31 @@
+"""SIMP penaliser bookkeeping (the reference's src/penalizers.py:7-46).
+
+The device evaluates r(x) = m + x^p (1 - m) inside the kernels; this object
+keeps the reference's host-side contract (penalisation must be set before
+use, ``ValueError`` otherwise) and evaluates r and r' on host or torch data.
+"""
+from __future__ import annotations
+
+
+class ElasticPenalizer:
+    """Solid isotropic material penalisation with minimum m = 1e-6."""
+
+    def __init__(self):
+        self.penalization: float | None = None
+        self.minimum = 1e-6
+
+    def set_penalization(self, penalization: float):
+        self.penalization = penalization
+
+    def assert_has_penalization(self):
+        if self.penalization is None:
+            raise ValueError("You must set penalization before calling penalizer")
+        return self.penalization
+
+    def __call__(self, rho):
+        p, m = self.assert_has_penalization(), self.minimum
+        return m + rho ** p * (1 - m)
+
+    def derivative(self, rho):
+        p, m = self.assert_has_penalization(), self.minimum
+        return p * rho ** (p - 1) * (1 - m)
