@@ -99,7 +99,7 @@ def test_state_compliance_gradient_match_oracle(precision, case):
                     young_modulus=2.5, poisson_ratio=0.25,
                     body_force=dict(region=dict(center=[0.5, 0.5], radius=0.05), value=[0.0, -10.0]))
         nx, ny = 40, 40
-    prob, V = _gpu_problem(d, nx, ny, precision=precision, rtol=1e-12)
+    prob, V = _gpu_problem(d, nx, ny, precision=precision, rtol=1e-11)
     o = FEMOracle(Lattice(d.width, d.height, nx, ny), d)
     prob.set_penalization(3.0)
     o.set_penalization(3.0)
@@ -156,7 +156,7 @@ def test_triangle_known_answer(precision, tmp_path):
     import topomax_gb300 as tg
     gold = json.load(open(os.path.join(GOLDEN, "triangle_N10.json")))
     s = tg.FEMSolver(10, os.path.join(GOLDEN, "designs", "triangle.json"), data_path=str(tmp_path),
-                     skip_multiple=999, precision=precision, rtol=1e-12, verbose=False)
+                     skip_multiple=999, precision=precision, rtol=1e-10, verbose=False)
     hist = s.solve()[3.0]
     assert hist["exit_condition"] == "Convergence treshold reached"
     assert hist["iterations"] == gold["iteration"]
@@ -217,5 +217,5 @@ def test_large_grid_properties(precision):
     v = torch.randn(u.numel(), generator=g, dtype=torch.float64).cuda()
     lhs = torch.dot(v, Ku).item()
     rhs = torch.dot(u, prob.apply_operator(xi, v)).item()
-    assert abs(lhs - rhs) <= 1e-10 * (abs(lhs) + 1e-300) + 1e-12
+    assert abs(lhs - rhs) <= 1e-12 * (v.norm() * Ku.norm()).item()
     assert prob.filtered_rho.tensor.min().item() > 0.0

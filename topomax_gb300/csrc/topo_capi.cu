@@ -31,6 +31,19 @@ struct NewtonState {
   int done, ok, iters, pad;
 };
 
+// Workspace of the flexible-GMRES refinement loop.
+struct Fgmres {
+  static constexpr int m = 8;  // restart length
+  double* V = nullptr;         // (m+1) x n Krylov basis (FP64)
+  float* Z = nullptr;          // m x n preconditioned directions (FP32 inner solutions)
+  double* t = nullptr;         // n
+  void init(Arena& a, size_t n) {
+    V = a.alloc_n<double>((m + 1) * n);
+    Z = a.alloc_n<float>(m * n);
+    t = a.alloc_n<double>(n);
+  }
+};
+
 __device__ __forceinline__ double expit_d(double x) { return 1.0 / (1.0 + exp(-x)); }
 
 // ---------------------------------------------------------------------------
@@ -227,6 +240,7 @@ struct topo_ctx {
   double* fr64 = nullptr;
   double* fy64 = nullptr;
   float* fd32 = nullptr;
+  Fgmres sgm, fgm;
   // sensitivity / design scratch
   void* sens_tri = nullptr;
   double* half = nullptr;
@@ -254,7 +268,7 @@ struct topo_ctx {
   int grid(size_t n) const { return vec_grid(n, sms); }
 
   template <class T>
-  P2Params<T> p2params() const {
+  P2Params<T> p2params(int clamp = 0) const {
     P2Params<T> P;
     std::memset(&P, 0, sizeof(P));
     P.nx = nx;
@@ -264,7 +278,7 @@ struct topo_ctx {
     const double area = 0.5 * hx * hy;
     P.lamT = T(lmbda * area);
     P.mu2T = T(2.0 * mu * area);
-    P.pen = make_penal<T>(p, pmin);
+    P.pen = make_penal<T>(p, pmin, clamp);
     P.dir = dir_p2;
     return P;
   }
@@ -339,6 +353,7 @@ int init_filter(topo_ctx* C, double eps) {
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg32.set_coefficients(kK, kM);
     C->fd32 = C->arena.alloc_n<float>(C->nv);
+    C->fgm.init(C->arena, C->nv);
     if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
     st = C->fmg32.setup(s);
   } else {
@@ -359,10 +374,16 @@ void filter_apply64(topo_ctx* C, const double* x, double* y, bool stiff, cudaStr
   k_p1_apply<double, 1><<<C->grid(C->nv), kVecThreads, 0, s>>>(P, x, y);
 }
 
-// Iterative refinement: FP32 multigrid CG inside an FP64 residual loop.
+// FP32 multigrid Krylov solves inside an FP64 flexible GMRES (right
+// preconditioning, restart Fgmres::m): every outer step computes the true FP64
+// residual, the inner FP32 solve supplies the next search direction and the
+// outer least-squares step fixes its length.  Converges like iterative
+// refinement on well-conditioned problems and stays robust when the operator
+// has a nearly singular or slightly negative mode that FP32 cannot resolve.
 template <class Apply64>
-int ir_solve(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, double* x, bool warm, size_t n,
-             double rtol, double* r64, double* y64, float* d32, int maxit, SolveStats& st, cudaStream_t s) {
+int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, double* x, bool warm, size_t n,
+              double rtol, Fgmres& W, int maxit, SolveStats& st, cudaStream_t s) {
+  constexpr int m = Fgmres::m;
   const int g = C->grid(n);
   st = SolveStats{};
   if (!warm) k_fill<double><<<g, kVecThreads, 0, s>>>(x, 0.0, n);
@@ -373,24 +394,88 @@ int ir_solve(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doubl
     return TOPO_OK;
   }
   float* r32 = mg.scratch0(4);
-  for (int outer = 0; outer <= kMaxOuter; ++outer) {
-    apply64(x, y64, s);
-    k_sub<double><<<g, kVecThreads, 0, s>>>(r64, b, y64, n);
-    const double rn = std::sqrt(C->dot64(r64, r64, n, s));
-    st.relres = rn / bn;
-    st.outer = outer;
-    if (!std::isfinite(rn)) return C->fail(TOPO_ERR_NAN, "non-finite residual");
-    if (rn <= rtol * bn) return TOPO_OK;
-    if (outer == kMaxOuter) break;
-    k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, r64, 1.0 / rn, n);
-    const double inner = std::min(0.1, std::max(1e-5, 0.3 * rtol * bn / rn));
-    SolveStats is;
-    const int rc = mg.pcg(r32, d32, false, inner, maxit, is, s);
-    st.iterations += is.iterations;
-    if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
-    if (rc != 0 && !(is.relres < 0.5)) return C->fail(TOPO_ERR_NOT_CONVERGED, "inner solve stalled (relres %.3g)", is.relres);
-    k_add_scaled<double, float><<<g, kVecThreads, 0, s>>>(x, rn, d32, n);
+  double* hbuf = C->red.host;
+  auto multidot = [&](int count, const double* w) {
+    k_multidot<double, double><<<C->red.blocks, kVecThreads, 0, s>>>(W.V, n, count, w, n, C->red.partials,
+                                                                     C->red.counter, C->red.out);
+    cudaMemcpyAsync(hbuf, C->red.out, count * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+  };
+  double prev = 0.0;
+  for (int cycle = 0; cycle < kMaxOuter; ++cycle) {
+    double* r = W.V;
+    apply64(x, W.t, s);
+    k_sub<double><<<g, kVecThreads, 0, s>>>(r, b, W.t, n);
+    const double beta = std::sqrt(C->dot64(r, r, n, s));
+    st.relres = beta / bn;
+    if (!std::isfinite(beta)) return C->fail(TOPO_ERR_NAN, "non-finite residual");
+    if (beta <= rtol * bn) return TOPO_OK;
+    if (cycle > 0 && beta > 0.9 * prev) break;  // stagnation at the FP64 residual floor
+    prev = beta;
+    k_scale<double><<<g, kVecThreads, 0, s>>>(r, 1.0 / beta, n);
+    const double inner = std::min(0.1, std::max(1e-5, 0.3 * rtol * bn / beta));
+    double H[m + 1][m] = {};
+    double cs[m], sn[m], gv[m + 1] = {};
+    gv[0] = beta;
+    int k = 0;
+    for (int j = 0; j < m; ++j) {
+      st.outer += 1;
+      double* vj = W.V + size_t(j) * n;
+      float* zj = W.Z + size_t(j) * n;
+      k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, vj, 1.0, n);
+      SolveStats is;
+      const int rc = mg.pcg(r32, zj, false, inner, maxit, is, s);
+      st.iterations += is.iterations;
+      st.minres |= is.minres;
+      if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
+      k_convert<double, float><<<g, kVecThreads, 0, s>>>(W.t, zj, 1.0, n);
+      double* w = W.V + size_t(j + 1) * n;
+      apply64(W.t, w, s);
+      // classical Gram-Schmidt, twice
+      double h[m + 1] = {};
+      for (int pass = 0; pass < 2; ++pass) {
+        multidot(j + 1, w);
+        MultiCoef cf{};
+        for (int i = 0; i <= j; ++i) {
+          cf.c[i] = hbuf[i];
+          h[i] += hbuf[i];
+        }
+        k_sub_multi<double, double><<<g, kVecThreads, 0, s>>>(w, W.V, n, j + 1, cf, n);
+      }
+      const double hn = std::sqrt(C->dot64(w, w, n, s));
+      if (!std::isfinite(hn)) return C->fail(TOPO_ERR_NAN, "non-finite Krylov vector");
+      for (int i = 0; i <= j; ++i) H[i][j] = h[i];
+      H[j + 1][j] = hn;
+      if (hn > 0) k_scale<double><<<g, kVecThreads, 0, s>>>(w, 1.0 / hn, n);
+      for (int i = 0; i < j; ++i) {  // previous rotations
+        const double t0 = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
+        H[i + 1][j] = -sn[i] * H[i][j] + cs[i] * H[i + 1][j];
+        H[i][j] = t0;
+      }
+      const double den = std::hypot(H[j][j], H[j + 1][j]);
+      cs[j] = den > 0 ? H[j][j] / den : 1.0;
+      sn[j] = den > 0 ? H[j + 1][j] / den : 0.0;
+      H[j][j] = den;
+      H[j + 1][j] = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      k = j + 1;
+      if (std::fabs(gv[j + 1]) <= 0.5 * rtol * bn || hn == 0.0) break;
+    }
+    double y[m] = {};
+    for (int i = k - 1; i >= 0; --i) {
+      double acc = gv[i];
+      for (int l = i + 1; l < k; ++l) acc -= H[i][l] * y[l];
+      y[i] = (H[i][i] != 0.0) ? acc / H[i][i] : 0.0;
+    }
+    MultiCoef cf{};
+    for (int i = 0; i < k; ++i) cf.c[i] = y[i];
+    k_add_multi<float, double><<<g, kVecThreads, 0, s>>>(x, W.Z, n, k, cf, n);
   }
+  apply64(x, W.t, s);
+  k_sub<double><<<g, kVecThreads, 0, s>>>(W.V, b, W.t, n);
+  st.relres = std::sqrt(C->dot64(W.V, W.V, n, s)) / bn;
+  if (st.relres <= rtol) return TOPO_OK;
   return C->fail(TOPO_ERR_NOT_CONVERGED, "refinement did not reach rtol %.3g (relres %.3g)", rtol, st.relres);
 }
 
@@ -399,7 +484,7 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   int rc;
   if (C->precision == TOPO_PREC_MIXED) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
-    rc = ir_solve(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fr64, C->fy64, C->fd32, kFilterMaxIt, st, s);
+    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, kFilterMaxIt, st, s);
   } else {
     rc = C->fmg64.pcg(b, xi, false, rtol, kFilterMaxIt, st, s);
     if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
@@ -412,7 +497,7 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
 
 int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const int L = int(C->sspec.size());
-  Penal<double> pen = make_penal<double>(C->p, C->pmin);
+  Penal<double> pen = make_penal<double>(C->p, C->pmin, 1);
   k_kappa_p2<<<C->grid(C->sspec[1].ntri()), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->skK[1]);
   for (int l = 2; l < L; ++l) {
     const LevelSpec &F = C->sspec[l - 1], &Cc = C->sspec[l];
@@ -421,10 +506,10 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   int st;
   if (C->precision == TOPO_PREC_MIXED) {
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
-    C->smg32.set_p2(C->p2params<float>(), C->xi32);
+    C->smg32.set_p2(C->p2params<float>(0), C->p2params<float>(1), C->xi32);
     st = C->smg32.setup(s);
   } else {
-    C->smg64.set_p2(C->p2params<double>(), xi);
+    C->smg64.set_p2(C->p2params<double>(0), C->p2params<double>(1), xi);
     st = C->smg64.setup(s);
   }
   if (st == -5) return C->fail(TOPO_ERR_CUDA, "state set-up: CUDA error");
@@ -508,6 +593,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg32.set_coefficients(kK, kM);
         C->xi32 = C->arena.alloc_n<float>(C->nv);
         C->d32 = C->arena.alloc_n<float>(n);
+        C->sgm.init(C->arena, n);
         C->sens_tri = C->arena.alloc_n<float>(size_t(3) * C->sspec[0].ntri());
       } else {
         C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
@@ -604,8 +690,7 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     if (ctx->precision == TOPO_PREC_MIXED) {
       P2Params<double> P64 = ctx->p2params<double>();
       auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
-      rc = ir_solve(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->r64, ctx->y64, ctx->d32, kStateMaxIt,
-                    st, s);
+      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, kStateMaxIt, st, s);
     } else {
       rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, kStateMaxIt, st, s);
       if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");

@@ -67,14 +67,22 @@ struct Penal {
   int ip;  // p as a positive integer, or -1
   T pm1;   // p-1
   int ipm1;
+  int clamp;  // 1: r is clamped below at pmin (the SPD preconditioner's coefficient)
 
-  TOPO_HD T r(T x) const { return pmin + pow_p(x, ip, p) * (T(1) - pmin); }
+  TOPO_HD T r(T x) const {
+    const T v = pmin + pow_p(x, ip, p) * (T(1) - pmin);
+    return (clamp && !(v >= pmin)) ? pmin : v;
+  }
   TOPO_HD T dr(T x) const { return p * pow_p(x, ipm1, pm1) * (T(1) - pmin); }
 };
 
+// clamp: the multigrid preconditioner uses max(r, m) so that it stays SPD even
+// where the filtered density undershoots below zero (then r(xi) < 0 at some
+// quadrature points and the true operator can be indefinite).
 template <class T>
-TOPO_HD Penal<T> make_penal(double p, double pmin) {
+TOPO_HD Penal<T> make_penal(double p, double pmin, int clamp = 0) {
   Penal<T> q;
+  q.clamp = clamp;
   q.pmin = T(pmin);
   q.p = T(p);
   q.pm1 = T(p - 1.0);

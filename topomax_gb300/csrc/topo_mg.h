@@ -63,7 +63,7 @@ ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu);
 
 // Reduction scratch shared by one stream.
 struct Reducer {
-  double* partials = nullptr;  // [blocks * 4]
+  double* partials = nullptr;  // [blocks * 16]
   unsigned* counter = nullptr;
   double* out = nullptr;       // device scalars [16]
   double* host = nullptr;      // pinned mirror [16]
@@ -73,7 +73,8 @@ struct Reducer {
 };
 
 struct SolveStats {
-  int iterations = 0;       // inner CG iterations (sum)
+  int iterations = 0;       // inner Krylov iterations (sum)
+  int minres = 0;           // 1 if the MINRES fallback ran
   int outer = 0;            // refinement steps
   double relres = 0.0;      // final relative residual (in the solve's precision)
   int status = 0;
@@ -86,8 +87,14 @@ class MG {
   // the caller and must outlive the MG object.
   void init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, double lmbda, double mu,
             Arena& arena, Reducer* red);
-  // level-0 P2 parameters; xi points to the design in precision T
-  void set_p2(const P2Params<T>& p, const T* xi) { p2_ = p; xi_ = xi; }
+  // level-0 P2 parameters: the Krylov operator (true penalisation) and the
+  // preconditioner's operator (penalisation clamped at its minimum, SPD);
+  // xi points to the design in precision T
+  void set_p2(const P2Params<T>& op, const P2Params<T>& pc, const T* xi) {
+    p2_op_ = op;
+    p2_ = pc;
+    xi_ = xi;
+  }
   // kK/kM masters per level (entries for P2 level ignored; nullptr allowed)
   void set_coefficients(const std::vector<const double*>& kK, const std::vector<const double*>& kM) {
     kK64_ = kK;
@@ -95,16 +102,22 @@ class MG {
   }
   // constant mass coefficient on level 0 when it is P1 (filter)
   int setup(cudaStream_t s);  // diagonals, eigen bounds, coarse inverse
-  void apply(int l, const T* x, T* y, cudaStream_t s);
+  // y = A_l x; on level 0, op selects the Krylov operator instead of the
+  // preconditioner's (they differ only where the penalisation is clamped)
+  void apply(int l, const T* x, T* y, cudaStream_t s, bool op = false);
   void vcycle(const T* b, T* x, cudaStream_t s);
-  // preconditioned CG on level 0: solves A x = b to ||r|| <= rtol ||b||
-  // (x used as initial guess when x_nonzero)
+  // Krylov solve on level 0, multigrid-preconditioned: CG, restarted as MINRES
+  // from the current iterate if CG meets p.Ap <= 0 (an indefinite operator).
+  // Solves A x = b to ||r|| <= rtol ||b|| (x used as initial guess when x_nonzero).
+  // Returns 0, -2 (iteration cap) or -4 (non-finite).
   int pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s);
+  int minres(const T* b, T* x, double rtol, int maxit, SolveStats& st, cudaStream_t s);
   const LevelSpec& spec(int l) const { return specs_[l]; }
   int levels() const { return int(specs_.size()); }
   double lmax(int l) const { return lv_[l].lmax; }
   // device scratch vectors of level 0 (n dofs), free for callers between solves
   T* scratch0(int k) { return pcg_[k]; }
+  static constexpr int kScratch = 9;
 
   int cheb_degree = 2;
   double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
@@ -132,11 +145,12 @@ class MG {
   const ElemRefs* refs_ = nullptr;
   std::vector<const double*> kK64_, kM64_;
   double lmbda_ = 0, mu_ = 0;
-  P2Params<T> p2_{};
+  P2Params<T> p2_{};     // preconditioner operator (clamped penalisation)
+  P2Params<T> p2_op_{};  // Krylov operator
   const T* xi_ = nullptr;
   T* cinv_ = nullptr;  // dense coarsest inverse
   int* cstat_ = nullptr;
-  T* pcg_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  T* pcg_[kScratch] = {};
   Reducer* red_ = nullptr;
   int sms_ = 148;
 };

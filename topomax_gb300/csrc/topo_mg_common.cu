@@ -145,7 +145,7 @@ ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu) {
 void Reducer::init(Arena& a, int nsms) {
   sms = nsms;
   blocks = nsms * 8;
-  partials = a.alloc_n<double>(size_t(blocks) * 4);
+  partials = a.alloc_n<double>(size_t(blocks) * 16);
   counter = a.alloc_n<unsigned>(1);
   out = a.alloc_n<double>(16);
   cudaMallocHost(&host, 16 * sizeof(double));

@@ -235,17 +235,17 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
     }
   }
   const size_t n0 = specs[0].ndof();
-  for (int k = 0; k < 5; ++k) pcg_[k] = arena.alloc_n<T>(n0);
+  for (int k = 0; k < kScratch; ++k) pcg_[k] = arena.alloc_n<T>(n0);
   const int nc = int(specs.back().ndof());
   cinv_ = arena.alloc_n<T>(size_t(nc) * nc);
   cstat_ = arena.alloc_n<int>(1);
 }
 
 template <class T>
-void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s) {
+void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   const LevelSpec& L = specs_[l];
   if (L.p2) {
-    launch_p2_apply<T>(p2_, xi_, x, y, s);
+    launch_p2_apply<T>(op ? p2_op_ : p2_, xi_, x, y, s);
     return;
   }
   const int g = vec_grid(L.nn(), sms_);
@@ -427,7 +427,7 @@ int MG<T>::pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveSt
     return 0;
   }
   if (x_nonzero) {
-    apply(0, x, q, s);
+    apply(0, x, q, s, true);
     k_sub<T><<<g, kVecThreads, 0, s>>>(r, b, q, n);
   } else {
     k_fill<T><<<g, kVecThreads, 0, s>>>(x, T(0), n);
@@ -440,11 +440,20 @@ int MG<T>::pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveSt
   double rz = dot(r, z, n, s);
   cudaMemcpyAsync(p, z, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   for (int it = 1; it <= maxit; ++it) {
-    apply(0, p, q, s);
+    apply(0, p, q, s, true);
     const double pq = dot(p, q, n, s);
-    if (!(pq > 0.0) || !std::isfinite(pq) || !std::isfinite(rz)) {
+    if (!std::isfinite(pq) || !std::isfinite(rz)) {
       st.iterations = it;
-      return std::isfinite(pq) ? -2 : -4;
+      return -4;
+    }
+    if (!(pq > 0.0) || !(rz > 0.0)) {
+      // indefinite operator: continue with MINRES from the current iterate
+      SolveStats ms;
+      const int rc = minres(b, x, rtol, maxit - it, ms, s);
+      st.iterations = it + ms.iterations;
+      st.relres = ms.relres;
+      st.minres = 1;
+      return rc;
     }
     const double alpha = rz / pq;
     k_axpy<T><<<g, kVecThreads, 0, s>>>(x, T(alpha), p, n);
@@ -461,6 +470,96 @@ int MG<T>::pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveSt
     k_xpby<T><<<g, kVecThreads, 0, s>>>(p, z, T(beta), n);
   }
   return -2;
+}
+
+// Preconditioned MINRES (Paige & Saunders) with the SPD V-cycle as M, started
+// from x.  The recurrence's residual estimate (in the M^-1 norm) steers the
+// iteration; the true 2-norm residual is checked before returning.
+template <class T>
+int MG<T>::minres(const T* b, T* x, double rtol, int maxit, SolveStats& st, cudaStream_t s) {
+  const size_t n = specs_[0].ndof();
+  const int g = vec_grid(n, sms_);
+  T* r1 = pcg_[0];
+  T* r2 = pcg_[1];
+  T* y = pcg_[2];
+  T* v = pcg_[3];
+  T* w = pcg_[5];
+  T* w1 = pcg_[6];
+  T* w2 = pcg_[7];
+  T* t = pcg_[8];
+  st = SolveStats{};
+  const double bn = std::sqrt(dot(b, b, n, s));
+  if (!std::isfinite(bn)) return -4;
+  int total = 0;
+  for (int restart = 0; restart < 4 && total < maxit; ++restart) {
+    apply(0, x, t, s, true);
+    k_sub<T><<<g, kVecThreads, 0, s>>>(r1, b, t, n);
+    const double rn0 = std::sqrt(dot(r1, r1, n, s));
+    st.relres = rn0 / bn;
+    if (!std::isfinite(rn0)) return -4;
+    if (rn0 <= rtol * bn) return 0;
+    vcycle(r1, y, s);
+    double beta1 = dot(r1, y, n, s);
+    if (!(beta1 > 0.0)) return -2;
+    beta1 = std::sqrt(beta1);
+    cudaMemcpyAsync(r2, r1, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    k_fill<T><<<g, kVecThreads, 0, s>>>(w, T(0), n);
+    k_fill<T><<<g, kVecThreads, 0, s>>>(w2, T(0), n);
+    double beta = beta1, oldb = 0.0, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0;
+    // the M^-1-norm estimate is compared against the same ratio of the 2-norms
+    const double target = rtol * bn / rn0;
+    for (int it = 1; it <= maxit - total; ++it) {
+      // v = y / beta ; y = A v - (beta/oldb) r1
+      k_convert<T, T><<<g, kVecThreads, 0, s>>>(v, y, 1.0 / beta, n);
+      apply(0, v, y, s, true);
+      if (it >= 2) k_axpy<T><<<g, kVecThreads, 0, s>>>(y, T(-beta / oldb), r1, n);
+      const double alpha = dot(v, y, n, s);
+      k_axpy<T><<<g, kVecThreads, 0, s>>>(y, T(-alpha / beta), r2, n);
+      std::swap(r1, r2);  // r1 <- r2, r2 <- y
+      cudaMemcpyAsync(r2, y, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+      vcycle(r2, y, s);
+      oldb = beta;
+      const double bb = dot(r2, y, n, s);
+      if (!std::isfinite(alpha) || !std::isfinite(bb)) return -4;
+      if (!(bb > 0.0)) {
+        total += it;
+        break;
+      }
+      beta = std::sqrt(bb);
+      const double oldeps = epsln;
+      const double delta = cs * dbar + sn * alpha;
+      const double gbar = sn * dbar - cs * alpha;
+      epsln = sn * beta;
+      dbar = -cs * beta;
+      double gamma = std::sqrt(gbar * gbar + beta * beta);
+      if (gamma < 1e-300) gamma = 1e-300;
+      cs = gbar / gamma;
+      sn = beta / gamma;
+      const double phi = cs * phibar;
+      phibar = sn * phibar;
+      // w1 <- w2, w2 <- w, w = (v - oldeps w1 - delta w2) / gamma ; x += phi w
+      std::swap(w1, w2);  // w1 <- old w2
+      std::swap(w2, w);   // w2 <- old w ; w now holds the stale w1 (overwritten below)
+      k_fill<T><<<g, kVecThreads, 0, s>>>(w, T(0), n);
+      k_axpy<T><<<g, kVecThreads, 0, s>>>(w, T(1.0 / gamma), v, n);
+      k_axpy<T><<<g, kVecThreads, 0, s>>>(w, T(-oldeps / gamma), w1, n);
+      k_axpy<T><<<g, kVecThreads, 0, s>>>(w, T(-delta / gamma), w2, n);
+      k_axpy<T><<<g, kVecThreads, 0, s>>>(x, T(phi), w, n);
+      st.iterations = total + it;
+      if (phibar / beta1 <= 0.5 * target) {
+        total += it;
+        break;
+      }
+      if (it == maxit - total) total = maxit;
+    }
+    st.minres = 1;
+  }
+  apply(0, x, t, s, true);
+  k_sub<T><<<g, kVecThreads, 0, s>>>(r1, b, t, n);
+  const double rn = std::sqrt(dot(r1, r1, n, s));
+  st.relres = rn / bn;
+  if (!std::isfinite(rn)) return -4;
+  return rn <= rtol * bn ? 0 : -2;
 }
 
 }  // namespace topo

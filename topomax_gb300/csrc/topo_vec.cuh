@@ -171,4 +171,46 @@ __global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T
   }
 }
 
+// up to kMaxMulti dot products against one vector: out[k] = V_k . w
+constexpr int kMaxMulti = 16;
+struct MultiCoef {
+  double c[kMaxMulti];
+};
+
+template <class TV, class TW>
+__global__ void k_multidot(const TV* __restrict__ V, size_t stride, int count, const TW* __restrict__ w, size_t n,
+                           double* partials, unsigned* counter, double* out) {
+  double v[kMaxMulti];
+  for (int k = 0; k < kMaxMulti; ++k) v[k] = 0.0;
+  TOPO_GRID_STRIDE(i, n) {
+    const double wi = double(w[i]);
+    for (int k = 0; k < count; ++k) v[k] += double(V[size_t(k) * stride + i]) * wi;
+  }
+  double tot[kMaxMulti];
+  if (finish_reduction<kMaxMulti>(v, partials, counter, tot))
+    for (int k = 0; k < count; ++k) out[k] = tot[k];
+}
+
+// w -= sum_k c_k V_k
+template <class TV, class TW>
+__global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t stride, int count, MultiCoef c,
+                            size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    double s = double(w[i]);
+    for (int k = 0; k < count; ++k) s -= c.c[k] * double(V[size_t(k) * stride + i]);
+    w[i] = TW(s);
+  }
+}
+
+// x += sum_k c_k Z_k
+template <class TZ, class TX>
+__global__ void k_add_multi(TX* __restrict__ x, const TZ* __restrict__ Z, size_t stride, int count, MultiCoef c,
+                            size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    double s = double(x[i]);
+    for (int k = 0; k < count; ++k) s += c.c[k] * double(Z[size_t(k) * stride + i]);
+    x[i] = TX(s);
+  }
+}
+
 }  // namespace topo

@@ -316,12 +316,12 @@ class ElasticityProblem(Problem):
 
     def calculate_objective(self, rho) -> float:
         """phi(rho) = int u.f dx + int u.t ds with u the state of the filtered rho."""
-        self.filtered_rho = self.filter.apply(rho)
-        self.stats["filter_iterations"] += self.filter.last_iterations
         try:
+            self.filtered_rho = self.filter.apply(rho)
+            self.stats["filter_iterations"] += self.filter.last_iterations
             self.u = self.forward(self.filtered_rho)
         except _capi.TopoError as e:
-            if e.code == _capi.TOPO_ERR_NAN:
+            if e.code == _capi.TOPO_ERR_NAN:   # the reference's solve returns NaN, Solver stops on it
                 return float("nan")
             raise
         return self.compliance(self.u)
