@@ -8,6 +8,7 @@
 // the FP64 oracle without a GPU.  It is never linked into the product library.
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <vector>
 
 #include "topo_mg.h"
@@ -42,16 +43,26 @@ void dir_to(const Dir& r, int* d) {
 }
 
 template <class T>
-void p2_run(const P2Params<T>& P, const T* xi, const T* u, T* y, int mode) {
+void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io) {
   auto s = std::make_unique<P2Smem<T>>();
   const int gx = (P.nx + P2_TX - 1) / P2_TX, gy = (P.ny + P2_TY - 1) / P2_TY;
   for (int by = 0; by < gy; ++by)
     for (int bx = 0; bx < gx; ++bx) {
       std::memset(s.get(), 0xff, sizeof(P2Smem<T>));  // poison: unwritten smem shows up as NaN
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::load(t, P2_THREADS, bx, by, P, mode == 1 ? nullptr : u, xi, *s);
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::compute(t, P2_THREADS, bx, by, P, *s, mode);
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::gather(t, P2_THREADS, bx, by, P, *s, u, y, mode);
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::load(t, P2_THREADS, bx, by, P, io, xi, *s);
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::compute(t, P2_THREADS, bx, by, P, *s, io.mode == kP2Diag ? 1 : 0);
+      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::gather(t, P2_THREADS, bx, by, P, *s, io);
     }
+}
+
+template <class T>
+void p2_run(const P2Params<T>& P, const T* xi, const T* u, T* y, int mode) {
+  P2Io<T> io;
+  std::memset(&io, 0, sizeof(io));
+  io.mode = mode == 1 ? kP2Diag : kP2Apply;
+  io.u = u;
+  io.y = y;
+  p2_run_io<T>(P, xi, io);
 }
 
 template <class T>
@@ -149,6 +160,72 @@ int emu_transfer(int NC, int NXf, int NYf, const int* dirf, int NXc, int NYc, co
       for (int I = 0; I < NXc; ++I)
         NC == 2 ? TransferKern<double, 2>::node_restrict(I, J, X, in, out)
                 : TransferKern<double, 1>::node_restrict(I, J, X, in, out);
+  }
+  return 0;
+}
+
+// fused smoothing steps (FP64).  bufs = {b, dinv, x, x2, r, d}; cheb = {c0, c1, c2};
+// level given by p2 (P2 lattice of nx x ny cells) or P1 (NC comps on nx x ny cells);
+// xc / dirc / NXc, NYc: the next coarser lattice (post1 source, resr target bc)
+int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, double lam, double mu, double p,
+               double pmin, const int* dir, const double* xi, const double* kK, double* const* bufs,
+               const double* cheb, int NXc, int NYc, const int* dirc, const double* xc, double* bc) {
+  SmoothBufs<double> B{bufs[0], bufs[1], bufs[2], bufs[3], bufs[4], bufs[5], cheb};
+  Transfer X;
+  X.NXf = p2 ? 2 * nx + 1 : nx + 1;
+  X.NYf = p2 ? 2 * ny + 1 : ny + 1;
+  X.NXc = NXc;
+  X.NYc = NYc;
+  X.dirf = dir_from(dir);
+  X.dirc = dir_from(dirc);
+  if (p2) {
+    auto P = p2params<double>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
+    P2Io<double> io;
+    std::memset(&io, 0, sizeof(io));
+    io.mode = mode;
+    io.u = bufs[2];
+    io.B = B;
+    io.xc = xc;
+    io.X = X;
+    p2_run_io<double>(P, xi, io);
+    return 0;
+  }
+  const ElemRefs R = make_elem_refs(hx, hy, lam, mu);
+  auto go = [&](auto& P, auto nc_tag) {
+    constexpr int K = decltype(nc_tag)::value;
+    P.nx = nx;
+    P.ny = ny;
+    P.dir = dir_from(dir);
+    for (int o = 0; o < 2; ++o) {
+      for (int a = 0; a < 3 * K; ++a)
+        for (int b = 0; b < 3 * K; ++b) P.K[o][a][b] = K == 2 ? R.K2[o][a][b] : R.K1[o][a][b];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) P.Mm[o][a][b] = R.M1[o][a][b];
+    }
+    P.kK = kK;
+    P.kM = nullptr;
+    P.kK_c = 0;
+    P.kM_c = K == 1 ? 1.0 : 0.0;
+    if (mode == kP2Res) {
+      for (int J = 0; J < NYc; ++J)
+        for (int I = 0; I < NXc; ++I) P1Smooth<double, K>::resr(I, J, P, B, X, bc);
+      return;
+    }
+    for (int b = 0; b <= ny; ++b)
+      for (int a = 0; a <= nx; ++a) {
+        if (mode == kP2Pre) P1Smooth<double, K>::pre(a, b, P, B);
+        else if (mode == kP2Post1) P1Smooth<double, K>::post1(a, b, P, B, xc, X);
+        else P1Smooth<double, K>::post2(a, b, P, B);
+      }
+  };
+  if (NC == 2) {
+    P1Params<double, 2> P;
+    std::memset(&P, 0, sizeof(P));
+    go(P, std::integral_constant<int, 2>{});
+  } else {
+    P1Params<double, 1> P;
+    std::memset(&P, 0, sizeof(P));
+    go(P, std::integral_constant<int, 1>{});
   }
   return 0;
 }

@@ -214,3 +214,67 @@ def test_level_chain_shapes():
     assert c["nx"] == 5 and c["dir"][2] == 5
     c2 = lv[3]                                        # 5 cells -> 3 (padded)
     assert c2["nx"] == 3 and c2["dir"][2] == 2
+
+
+@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1"])
+def test_fused_smoothing_steps_match_composition(level):
+    """PRE / RES(R) / POST1 / POST2 against the same steps composed from plain applies."""
+    nx, ny, hx, hy, p = 34, 10, 0.05, 0.05, 3.0
+    lam, mu = lame(1.0, 0.3)
+    rng = np.random.default_rng(21)
+    xi = rng.uniform(0.05, 1.0, (nx + 1) * (ny + 1))
+    p2 = level == "p2"
+    NC = 1 if level == "p1x1" else 2
+    if p2:
+        dirv = emu.make_dir(nx, ny, hx, hy, ["Left"])
+        lv = emu.build_levels(True, nx, ny, hx, hy, dirv, 2)
+        f, c = lv[0], lv[1]
+        A = lambda u: emu.p2_apply(nx, ny, hx, hy, lam, mu, p, dirv, xi, u)
+        kK = None
+    else:
+        dirv = emu.no_dir(nx + 1, ny + 1)
+        if NC == 2:
+            dirv[0] = 1
+        lv = emu.build_levels(False, nx, ny, hx, hy, dirv, NC)
+        f, c = lv[0], lv[1]
+        kK = emu.kappa(nx, ny, p, xi) if NC == 2 else np.full(2 * nx * ny, 0.05 ** 2)
+        A = lambda u: emu.p1_apply(NC, nx, ny, hx, hy, lam, mu, dirv, kK, None, u, kMc=1.0 if NC == 1 else 0.0)
+    n = NC * f["NX"] * f["NY"]
+    free = _free_rows(f["dir"], f["NX"], f["NY"], NC)
+    b = rng.standard_normal(n) * free
+    x = rng.standard_normal(n) * free
+    dinv = 1.0 / (A(np.ones(n)) * 0 + 1.0)        # any positive scaling is fine for the algebra
+    dinv = rng.uniform(0.5, 2.0, n)
+    dinv[~free] = 1.0
+    cheb = np.array([0.7, 0.3, 0.9])
+    bufs = dict(b=b.copy(), dinv=dinv.copy(), x=x.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
+    # PRE
+    emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    d0 = cheb[0] * dinv * b
+    ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
+    assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
+    # RES (P2) / RESR (P1)
+    bufs["x"] = x.copy()
+    cb = np.zeros(NC * c["NX"] * c["NY"])
+    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, c["NX"], c["NY"], c["dir"],
+               bc=cb)
+    rr = b - A(x)
+    if p2:
+        assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
+    else:
+        ref_c = emu.restrict(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], rr)
+        assert np.max(np.abs(cb - ref_c)) <= 1e-12 * np.max(np.abs(ref_c))
+    # POST1 then POST2
+    xc = rng.standard_normal(NC * c["NX"] * c["NY"]) * _free_rows(c["dir"], c["NX"], c["NY"], NC)
+    bufs["x"] = x.copy()
+    emu.smooth("post1", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, c["NX"], c["NY"], c["dir"],
+               xc=xc)
+    u = x + emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
+    r0 = b - A(u)
+    dd0 = cheb[0] * dinv * r0
+    assert np.max(np.abs(bufs["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
+    assert np.max(np.abs(bufs["x2"] - (u + dd0))) <= 1e-12 * np.max(np.abs(u))
+    emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    r1 = r0 - A(dd0)
+    ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
+    assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))

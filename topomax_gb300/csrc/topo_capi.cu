@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -61,6 +62,12 @@ __global__ void k_kappa_p2(int nx, int ny, Penal<double> pen, const double* __re
     for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
     kK[t] = tri_kappa(xe, pen);
   }
+}
+
+template <class T>
+__global__ void k_cell_rmass(int nx, int ny, Penal<double> pen, const double* __restrict__ xi, T* __restrict__ out) {
+  const size_t nc = size_t(nx) * ny;
+  TOPO_GRID_STRIDE(c, nc) cell_rmass<T>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
 }
 
 __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
@@ -227,6 +234,11 @@ struct topo_ctx {
   MG<float> smg32;
   MG<double> smg64;
   float* xi32 = nullptr;
+  // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
+  double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
+  double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
+  float* rm_op32 = nullptr;
+  float* rm_pc32 = nullptr;
   double* r64 = nullptr;
   double* y64 = nullptr;
   float* d32 = nullptr;
@@ -268,7 +280,7 @@ struct topo_ctx {
   int grid(size_t n) const { return vec_grid(n, sms); }
 
   template <class T>
-  P2Params<T> p2params(int clamp = 0) const {
+  P2Params<T> p2params(int clamp = 0, const T* rmass = nullptr) const {
     P2Params<T> P;
     std::memset(&P, 0, sizeof(P));
     P.nx = nx;
@@ -280,6 +292,7 @@ struct topo_ctx {
     P.mu2T = T(2.0 * mu * area);
     P.pen = make_penal<T>(p, pmin, clamp);
     P.dir = dir_p2;
+    P.rmass = rmass;
     return P;
   }
 
@@ -293,6 +306,11 @@ struct topo_ctx {
 
 namespace {
 
+
+bool graphs_enabled() {
+  const char* e = std::getenv("TOPO_GRAPHS");
+  return !(e && e[0] == '0');
+}
 
 int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
   if (!g || g->nx < 1 || g->ny < 1 || !(g->width > 0) || !(g->height > 0))
@@ -350,6 +368,7 @@ int init_filter(topo_ctx* C, double eps) {
   C->fy64 = C->arena.alloc_n<double>(C->nv);
   int st;
   if (C->precision == TOPO_PREC_MIXED) {
+    C->fmg32.use_graphs = graphs_enabled();
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg32.set_coefficients(kK, kM);
     C->fd32 = C->arena.alloc_n<float>(C->nv);
@@ -357,6 +376,7 @@ int init_filter(topo_ctx* C, double eps) {
     if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
     st = C->fmg32.setup(s);
   } else {
+    C->fmg64.use_graphs = graphs_enabled();
     C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg64.set_coefficients(kK, kM);
     if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
@@ -371,7 +391,7 @@ void filter_apply64(topo_ctx* C, const double* x, double* y, bool stiff, cudaStr
   auto P = make_p1<double, 1>(C->fspec[0], C->frefs[0], nullptr, nullptr);
   P.kK_c = stiff ? C->eps * C->eps : 0.0;
   P.kM_c = 1.0;
-  k_p1_apply<double, 1><<<C->grid(C->nv), kVecThreads, 0, s>>>(P, x, y);
+  k_p1_apply<double, 1><<<row_grid(C->nx + 1, C->ny + 1), kRowThreads, 0, s>>>(P, x, y);
 }
 
 // FP32 multigrid Krylov solves inside an FP64 flexible GMRES (right
@@ -396,9 +416,12 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
   float* r32 = mg.scratch0(4);
   double* hbuf = C->red.host;
   auto multidot = [&](int count, const double* w) {
-    k_multidot<double, double><<<C->red.blocks, kVecThreads, 0, s>>>(W.V, n, count, w, n, C->red.partials,
-                                                                     C->red.counter, C->red.out);
-    cudaMemcpyAsync(hbuf, C->red.out, count * sizeof(double), cudaMemcpyDeviceToHost, s);
+#define TOPO_MD(K)                                                                                            \
+  k_multidot<double, double, K><<<C->red.blocks, kVecThreads, 0, s>>>(W.V, n, w, n, C->red.partials, C->red.counter, \
+                                                                     C->red.out)
+    TOPO_DISPATCH_COUNT(count, TOPO_MD)
+#undef TOPO_MD
+    cudaMemcpyAsync(hbuf, C->red.out, (count + 1) * sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
   };
   double prev = 0.0;
@@ -428,21 +451,34 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       st.iterations += is.iterations;
       st.minres |= is.minres;
       if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
+      if (rc == -5) return C->fail(TOPO_ERR_CUDA, "inner solve: CUDA graph recording or launch failed");
       k_convert<double, float><<<g, kVecThreads, 0, s>>>(W.t, zj, 1.0, n);
       double* w = W.V + size_t(j + 1) * n;
       apply64(W.t, w, s);
-      // classical Gram-Schmidt, twice
+      // classical Gram-Schmidt; a second pass only when the first one cancelled
+      // more than half of w (Kahan's "twice is enough" test)
       double h[m + 1] = {};
+      double hn = 0.0;
       for (int pass = 0; pass < 2; ++pass) {
         multidot(j + 1, w);
         MultiCoef cf{};
+        double hh = 0.0;
         for (int i = 0; i <= j; ++i) {
           cf.c[i] = hbuf[i];
           h[i] += hbuf[i];
+          hh += hbuf[i] * hbuf[i];
         }
-        k_sub_multi<double, double><<<g, kVecThreads, 0, s>>>(w, W.V, n, j + 1, cf, n);
+        const double ww = hbuf[j + 1];
+#define TOPO_SM(K) k_sub_multi<double, double, K><<<g, kVecThreads, 0, s>>>(w, W.V, n, cf, n)
+        TOPO_DISPATCH_COUNT(j + 1, TOPO_SM)
+#undef TOPO_SM
+        const double est = ww - hh;
+        if (pass == 0 && est >= 0.5 * ww) {
+          hn = std::sqrt(est);
+          break;
+        }
+        if (pass == 1) hn = std::sqrt(C->dot64(w, w, n, s));
       }
-      const double hn = std::sqrt(C->dot64(w, w, n, s));
       if (!std::isfinite(hn)) return C->fail(TOPO_ERR_NAN, "non-finite Krylov vector");
       for (int i = 0; i <= j; ++i) H[i][j] = h[i];
       H[j + 1][j] = hn;
@@ -470,7 +506,9 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     }
     MultiCoef cf{};
     for (int i = 0; i < k; ++i) cf.c[i] = y[i];
-    k_add_multi<float, double><<<g, kVecThreads, 0, s>>>(x, W.Z, n, k, cf, n);
+#define TOPO_AM(K) k_add_multi<float, double, K><<<g, kVecThreads, 0, s>>>(x, W.Z, n, cf, n)
+    TOPO_DISPATCH_COUNT(k, TOPO_AM)
+#undef TOPO_AM
   }
   apply64(x, W.t, s);
   k_sub<double><<<g, kVecThreads, 0, s>>>(W.V, b, W.t, n);
@@ -488,6 +526,7 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   } else {
     rc = C->fmg64.pcg(b, xi, false, rtol, kFilterMaxIt, st, s);
     if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
+    else if (rc == -5) rc = C->fail(TOPO_ERR_CUDA, "filter solve: CUDA graph recording or launch failed");
     else if (rc) rc = C->fail(TOPO_ERR_NOT_CONVERGED, "filter CG did not converge (relres %.3g)", st.relres);
   }
   if (iters) *iters = st.iterations;
@@ -504,12 +543,18 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
     k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->skK[l - 1], F.nx, F.ny, C->skK[l], Cc.nx, Cc.ny);
   }
   int st;
+  const size_t ncell = size_t(C->nx) * C->ny;
+  const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
+  k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64);
   if (C->precision == TOPO_PREC_MIXED) {
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
-    C->smg32.set_p2(C->p2params<float>(0), C->p2params<float>(1), C->xi32);
+    k_convert<float, double><<<C->grid(12 * ncell), kVecThreads, 0, s>>>(C->rm_op32, C->rm_op64, 1.0, 12 * ncell);
+    k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc32);
+    C->smg32.set_p2(C->p2params<float>(0, C->rm_op32), C->p2params<float>(1, C->rm_pc32), C->xi32);
     st = C->smg32.setup(s);
   } else {
-    C->smg64.set_p2(C->p2params<double>(0), C->p2params<double>(1), xi);
+    k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc64);
+    C->smg64.set_p2(C->p2params<double>(0, C->rm_op64), C->p2params<double>(1, C->rm_pc64), xi);
     st = C->smg64.setup(s);
   }
   if (st == -5) return C->fail(TOPO_ERR_CUDA, "state set-up: CUDA error");
@@ -586,17 +631,27 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       }
       std::vector<const double*> kK(C->skK.begin(), C->skK.end()), kM(L, nullptr);
       const size_t n = 2 * C->nn2;
+      const size_t ncell = size_t(C->nx) * C->ny;
+      C->rm_op64 = C->arena.alloc_n<double>(12 * ncell);
+      if (precision == TOPO_PREC_MIXED) {
+        C->rm_op32 = C->arena.alloc_n<float>(12 * ncell);
+        C->rm_pc32 = C->arena.alloc_n<float>(12 * ncell);
+      } else {
+        C->rm_pc64 = C->arena.alloc_n<double>(12 * ncell);
+      }
       C->r64 = C->arena.alloc_n<double>(n);
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
-        C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg32.use_graphs = graphs_enabled();
+    C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg32.set_coefficients(kK, kM);
         C->xi32 = C->arena.alloc_n<float>(C->nv);
         C->d32 = C->arena.alloc_n<float>(n);
         C->sgm.init(C->arena, n);
         C->sens_tri = C->arena.alloc_n<float>(size_t(3) * C->sspec[0].ntri());
       } else {
-        C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg64.use_graphs = graphs_enabled();
+    C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg64.set_coefficients(kK, kM);
         C->sens_tri = C->arena.alloc_n<double>(size_t(3) * C->sspec[0].ntri());
       }
@@ -688,12 +743,13 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
     SolveStats st;
     if (ctx->precision == TOPO_PREC_MIXED) {
-      P2Params<double> P64 = ctx->p2params<double>();
+      P2Params<double> P64 = ctx->p2params<double>(0, ctx->rm_op64);
       auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
       rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, kStateMaxIt, st, s);
     } else {
       rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, kStateMaxIt, st, s);
       if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");
+      else if (rc == -5) rc = ctx->fail(TOPO_ERR_CUDA, "state solve: CUDA graph recording or launch failed");
       else if (rc) rc = ctx->fail(TOPO_ERR_NOT_CONVERGED, "state CG did not converge (relres %.3g)", st.relres);
     }
     if (iters) *iters = st.iterations;

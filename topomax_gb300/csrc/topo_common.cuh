@@ -146,6 +146,21 @@ TOPO_HD constexpr int gys() {
   return O == 0 ? (I == 0 ? 0 : (I == 1 ? -1 : 1)) : (I == 0 ? -1 : (I == 1 ? 1 : 0));
 }
 
+// Compile-time local offsets (used in the kernels' inner loops so no table is
+// indexed at run time).
+template <int O, int K>
+struct P2Off {
+  static constexpr int a = O == 0 ? (K == 0 ? 0 : K == 1 ? 2 : K == 2 ? 2 : K == 3 ? 2 : 1)
+                                  : (K == 0 ? 0 : K == 1 ? 0 : K == 2 ? 2 : K == 3 ? 1 : K == 4 ? 1 : 0);
+  static constexpr int b = O == 0 ? (K == 0 ? 0 : K == 1 ? 0 : K == 2 ? 2 : K == 3 ? 1 : K == 4 ? 1 : 0)
+                                  : (K == 0 ? 0 : K == 1 ? 2 : K == 2 ? 2 : K == 3 ? 2 : 1);
+};
+template <int O, int K>
+struct P1Off {
+  static constexpr int a = O == 0 ? (K == 0 ? 0 : 1) : (K == 2 ? 1 : 0);
+  static constexpr int b = O == 0 ? (K == 2 ? 1 : 0) : (K == 0 ? 0 : 1);
+};
+
 // Local P2 node offsets (da,db) inside a square, order [A,B,C,mid(BC),mid(AC),mid(AB)].
 TOPO_HD int p2_off_a(int o, int k) {
   const int t[2][6] = {{0, 2, 2, 2, 1, 1}, {0, 0, 2, 1, 1, 0}};

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -17,7 +18,7 @@
 
 namespace topo {
 
-constexpr int kCoarseMaxDofs = 64;
+constexpr int kCoarseMaxDofs = 32;
 
 // Device memory owner: everything allocated here is freed with the arena.
 class Arena {
@@ -60,6 +61,7 @@ struct ElemRefs {
   double M1[2][3][3];  // mass
 };
 ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu);
+double p1_elasticity_bound(const ElemRefs& R);
 
 // Reduction scratch shared by one stream.
 struct Reducer {
@@ -70,6 +72,13 @@ struct Reducer {
   int sms = 148;
   int blocks = 0;
   void init(Arena& a, int sms);
+};
+
+// Device-resident scalars of one preconditioned-CG solve (read back once at the end).
+struct PcgDev {
+  double bb, rz, pq, beta, tol2, relres;
+  double rr, rz_new;  // adjacent: one two-value reduction writes both
+  int it, maxit, status, pad;  // status: 0 converged, 1 running, 2 iteration cap, 3 breakdown, 4 non-finite, 5 zero rhs
 };
 
 struct SolveStats {
@@ -91,10 +100,17 @@ class MG {
   // preconditioner's operator (penalisation clamped at its minimum, SPD);
   // xi points to the design in precision T
   void set_p2(const P2Params<T>& op, const P2Params<T>& pc, const T* xi) {
+    // kernel parameters are baked into the captured solve graphs
+    if (std::memcmp(&op, &p2_op_, sizeof(op)) || std::memcmp(&pc, &p2_, sizeof(pc)) || xi != xi_)
+      graph_valid_ = false;
     p2_op_ = op;
     p2_ = pc;
     xi_ = xi;
   }
+  MG() = default;
+  MG(const MG&) = delete;
+  MG& operator=(const MG&) = delete;
+  ~MG();
   // kK/kM masters per level (entries for P2 level ignored; nullptr allowed)
   void set_coefficients(const std::vector<const double*>& kK, const std::vector<const double*>& kM) {
     kK64_ = kK;
@@ -119,23 +135,30 @@ class MG {
   T* scratch0(int k) { return pcg_[k]; }
   static constexpr int kScratch = 9;
 
-  int cheb_degree = 2;
+  int cheb_degree = 2;  // the fused smoothing kernels implement degree 2
   double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
-  int power_iters = 12;
+  int power_iters = 10;
+  // kernels launched by this object since construction (graph nodes counted per execution)
+  long long launches = 0;
+  // record the CG loop as a CUDA graph with a device-side WHILE node (default);
+  // false runs the same kernels from a host loop
+  bool use_graphs = true;
 
  private:
   struct Lev {
-    T *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *t = nullptr;
+    T *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *t = nullptr, *x2 = nullptr;
     T* diag = nullptr;
     T* dinv = nullptr;
     T* kK = nullptr;
     T* kM = nullptr;
     double lmax = 1.0;
+    bool bound = false;  // lmax is a guaranteed upper bound (no safety factor)
   };
-  void vcycle_level(int l, cudaStream_t s);
-  void smooth(int l, const T* b, T* x, bool xzero, cudaStream_t s);
-  void restrict_to(int l, const T* rf, T* bc, cudaStream_t s);
-  void prolong_add(int l, const T* xc, T* xf, cudaStream_t s);
+  void vcycle_level(int l, const T* b, T* x, cudaStream_t s);
+  int capture_pcg(bool warm);
+  void pcg_prologue(bool warm, cudaStream_t s);
+  void pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond);
+  int graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s);
   double dot(const T* a, const T* b, size_t n, cudaStream_t s);  // synchronising
   void diag_of(int l, T* d, cudaStream_t s);
   double estimate_lmax(int l, cudaStream_t s);
@@ -150,6 +173,16 @@ class MG {
   const T* xi_ = nullptr;
   T* cinv_ = nullptr;  // dense coarsest inverse
   int* cstat_ = nullptr;
+  double* cheb_ = nullptr;  // Chebyshev coefficients, 8 per level (device)
+  PcgDev* dev_ = nullptr;   // device scalars of the graph solve
+  PcgDev* hdev_ = nullptr;  // pinned mirror
+  cudaStream_t cap_[2] = {nullptr, nullptr};  // owned streams: graph recording only
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    long long prologue_nodes = 0, body_nodes = 0;
+  } graph_[2];
+  bool graph_valid_ = false;
+
   T* pcg_[kScratch] = {};
   Reducer* red_ = nullptr;
   int sms_ = 148;

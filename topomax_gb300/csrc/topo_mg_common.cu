@@ -1,5 +1,6 @@
 // Precision-independent parts of the multigrid set-up.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "topo_mg.h"
@@ -140,6 +141,52 @@ ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu) {
       }
   }
   return R;
+}
+
+// Largest eigenvalue of the symmetric n x n matrix A (cyclic Jacobi rotations).
+static double sym_eig_max(std::vector<double> A, int n) {
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += A[p * n + q] * A[p * n + q];
+    if (off < 1e-30) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - sn * akq;
+          A[k * n + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - sn * aqk;
+          A[q * n + k] = sn * apk + c * aqk;
+        }
+      }
+  }
+  double m = A[0];
+  for (int k = 1; k < n; ++k) m = std::max(m, A[k * n + k]);
+  return m;
+}
+
+// max over orientations of lambda_max(D_e^-1 K_e) for the unit-coefficient P1
+// elasticity element: since lambda_max(D^-1 A) <= max_e lambda_max(D_e^-1 A_e)
+// and a per-triangle coefficient cancels in D_e^-1 A_e, this bounds every P1
+// elasticity level whatever its coefficients.
+double p1_elasticity_bound(const ElemRefs& R) {
+  double m = 1.0;
+  for (int o = 0; o < 2; ++o) {
+    std::vector<double> A(36);
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) A[i * 6 + j] = R.K2[o][i][j] / std::sqrt(R.K2[o][i][i] * R.K2[o][j][j]);
+    m = std::max(m, sym_eig_max(A, 6));
+  }
+  return m;
 }
 
 void Reducer::init(Arena& a, int nsms) {

@@ -16,55 +16,59 @@ namespace topo {
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
+// Lattice kernels use a 2D grid: blockIdx.y is the row, x covers the columns.
+constexpr int kRowThreads = 128;
+#define kRowThreads_ 128
+inline dim3 row_grid(int NX, int NY) { return dim3((NX + kRowThreads - 1) / kRowThreads, NY); }
+
+// The tiled P2 kernel: load the operand tile, per-triangle element work,
+// gather onto owned nodes with the mode's epilogue (apply, diagonal or one of
+// the fused Chebyshev smoothing steps).
 template <class T>
 __global__ void __launch_bounds__(P2_THREADS)
-    k_p2_apply(P2Params<T> P, const T* __restrict__ xi, const T* __restrict__ u, T* __restrict__ y) {
+    k_p2_tile(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& s = *reinterpret_cast<P2Smem<T>*>(smem_raw);
-  P2Kern<T>::load(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, u, xi, s);
+  P2Kern<T>::load(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, io, xi, s);
   __syncthreads();
-  P2Kern<T>::compute(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, 0);
+  P2Kern<T>::compute(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, io.mode == kP2Diag ? 1 : 0);
   __syncthreads();
-  P2Kern<T>::gather(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, u, y, 0);
+  P2Kern<T>::gather(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, io);
 }
 
-template <class T>
-__global__ void __launch_bounds__(P2_THREADS)
-    k_p2_diag(P2Params<T> P, const T* __restrict__ xi, T* __restrict__ d) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& s = *reinterpret_cast<P2Smem<T>*>(smem_raw);
-  P2Kern<T>::load(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, nullptr, xi, s);
-  __syncthreads();
-  P2Kern<T>::compute(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, 1);
-  __syncthreads();
-  P2Kern<T>::gather(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, nullptr, d, 1);
+template <class T, int NC, int MODE>
+__global__ void __launch_bounds__(kRowThreads_)
+    k_p1_smooth(P1Params<T, NC> P, SmoothBufs<T> B, const T* __restrict__ xc, Transfer X, T* __restrict__ bc) {
+  const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
+  if (MODE == 3) {  // residual + restriction, grid over coarse nodes
+    if (a < X.NXc) P1Smooth<T, NC>::resr(a, b, P, B, X, bc);
+    return;
+  }
+  if (a > P.nx) return;
+  if (MODE == 2) P1Smooth<T, NC>::pre(a, b, P, B);
+  else if (MODE == 4) P1Smooth<T, NC>::post1(a, b, P, B, xc, X);
+  else P1Smooth<T, NC>::post2(a, b, P, B);
 }
 
 template <class T, int NC>
-__global__ void k_p1_apply(P1Params<T, NC> P, const T* __restrict__ u, T* __restrict__ y) {
-  const int NX = P.nx + 1, NY = P.ny + 1;
-  const size_t nn = size_t(NX) * NY;
-  TOPO_GRID_STRIDE(n, nn) P1Kern<T, NC>::node_apply(int(n % NX), int(n / NX), P, u, y);
+__global__ void __launch_bounds__(kRowThreads) k_p1_apply(P1Params<T, NC> P, const T* __restrict__ u, T* __restrict__ y) {
+  const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
+  if (a <= P.nx) P1Kern<T, NC>::node_apply(a, b, P, u, y);
 }
 
 template <class T, int NC>
-__global__ void k_p1_diag(P1Params<T, NC> P, T* __restrict__ d) {
-  const int NX = P.nx + 1, NY = P.ny + 1;
-  const size_t nn = size_t(NX) * NY;
-  TOPO_GRID_STRIDE(n, nn) P1Kern<T, NC>::node_diag(int(n % NX), int(n / NX), P, d);
+__global__ void __launch_bounds__(kRowThreads) k_p1_diag(P1Params<T, NC> P, T* __restrict__ d) {
+  const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
+  if (a <= P.nx) P1Kern<T, NC>::node_diag(a, b, P, d);
 }
 
 template <class T, int NC>
-__global__ void k_restrict(Transfer X, const T* __restrict__ rf, T* __restrict__ bc) {
-  const size_t nn = size_t(X.NXc) * X.NYc;
-  TOPO_GRID_STRIDE(n, nn) TransferKern<T, NC>::node_restrict(int(n % X.NXc), int(n / X.NXc), X, rf, bc);
+__global__ void __launch_bounds__(kRowThreads) k_restrict(Transfer X, const T* __restrict__ rf, T* __restrict__ bc,
+                                                          const T* __restrict__ tf) {
+  const int I = blockIdx.x * kRowThreads + threadIdx.x, J = blockIdx.y;
+  if (I < X.NXc) TransferKern<T, NC>::node_restrict(I, J, X, rf, bc, tf);
 }
 
-template <class T, int NC>
-__global__ void k_prolong_add(Transfer X, const T* __restrict__ xc, T* __restrict__ xf) {
-  const size_t nn = size_t(X.NXf) * X.NYf;
-  TOPO_GRID_STRIDE(n, nn) TransferKern<T, NC>::node_prolong_add(int(n % X.NXf), int(n / X.NXf), X, xc, xf);
-}
 
 // deterministic pseudo-random start vector for the power iteration
 template <class T>
@@ -162,17 +166,26 @@ template <class T>
 inline void set_p2_smem_attr() {
   static bool done = false;
   if (!done) {
-    cudaFuncSetAttribute(k_p2_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(P2Smem<T>)));
-    cudaFuncSetAttribute(k_p2_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(P2Smem<T>)));
+    cudaFuncSetAttribute(k_p2_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(P2Smem<T>)));
     done = true;
   }
 }
 
 template <class T>
-inline void launch_p2_apply(const P2Params<T>& P, const T* xi, const T* x, T* y, cudaStream_t s) {
+inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
   set_p2_smem_attr<T>();
   dim3 g((P.nx + P2_TX - 1) / P2_TX, (P.ny + P2_TY - 1) / P2_TY);
-  k_p2_apply<T><<<g, P2_THREADS, sizeof(P2Smem<T>), s>>>(P, xi, x, y);
+  k_p2_tile<T><<<g, P2_THREADS, sizeof(P2Smem<T>), s>>>(P, xi, io);
+}
+
+template <class T>
+inline void launch_p2_apply(const P2Params<T>& P, const T* xi, const T* x, T* y, cudaStream_t s) {
+  P2Io<T> io;
+  std::memset(&io, 0, sizeof(io));
+  io.mode = kP2Apply;
+  io.u = x;
+  io.y = y;
+  launch_p2_tile<T>(P, xi, io, s);
 }
 
 template <class T, int NC>
@@ -207,8 +220,71 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 }
 
 // ---------------------------------------------------------------------------
+// graph-resident CG scalars
+// ---------------------------------------------------------------------------
+// x += alpha p ; r -= alpha q with alpha = rz / pq read from device memory
+template <class T>
+__global__ void k_pcg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+                         const PcgDev* __restrict__ dv, size_t n) {
+  const double pq = dv->pq;
+  if (!(pq > 0.0) || !isfinite(pq)) return;
+  const T alpha = T(dv->rz / pq);
+  TOPO_GRID_STRIDE(i, n) {
+    x[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
+}
+
+// p = z + beta p
+template <class T>
+__global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, const PcgDev* __restrict__ dv, size_t n) {
+  const T beta = T(dv->beta);
+  TOPO_GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
+}
+
+// after the prologue: decide whether the loop runs at all.  On entry dv->tol2
+// holds rtol^2 and dv->maxit the iteration cap (both written by the host).
+static __global__ void k_pcg_start(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
+  const double bb = dv->bb, rr = dv->rr;
+  dv->tol2 = dv->tol2 * bb;
+  dv->it = 0;
+  dv->relres = bb > 0 ? sqrt(rr / bb) : 0.0;
+  int st = 1;
+  if (!isfinite(bb) || !isfinite(rr) || !isfinite(dv->rz)) st = 4;
+  else if (bb == 0.0) st = 5;
+  else if (rr <= dv->tol2) st = 0;
+  dv->status = st;
+  if (use_cond) cudaGraphSetConditional(h, st == 1 ? 1u : 0u);
+}
+
+// end of one iteration: convergence / cap / breakdown test and beta
+static __global__ void k_pcg_check(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
+  dv->it += 1;
+  const double pq = dv->pq, rr = dv->rr, rzn = dv->rz_new;
+  dv->relres = sqrt(rr / dv->bb);
+  int st = 1;
+  if (!isfinite(pq) || !isfinite(rr) || !isfinite(rzn)) st = 4;
+  else if (!(pq > 0.0) || !(dv->rz > 0.0)) st = 3;
+  else if (rr <= dv->tol2) st = 0;
+  else if (dv->it >= dv->maxit) st = 2;
+  dv->beta = (st == 1) ? rzn / dv->rz : 0.0;
+  dv->rz = rzn;
+  dv->status = st;
+  if (use_cond) cudaGraphSetConditional(h, st == 1 ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
 // MG<T>
 // ---------------------------------------------------------------------------
+template <class T>
+MG<T>::~MG() {
+  for (auto& g : graph_)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  for (auto c : cap_)
+    if (c) cudaStreamDestroy(c);
+  if (hdev_) cudaFreeHost(hdev_);
+}
+
 template <class T>
 void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, double lmbda, double mu,
                  Arena& arena, Reducer* red) {
@@ -222,11 +298,14 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   for (size_t l = 0; l < specs.size(); ++l) {
     const size_t n = specs[l].ndof();
     Lev& v = lv_[l];
-    v.x = arena.alloc_n<T>(n);
-    v.b = arena.alloc_n<T>(n);
+    if (l > 0) {
+      v.x = arena.alloc_n<T>(n);
+      v.b = arena.alloc_n<T>(n);
+    }
     v.r = arena.alloc_n<T>(n);
     v.d = arena.alloc_n<T>(n);
     v.t = arena.alloc_n<T>(n);
+    v.x2 = arena.alloc_n<T>(n);
     v.diag = arena.alloc_n<T>(n);
     v.dinv = arena.alloc_n<T>(n);
     if (!specs[l].p2) {
@@ -239,46 +318,58 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   const int nc = int(specs.back().ndof());
   cinv_ = arena.alloc_n<T>(size_t(nc) * nc);
   cstat_ = arena.alloc_n<int>(1);
+  cheb_ = arena.alloc_n<double>(8 * specs.size());
+  dev_ = arena.alloc_n<PcgDev>(1);
+  if (!hdev_) cudaMallocHost(&hdev_, sizeof(PcgDev));
+  for (auto& c : cap_)
+    if (!c) cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
+  set_p2_smem_attr<T>();
+  graph_valid_ = false;
 }
 
 template <class T>
 void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   const LevelSpec& L = specs_[l];
+  ++launches;
   if (L.p2) {
     launch_p2_apply<T>(op ? p2_op_ : p2_, xi_, x, y, s);
     return;
   }
-  const int g = vec_grid(L.nn(), sms_);
+  const dim3 g = row_grid(L.NX, L.NY);
   if (L.NC == 2) {
     auto P = make_p1<T, 2>(L, refs_[l], lv_[l].kK, nullptr);
-    k_p1_apply<T, 2><<<g, kVecThreads, 0, s>>>(P, x, y);
+    k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(P, x, y);
   } else {
     auto P = make_p1<T, 1>(L, refs_[l], lv_[l].kK, lv_[l].kM);
-    k_p1_apply<T, 1><<<g, kVecThreads, 0, s>>>(P, x, y);
+    k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(P, x, y);
   }
 }
 
 template <class T>
 void MG<T>::diag_of(int l, T* d, cudaStream_t s) {
   const LevelSpec& L = specs_[l];
+  ++launches;
   if (L.p2) {
-    set_p2_smem_attr<T>();
-    dim3 g((L.nx + P2_TX - 1) / P2_TX, (L.ny + P2_TY - 1) / P2_TY);
-    k_p2_diag<T><<<g, P2_THREADS, sizeof(P2Smem<T>), s>>>(p2_, xi_, d);
+    P2Io<T> io;
+    std::memset(&io, 0, sizeof(io));
+    io.mode = kP2Diag;
+    io.y = d;
+    launch_p2_tile<T>(p2_, xi_, io, s);
     return;
   }
-  const int g = vec_grid(L.nn(), sms_);
+  const dim3 g = row_grid(L.NX, L.NY);
   if (L.NC == 2) {
     auto P = make_p1<T, 2>(L, refs_[l], lv_[l].kK, nullptr);
-    k_p1_diag<T, 2><<<g, kVecThreads, 0, s>>>(P, d);
+    k_p1_diag<T, 2><<<g, kRowThreads, 0, s>>>(P, d);
   } else {
     auto P = make_p1<T, 1>(L, refs_[l], lv_[l].kK, lv_[l].kM);
-    k_p1_diag<T, 1><<<g, kVecThreads, 0, s>>>(P, d);
+    k_p1_diag<T, 1><<<g, kRowThreads, 0, s>>>(P, d);
   }
 }
 
 template <class T>
 double MG<T>::dot(const T* a, const T* b, size_t n, cudaStream_t s) {
+  ++launches;
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(a, b, n, red_->partials, red_->counter, red_->out);
   cudaMemcpyAsync(red_->host, red_->out, sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
@@ -290,20 +381,25 @@ double MG<T>::estimate_lmax(int l, cudaStream_t s) {
   const size_t n = specs_[l].ndof();
   const int g = vec_grid(n, sms_);
   Lev& v = lv_[l];
-  k_power_start<T><<<g, kVecThreads, 0, s>>>(v.x, n);
+  T* x = v.r;
+  T* y = v.d;
+  k_power_start<T><<<g, kVecThreads, 0, s>>>(x, n);
   for (int it = 0; it < power_iters; ++it) {
-    apply(l, v.x, v.t, s);
-    k_mul<T><<<g, kVecThreads, 0, s>>>(v.x, v.dinv, v.t, n);
+    apply(l, x, y, s);
+    k_mul<T><<<g, kVecThreads, 0, s>>>(x, v.dinv, y, n);
+    launches += 1;
     if (it % 4 == 3) {  // rescale to stay in range
-      const double nrm = std::sqrt(dot(v.x, v.x, n, s));
+      const double nrm = std::sqrt(dot(x, x, n, s));
       if (!(nrm > 0) || !std::isfinite(nrm)) return 4.0;
-      k_scale<T><<<g, kVecThreads, 0, s>>>(v.x, T(1.0 / nrm), n);
+      k_scale<T><<<g, kVecThreads, 0, s>>>(x, T(1.0 / nrm), n);
+      launches += 1;
     }
   }
-  apply(l, v.x, v.t, s);
-  const double num = dot(v.x, v.t, n, s);
-  k_mul<T><<<g, kVecThreads, 0, s>>>(v.r, v.diag, v.x, n);
-  const double den = dot(v.x, v.r, n, s);
+  apply(l, x, y, s);
+  const double num = dot(x, y, n, s);
+  k_mul<T><<<g, kVecThreads, 0, s>>>(v.t, v.diag, x, n);
+  launches += 2;
+  const double den = dot(x, v.t, n, s);
   double lam = (den > 0) ? num / den : 4.0;
   if (!std::isfinite(lam) || lam <= 0) lam = 4.0;
   return lam;
@@ -319,6 +415,7 @@ int MG<T>::setup(cudaStream_t s) {
       const int g = vec_grid(S.ntri(), sms_);
       k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kK, kK64_[l], 1.0, S.ntri());
       if (v.kM) k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kM, kM64_[l], 1.0, S.ntri());
+      launches += v.kM ? 2 : 1;
     }
   }
   for (int l = 0; l < L; ++l) {
@@ -327,14 +424,38 @@ int MG<T>::setup(cudaStream_t s) {
     diag_of(l, lv_[l].diag, s);
     k_convert<T, T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, lv_[l].diag, 1.0, n);
     k_recip<T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, n);
+    launches += 2;
   }
-  for (int l = 0; l + 1 < L; ++l) lv_[l].lmax = estimate_lmax(l, s);
+  std::vector<double> cc(8 * L, 0.0);
+  for (int l = 0; l + 1 < L; ++l) {
+    const LevelSpec& S = specs_[l];
+    if (!S.p2 && S.NC == 2) {
+      lv_[l].lmax = p1_elasticity_bound(refs_[l]);
+      lv_[l].bound = true;
+    } else {
+      lv_[l].lmax = estimate_lmax(l, s);
+      lv_[l].bound = false;
+    }
+    const double hi = (lv_[l].bound ? 1.0 : 1.1) * lv_[l].lmax, lo = cheb_lo_frac * lv_[l].lmax;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    double* c = cc.data() + 8 * l;
+    c[0] = 1.0 / theta;
+    double rho_old = 1.0 / sigma;
+    for (int k = 1; k < cheb_degree && k < 4; ++k) {
+      const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+      c[2 * k - 1] = rho_new * rho_old;
+      c[2 * k] = 2.0 * rho_new / delta;
+      rho_old = rho_new;
+    }
+  }
+  cudaMemcpyAsync(cheb_, cc.data(), cc.size() * sizeof(double), cudaMemcpyHostToDevice, s);
   const LevelSpec& C = specs_[L - 1];
   if (C.NC == 2)
     k_coarse_inverse<T, 2><<<1, 256, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
   else
     k_coarse_inverse<T, 1><<<1, 256, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], kM64_[L - 1], cinv_,
                                              cstat_);
+  launches += 1;
   int st = 0;
   cudaMemcpyAsync(&st, cstat_, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamSynchronize(s);
@@ -342,136 +463,256 @@ int MG<T>::setup(cudaStream_t s) {
   return st ? -2 : 0;
 }
 
+// One V-cycle from level l down: fused degree-2 Chebyshev pre-smoothing from
+// x = 0, residual restriction, coarse correction, fused post-smoothing.
 template <class T>
-void MG<T>::smooth(int l, const T* b, T* x, bool xzero, cudaStream_t s) {
-  Lev& v = lv_[l];
-  const size_t n = specs_[l].ndof();
-  const int g = vec_grid(n, sms_);
-  const double hi = 1.1 * v.lmax, lo = cheb_lo_frac * v.lmax;
-  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
-  const double sigma = theta / delta;
-  if (xzero) {
-    cudaMemcpyAsync(v.r, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
-  } else {
-    apply(l, x, v.t, s);
-    k_sub<T><<<g, kVecThreads, 0, s>>>(v.r, b, v.t, n);
-  }
-  k_cheb_first<T><<<g, kVecThreads, 0, s>>>(v.r, v.dinv, v.d, x, T(1.0 / theta), xzero ? 1 : 0, n);
-  double rho_old = 1.0 / sigma;
-  for (int k = 1; k < cheb_degree; ++k) {
-    apply(l, v.d, v.t, s);
-    const double rho_new = 1.0 / (2.0 * sigma - rho_old);
-    k_cheb_next<T><<<g, kVecThreads, 0, s>>>(v.r, v.t, v.dinv, v.d, x, T(rho_new * rho_old),
-                                             T(2.0 * rho_new / delta), n);
-    rho_old = rho_new;
-  }
-}
-
-template <class T>
-void MG<T>::restrict_to(int l, const T* rf, T* bc, cudaStream_t s) {
-  const Transfer X = make_transfer(specs_[l], specs_[l + 1]);
-  const int g = vec_grid(specs_[l + 1].nn(), sms_);
-  if (specs_[l].NC == 2) k_restrict<T, 2><<<g, kVecThreads, 0, s>>>(X, rf, bc);
-  else k_restrict<T, 1><<<g, kVecThreads, 0, s>>>(X, rf, bc);
-}
-
-template <class T>
-void MG<T>::prolong_add(int l, const T* xc, T* xf, cudaStream_t s) {
-  const Transfer X = make_transfer(specs_[l], specs_[l + 1]);
-  const int g = vec_grid(specs_[l].nn(), sms_);
-  if (specs_[l].NC == 2) k_prolong_add<T, 2><<<g, kVecThreads, 0, s>>>(X, xc, xf);
-  else k_prolong_add<T, 1><<<g, kVecThreads, 0, s>>>(X, xc, xf);
-}
-
-template <class T>
-void MG<T>::vcycle_level(int l, cudaStream_t s) {
+void MG<T>::vcycle_level(int l, const T* b, T* x, cudaStream_t s) {
   Lev& v = lv_[l];
   const int L = levels();
+  const LevelSpec& S = specs_[l];
   if (l == L - 1) {
-    const int n = int(specs_[l].ndof());
-    k_dense_matvec<T><<<1, 256, 0, s>>>(cinv_, v.b, v.x, n);
+    k_dense_matvec<T><<<1, 256, 0, s>>>(cinv_, b, x, int(S.ndof()));
+    ++launches;
     return;
   }
-  const size_t n = specs_[l].ndof();
-  const int g = vec_grid(n, sms_);
-  smooth(l, v.b, v.x, true, s);
-  apply(l, v.x, v.t, s);
-  k_sub<T><<<g, kVecThreads, 0, s>>>(v.r, v.b, v.t, n);
-  restrict_to(l, v.r, lv_[l + 1].b, s);
-  vcycle_level(l + 1, s);
-  prolong_add(l, lv_[l + 1].x, v.x, s);
-  smooth(l, v.b, v.x, false, s);
+  SmoothBufs<T> B{b, v.dinv, x, v.x2, v.r, v.d, cheb_ + 8 * l};
+  const Transfer X = make_transfer(S, specs_[l + 1]);
+  Lev& c = lv_[l + 1];
+  if (S.p2) {
+    P2Io<T> io;
+    std::memset(&io, 0, sizeof(io));
+    io.B = B;
+    io.mode = kP2Pre;
+    launch_p2_tile<T>(p2_, xi_, io, s);
+    io.mode = kP2Res;
+    io.u = x;
+    launch_p2_tile<T>(p2_, xi_, io, s);
+    k_restrict<T, 2><<<row_grid(X.NXc, X.NYc), kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launches += 3;
+    vcycle_level(l + 1, c.b, c.x, s);
+    io.mode = kP2Post1;
+    io.xc = c.x;
+    io.X = X;
+    launch_p2_tile<T>(p2_, xi_, io, s);
+    io.mode = kP2Post2;
+    launch_p2_tile<T>(p2_, xi_, io, s);
+    launches += 2;
+    return;
+  }
+  const dim3 gf = row_grid(S.NX, S.NY), gc = row_grid(X.NXc, X.NYc);
+  auto run = [&](auto nc_tag) {
+    constexpr int NC = decltype(nc_tag)::value;
+    const auto P = make_p1<T, NC>(S, refs_[l], v.kK, NC == 1 ? v.kM : nullptr);
+    k_p1_smooth<T, NC, 2><<<gf, kRowThreads, 0, s>>>(P, B, nullptr, X, nullptr);
+    k_p1_smooth<T, NC, 3><<<gc, kRowThreads, 0, s>>>(P, B, nullptr, X, c.b);
+    launches += 2;
+    vcycle_level(l + 1, c.b, c.x, s);
+    k_p1_smooth<T, NC, 4><<<gf, kRowThreads, 0, s>>>(P, B, c.x, X, nullptr);
+    k_p1_smooth<T, NC, 5><<<gf, kRowThreads, 0, s>>>(P, B, nullptr, X, nullptr);
+    launches += 2;
+  };
+  if (S.NC == 2) run(std::integral_constant<int, 2>{});
+  else run(std::integral_constant<int, 1>{});
 }
 
 template <class T>
 void MG<T>::vcycle(const T* b, T* x, cudaStream_t s) {
+  vcycle_level(0, b, x, s);
+}
+
+// Records the CG solve into a graph: a prologue (initial residual, first
+// preconditioned direction, start test) followed by a WHILE conditional node
+// whose body is one CG iteration; the body's last kernel decides whether the
+// loop continues, so the solve runs without host round trips.  The loop is
+// bounded by maxit (checked on the device).  Recording happens on two streams
+// owned by this object (capture is not possible on the legacy default stream);
+// every graph call is checked and nothing is launched unless all succeeded.
+template <class T>
+void MG<T>::pcg_prologue(bool warm, cudaStream_t s) {
   const size_t n = specs_[0].ndof();
-  cudaMemcpyAsync(lv_[0].b, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
-  vcycle_level(0, s);
-  cudaMemcpyAsync(x, lv_[0].x, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  const int g = vec_grid(n, sms_);
+  T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3], *bi = pcg_[5], *xi = pcg_[6];
+  if (warm) {
+    apply(0, xi, q, s, true);
+    k_sub<T><<<g, kVecThreads, 0, s>>>(r, bi, q, n);
+  } else {
+    k_fill<T><<<g, kVecThreads, 0, s>>>(xi, T(0), n);
+    cudaMemcpyAsync(r, bi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  }
+  k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(bi, bi, n, red_->partials, red_->counter, &dev_->bb);
+  k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(r, r, n, red_->partials, red_->counter, &dev_->rr);
+  vcycle(r, z, s);
+  k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(r, z, n, red_->partials, red_->counter, &dev_->rz);
+  cudaMemcpyAsync(p, z, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  launches += 5;
+}
+
+template <class T>
+void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
+  const size_t n = specs_[0].ndof();
+  const int g = vec_grid(n, sms_);
+  T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  apply(0, p, q, s, true);
+  k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(p, q, n, red_->partials, red_->counter, &dev_->pq);
+  k_pcg_xr<T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
+  vcycle(r, z, s);
+  k_dot2<T><<<red_->blocks, kVecThreads, 0, s>>>(r, r, r, z, n, red_->partials, red_->counter, &dev_->rr);
+  k_pcg_check<<<1, 1, 0, s>>>(dev_, h, use_cond);
+  k_pcg_p<T><<<g, kVecThreads, 0, s>>>(p, z, dev_, n);
+  launches += 5;
+}
+
+// Records the CG solve into a graph: a prologue (initial residual, first
+// preconditioned direction, start test) followed by a WHILE conditional node
+// whose body is one CG iteration; the body's last kernel decides whether the
+// loop continues, so the solve runs without host round trips.  The loop is
+// bounded by maxit (checked on the device).  Recording happens on two streams
+// owned by this object (capture is not possible on the legacy default stream);
+// every graph call is checked and nothing is launched unless all succeeded.
+template <class T>
+int MG<T>::capture_pcg(bool warm) {
+  cudaStream_t s = cap_[0], sb = cap_[1];
+  if (!s || !sb) return -5;
+  Graph& G = graph_[warm ? 1 : 0];
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  cudaGetLastError();
+  const long long l0 = launches;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -5;
+  bool ok = true;
+  cudaGraphNode_t wnode = nullptr;
+  long long l1 = 0, l2 = 0;
+  {
+    pcg_prologue(warm, s);
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    ok &= cudaStreamGetCaptureInfo(s, &cst, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
+    ok &= (cst == cudaStreamCaptureStatusActive) && cg != nullptr;
+    cudaGraphConditionalHandle h = 0;
+    if (ok) ok &= cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+      k_pcg_start<<<1, 1, 0, s>>>(dev_, h, 1);
+      ok &= cudaStreamGetCaptureInfo(s, &cst, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
+      ok &= (cst == cudaStreamCaptureStatusActive);
+    }
+    cudaGraphNodeParams cp = {};
+    if (ok) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      ok &= cudaGraphAddNode(&wnode, cg, deps, nullptr, ndeps, &cp) == cudaSuccess;
+      ok &= cp.conditional.phGraph_out != nullptr;
+    }
+    if (ok) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      l1 = launches;
+      ok &= cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+            cudaSuccess;
+      if (ok) {
+        pcg_body(sb, h, 1);
+        ok &= cudaStreamEndCapture(sb, &body) == cudaSuccess;
+      }
+      l2 = launches;
+      if (ok) ok &= cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                    cudaSuccess;
+    }
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+  ok &= (ee == cudaSuccess) && graph != nullptr;
+  if (ok) ok &= cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  ok &= cudaGetLastError() == cudaSuccess;
+  launches = l0;  // recording is not execution
+  if (!ok) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+    return -5;
+  }
+  G.prologue_nodes = (l1 - l0) + 1;
+  G.body_nodes = (l2 - l1);
+  return 0;
+}
+
+// Runs the captured solve: inputs are copied into the graph's fixed buffers,
+// rtol^2 and the iteration cap are written to the device scalars the start
+// kernel reads, and the result and the scalars come back after one sync.
+template <class T>
+int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s) {
+  const size_t n = specs_[0].ndof();
+  T* bi = pcg_[5];
+  T* xi = pcg_[6];
+  if (!graph_valid_) {
+    for (auto& G : graph_)
+      if (G.exec) {
+        cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+      }
+    graph_valid_ = true;
+  }
+  Graph& G = graph_[warm ? 1 : 0];
+  if (use_graphs && !G.exec) {
+    // the recording streams must not see work still queued on s
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
+    if (capture_pcg(warm) != 0) return -5;
+  }
+  hdev_->tol2 = rtol * rtol;
+  hdev_->maxit = maxit;
+  cudaMemcpyAsync(bi, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  if (warm) cudaMemcpyAsync(xi, x, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(&dev_->tol2, &hdev_->tol2, sizeof(double), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(&dev_->maxit, &hdev_->maxit, sizeof(int), cudaMemcpyHostToDevice, s);
+  if (use_graphs) {
+    cudaGraphLaunch(G.exec, s);
+    launches += G.prologue_nodes;
+  } else {
+    // host-driven loop over the same kernels (one sync per iteration)
+    pcg_prologue(warm, s);
+    k_pcg_start<<<1, 1, 0, s>>>(dev_, 0, 0);
+    ++launches;
+    for (;;) {
+      cudaMemcpyAsync(&hdev_->status, &dev_->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
+      if (hdev_->status != 1) break;
+      pcg_body(s, 0, 0);
+    }
+  }
+  cudaMemcpyAsync(x, xi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(hdev_, dev_, sizeof(PcgDev), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
+  st.iterations = hdev_->it;
+  st.relres = hdev_->relres;
+  if (use_graphs) launches += (long long)hdev_->it * G.body_nodes;
+  switch (hdev_->status) {
+    case 0: return 0;
+    case 5:
+      k_fill<T><<<vec_grid(n, sms_), kVecThreads, 0, s>>>(x, T(0), n);
+      return 0;
+    case 4: return -4;
+    case 3: return -3;  // breakdown: caller falls back
+    default: return -2;
+  }
 }
 
 template <class T>
 int MG<T>::pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s) {
-  const size_t n = specs_[0].ndof();
-  const int g = vec_grid(n, sms_);
-  T* r = pcg_[0];
-  T* z = pcg_[1];
-  T* p = pcg_[2];
-  T* q = pcg_[3];
   st = SolveStats{};
-  const double bn = std::sqrt(dot(b, b, n, s));
-  if (!std::isfinite(bn)) return -4;
-  if (bn == 0.0) {
-    k_fill<T><<<g, kVecThreads, 0, s>>>(x, T(0), n);
-    return 0;
+  int rc = graph_pcg(b, x, x_nonzero, rtol, maxit, st, s);
+  if (rc == -3) {
+    // p.Ap <= 0: the operator is indefinite here; continue with MINRES from x
+    SolveStats ms;
+    rc = minres(b, x, rtol, std::max(1, maxit - st.iterations), ms, s);
+    st.iterations += ms.iterations;
+    st.relres = ms.relres;
+    st.minres = 1;
   }
-  if (x_nonzero) {
-    apply(0, x, q, s, true);
-    k_sub<T><<<g, kVecThreads, 0, s>>>(r, b, q, n);
-  } else {
-    k_fill<T><<<g, kVecThreads, 0, s>>>(x, T(0), n);
-    cudaMemcpyAsync(r, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
-  }
-  double rn = std::sqrt(dot(r, r, n, s));
-  st.relres = rn / bn;
-  if (rn <= rtol * bn) return 0;
-  vcycle(r, z, s);
-  double rz = dot(r, z, n, s);
-  cudaMemcpyAsync(p, z, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
-  for (int it = 1; it <= maxit; ++it) {
-    apply(0, p, q, s, true);
-    const double pq = dot(p, q, n, s);
-    if (!std::isfinite(pq) || !std::isfinite(rz)) {
-      st.iterations = it;
-      return -4;
-    }
-    if (!(pq > 0.0) || !(rz > 0.0)) {
-      // indefinite operator: continue with MINRES from the current iterate
-      SolveStats ms;
-      const int rc = minres(b, x, rtol, maxit - it, ms, s);
-      st.iterations = it + ms.iterations;
-      st.relres = ms.relres;
-      st.minres = 1;
-      return rc;
-    }
-    const double alpha = rz / pq;
-    k_axpy<T><<<g, kVecThreads, 0, s>>>(x, T(alpha), p, n);
-    k_axpy<T><<<g, kVecThreads, 0, s>>>(r, T(-alpha), q, n);
-    rn = std::sqrt(dot(r, r, n, s));
-    st.iterations = it;
-    st.relres = rn / bn;
-    if (!std::isfinite(rn)) return -4;
-    if (rn <= rtol * bn) return 0;
-    vcycle(r, z, s);
-    const double rz_new = dot(r, z, n, s);
-    const double beta = rz_new / rz;
-    rz = rz_new;
-    k_xpby<T><<<g, kVecThreads, 0, s>>>(p, z, T(beta), n);
-  }
-  return -2;
+  return rc;
 }
-
 // Preconditioned MINRES (Paige & Saunders) with the SPD V-cycle as M, started
 // from x.  The recurrence's residual estimate (in the M^-1 norm) steers the
 // iteration; the true 2-norm residual is checked before returning.

@@ -32,39 +32,73 @@ TOPO_HD void p1_incidence(int e, int& dci, int& dcj, int& o, int& loc) {
   dci = t[e][0]; dcj = t[e][1]; o = t[e][2]; loc = t[e][3];
 }
 
+// Input of a node apply read directly from an array.
+template <class T, int NC>
+struct FetchArray {
+  const T* u;
+  TOPO_HD void operator()(size_t m, int, int, T (&v)[NC]) const {
+    for (int d = 0; d < NC; ++d) v[d] = u[NC * m + d];
+  }
+};
+
 template <class T, int NC>
 struct P1Kern {
+  // contribution of incidence (dci, dcj, O, LOC) of vertex (a,b) to y; chk
+  // enables the clamped-neighbour test (only needed near clamped nodes)
+  template <int DCI, int DCJ, int O, int LOC, class F>
+  TOPO_HD static void inc(int a, int b, const P1Params<T, NC>& P, const F& fetch, bool chk, T (&acc)[NC]) {
+    const int ci = a + DCI, cj = b + DCJ;
+    if (ci < 0 || ci >= P.nx || cj < 0 || cj >= P.ny) return;
+    const int NX = P.nx + 1;
+    const size_t t = (size_t(cj) * P.nx + ci) * 2 + O;
+    const T kk = P.kK ? P.kK[t] : P.kK_c;
+    T km = T(0);
+    if constexpr (NC == 1) km = P.kM ? P.kM[t] : P.kM_c;
+#define TOPO_P1_NB(L)                                                                     \
+  {                                                                                       \
+    const int al = ci + P1Off<O, L>::a, bl = cj + P1Off<O, L>::b;                         \
+    if (!(chk && is_clamped(P.dir, al, bl))) {                                            \
+      T ul[NC];                                                                           \
+      fetch(size_t(bl) * NX + al, al, bl, ul);                                            \
+      for (int c = 0; c < NC; ++c) {                                                      \
+        T sacc = T(0);                                                                    \
+        for (int d = 0; d < NC; ++d) sacc += P.K[O][LOC * NC + c][L * NC + d] * ul[d];    \
+        acc[c] += kk * sacc;                                                              \
+        if constexpr (NC == 1) acc[c] += km * P.Mm[O][LOC][L] * ul[c];                    \
+      }                                                                                   \
+    }                                                                                     \
+  }
+    TOPO_P1_NB(0) TOPO_P1_NB(1) TOPO_P1_NB(2)
+#undef TOPO_P1_NB
+  }
+
+  TOPO_HD static bool near_clamped(const Dir& d, int a, int b) {
+    return d.npts > 0 || (d.x_lo && a <= 1) || (d.y_lo && b <= 1) || a + 1 >= d.x_hi_from || b + 1 >= d.y_hi_from;
+  }
+
+  // t = (A u)(a,b) with u read through fetch; returns false for a clamped node
+  // (identity row: the caller uses u itself)
+  template <class F>
+  TOPO_HD static bool node_eval(int a, int b, const P1Params<T, NC>& P, const F& fetch, T (&acc)[NC]) {
+    const bool chk = near_clamped(P.dir, a, b);
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    if (chk && is_clamped(P.dir, a, b)) return false;
+    // the six incidences (cell offset, orientation, local vertex) of vertex (a,b)
+    inc<-1, -1, 0, 2>(a, b, P, fetch, chk, acc);
+    inc<-1, -1, 1, 2>(a, b, P, fetch, chk, acc);
+    inc<0, -1, 1, 1>(a, b, P, fetch, chk, acc);
+    inc<-1, 0, 0, 1>(a, b, P, fetch, chk, acc);
+    inc<0, 0, 0, 0>(a, b, P, fetch, chk, acc);
+    inc<0, 0, 1, 0>(a, b, P, fetch, chk, acc);
+    return true;
+  }
+
   TOPO_HD static void node_apply(int a, int b, const P1Params<T, NC>& P, const T* u, T* y) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
-    if (is_clamped(P.dir, a, b)) {
-      for (int c = 0; c < NC; ++c) y[NC * n + c] = u[NC * n + c];
-      return;
-    }
     T acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    for (int e = 0; e < 6; ++e) {
-      int dci, dcj, o, loc;
-      p1_incidence(e, dci, dcj, o, loc);
-      const int ci = a + dci, cj = b + dcj;
-      if (ci < 0 || ci >= P.nx || cj < 0 || cj >= P.ny) continue;
-      const size_t t = (size_t(cj) * P.nx + ci) * 2 + o;
-      const T kk = P.kK ? P.kK[t] : P.kK_c;
-      const T km = (NC == 1) ? (P.kM ? P.kM[t] : P.kM_c) : T(0);
-      for (int l = 0; l < 3; ++l) {
-        const int al = ci + p1_off_a(o, l), bl = cj + p1_off_b(o, l);
-        if (is_clamped(P.dir, al, bl)) continue;
-        const size_t m = size_t(bl) * NX + al;
-        T ul[NC];
-        for (int d = 0; d < NC; ++d) ul[d] = u[NC * m + d];
-        for (int c = 0; c < NC; ++c) {
-          T s = T(0);
-          for (int d = 0; d < NC; ++d) s += P.K[o][loc * NC + c][l * NC + d] * ul[d];
-          acc[c] += kk * s;
-          if (NC == 1) acc[c] += km * P.Mm[o][loc][l] * ul[c];
-        }
-      }
-    }
+    if (!node_eval(a, b, P, FetchArray<T, NC>{u}, acc))
+      for (int c = 0; c < NC; ++c) acc[c] = u[NC * n + c];
     for (int c = 0; c < NC; ++c) y[NC * n + c] = acc[c];
   }
 
@@ -121,8 +155,8 @@ struct Transfer {
 
 template <class T, int NC>
 struct TransferKern {
-  // b_c = P^T r_f
-  TOPO_HD static void node_restrict(int I, int J, const Transfer& X, const T* rf, T* bc) {
+  // b_c = P^T r_f, with r_f = bf - tf when tf is given (the fine residual)
+  TOPO_HD static void node_restrict(int I, int J, const Transfer& X, const T* rf, T* bc, const T* tf = nullptr) {
     const size_t nc = size_t(J) * X.NXc + I;
     if (is_clamped(X.dirc, I, J)) {
       for (int c = 0; c < NC; ++c) bc[NC * nc + c] = T(0);
@@ -132,14 +166,36 @@ struct TransferKern {
     const int nb[6][2] = {{a - 1, b}, {a + 1, b}, {a, b - 1}, {a, b + 1}, {a + 1, b + 1}, {a - 1, b - 1}};
     for (int c = 0; c < NC; ++c) {
       T s = T(0);
-      if (a < X.NXf && b < X.NYf) s = rf[NC * (size_t(b) * X.NXf + a) + c];
+      if (a < X.NXf && b < X.NYf) {
+        const size_t m = NC * (size_t(b) * X.NXf + a) + c;
+        s = tf ? rf[m] - tf[m] : rf[m];
+      }
       T h = T(0);
       for (int k = 0; k < 6; ++k) {
         const int aa = nb[k][0], bb = nb[k][1];
-        if (aa >= 0 && aa < X.NXf && bb >= 0 && bb < X.NYf)
-          h += rf[NC * (size_t(bb) * X.NXf + aa) + c];
+        if (aa >= 0 && aa < X.NXf && bb >= 0 && bb < X.NYf) {
+          const size_t m = NC * (size_t(bb) * X.NXf + aa) + c;
+          h += tf ? rf[m] - tf[m] : rf[m];
+        }
       }
       bc[NC * nc + c] = s + T(0.5) * h;
+    }
+  }
+
+  // (P x_c) at fine node (a,b) (0 at clamped fine nodes)
+  TOPO_HD static void prolong_value(int a, int b, const Transfer& X, const T* xc, T (&v)[NC]) {
+    if (is_clamped(X.dirf, a, b)) {
+      for (int c = 0; c < NC; ++c) v[c] = T(0);
+      return;
+    }
+    const int pa = a & 1, pb = b & 1;
+    const int I0 = (a - pa) >> 1, J0 = (b - pb) >> 1;
+    for (int c = 0; c < NC; ++c) {
+      const T x00 = xc[NC * (size_t(J0) * X.NXc + I0) + c];
+      if (!pa && !pb) v[c] = x00;
+      else if (pa && !pb) v[c] = T(0.5) * (x00 + xc[NC * (size_t(J0) * X.NXc + I0 + 1) + c]);
+      else if (!pa && pb) v[c] = T(0.5) * (x00 + xc[NC * (size_t(J0 + 1) * X.NXc + I0) + c]);
+      else v[c] = T(0.5) * (x00 + xc[NC * (size_t(J0 + 1) * X.NXc + I0 + 1) + c]);
     }
   }
 
@@ -158,6 +214,130 @@ struct TransferKern {
       else v = T(0.5) * (x00 + xc[NC * (size_t(J0 + 1) * X.NXc + I0 + 1) + c]);
       xf[NC * nf + c] += v;
     }
+  }
+};
+
+}  // namespace topo
+
+namespace topo {
+
+// ---------------------------------------------------------------------------
+// fused degree-2 Chebyshev smoothing steps of one P1 level (node-centric)
+// ---------------------------------------------------------------------------
+// Buffers of one level for the fused V-cycle.
+template <class T>
+struct SmoothBufs {
+  const T* b;      // right-hand side
+  const T* dinv;   // inverse diagonal
+  T* x;            // solution (pre-smoothed, then final)
+  T* x2;           // intermediate solution of post-smoothing
+  T* r;            // residual
+  T* d;            // Chebyshev direction
+  const double* cheb;  // c0 = 1/theta, c1, c2 of the second step
+};
+
+// PRE input: first step from x = 0, d0 = c0 Dinv b, computed per node
+template <class T, int NC>
+struct FetchPre {
+  const T* b;
+  const T* dinv;
+  T c0;
+  TOPO_HD void operator()(size_t m, int, int, T (&v)[NC]) const {
+    for (int d = 0; d < NC; ++d) v[d] = c0 * dinv[NC * m + d] * b[NC * m + d];
+  }
+};
+
+// POST1 input: x + P x_c (coarse-grid correction applied on the fly)
+template <class T, int NC>
+struct FetchCorr {
+  const T* x;
+  const T* xc;
+  Transfer X;
+  TOPO_HD void operator()(size_t m, int a, int b, T (&v)[NC]) const {
+    TransferKern<T, NC>::prolong_value(a, b, X, xc, v);
+    for (int d = 0; d < NC; ++d) v[d] += x[NC * m + d];
+  }
+};
+
+template <class T, int NC>
+struct P1Smooth {
+  // PRE: x = d0 + d1 with d0 = c0 Dinv b, r1 = b - A d0, d1 = c1 d0 + c2 Dinv r1
+  TOPO_HD static void pre(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+    const int NX = P.nx + 1;
+    const size_t n = size_t(b) * NX + a;
+    const T c0 = T(B.cheb[0]), c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
+    const FetchPre<T, NC> f{B.b, B.dinv, c0};
+    T t[NC], u[NC];
+    f(n, a, b, u);
+    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+      for (int c = 0; c < NC; ++c) t[c] = u[c];
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      const T r1 = B.b[i] - t[c];
+      B.x[i] = u[c] + c1 * u[c] + c2 * B.dinv[i] * r1;
+    }
+  }
+  // POST1: u = x + P xc ; r0 = b - A u ; d0 = c0 Dinv r0 ; x2 = u + d0 (writes r, d, x2)
+  TOPO_HD static void post1(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B, const T* xc,
+                            const Transfer& X) {
+    const int NX = P.nx + 1;
+    const size_t n = size_t(b) * NX + a;
+    const T c0 = T(B.cheb[0]);
+    const FetchCorr<T, NC> f{B.x, xc, X};
+    T t[NC], u[NC];
+    f(n, a, b, u);
+    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+      for (int c = 0; c < NC; ++c) t[c] = u[c];
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      const T r0 = B.b[i] - t[c];
+      const T d0 = c0 * B.dinv[i] * r0;
+      B.r[i] = r0;
+      B.d[i] = d0;
+      B.x2[i] = u[c] + d0;
+    }
+  }
+  // POST2: r1 = r0 - A d0 ; d1 = c1 d0 + c2 Dinv r1 ; x = x2 + d1
+  TOPO_HD static void post2(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+    const int NX = P.nx + 1;
+    const size_t n = size_t(b) * NX + a;
+    const T c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
+    const FetchArray<T, NC> f{B.d};
+    T t[NC];
+    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+      for (int c = 0; c < NC; ++c) t[c] = B.d[NC * n + c];
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      const T r1 = B.r[i] - t[c];
+      B.x[i] = B.x2[i] + c1 * B.d[i] + c2 * B.dinv[i] * r1;
+    }
+  }
+  // RESR: coarse b(I,J) = P^T (b - A x), the fine residual evaluated on the fly
+  // at the seven fine nodes of the coarse hat function
+  TOPO_HD static void resr(int I, int J, const P1Params<T, NC>& P, const SmoothBufs<T>& B, const Transfer& X,
+                           T* bc) {
+    const size_t nc = size_t(J) * X.NXc + I;
+    if (is_clamped(X.dirc, I, J)) {
+      for (int c = 0; c < NC; ++c) bc[NC * nc + c] = T(0);
+      return;
+    }
+    const FetchArray<T, NC> f{B.x};
+    const int a0 = 2 * I, b0 = 2 * J;
+    const int nb[7][2] = {{a0, b0}, {a0 - 1, b0}, {a0 + 1, b0}, {a0, b0 - 1},
+                          {a0, b0 + 1}, {a0 + 1, b0 + 1}, {a0 - 1, b0 - 1}};
+    T acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    for (int k = 0; k < 7; ++k) {
+      const int a = nb[k][0], b = nb[k][1];
+      if (a < 0 || a >= X.NXf || b < 0 || b >= X.NYf) continue;
+      const size_t m = size_t(b) * X.NXf + a;
+      T t[NC];
+      if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+        for (int c = 0; c < NC; ++c) t[c] = B.x[NC * m + c];
+      const T w = (k == 0) ? T(1) : T(0.5);
+      for (int c = 0; c < NC; ++c) acc[c] += w * (B.b[NC * m + c] - t[c]);
+    }
+    for (int c = 0; c < NC; ++c) bc[NC * nc + c] = acc[c];
   }
 };
 

@@ -14,6 +14,7 @@
 #pragma once
 
 #include "topo_common.cuh"
+#include "topo_p1.cuh"
 
 namespace topo {
 
@@ -24,6 +25,9 @@ struct P2Params {
   T lamT, mu2T;   // lambda*|T|, 2*mu*|T|
   Penal<T> pen;
   Dir dir;        // on the (2nx+1)x(2ny+1) node lattice
+  // optional precomputed r-weighted mass matrices, layout [o][k][cell] with
+  // cell = j*nx + i and k over [00,11,22,01,02,12] (null: evaluate r(xi) on the fly)
+  const T* rmass;
 };
 
 // r-weighted P1 mass matrix of one triangle, packed [00,11,22,01,02,12].
@@ -84,11 +88,9 @@ TOPO_HD void p2_vertex_grads(const TU (&u)[6][2], T ihx, T ihy, T (&G)[3][2][2])
   }
 }
 
-// y = K_T u for one triangle of orientation O.
+// y = K_T u for one triangle of orientation O with r-weighted mass matrix M.
 template <int O, class T>
-TOPO_HD void tri_apply(const T (&u)[6][2], const T (&xi)[3], const P2Params<T>& P, T (&y)[6][2]) {
-  T M[6];
-  tri_rmass(xi, P.pen, M);
+TOPO_HD void tri_apply_m(const T (&u)[6][2], const T (&M)[6], const P2Params<T>& P, T (&y)[6][2]) {
   T G[3][2][2];
   p2_vertex_grads<O>(u, P.ihx, P.ihy, G);
   const T muT = T(0.5) * P.mu2T;
@@ -136,6 +138,14 @@ TOPO_HD void tri_apply(const T (&u)[6][2], const T (&xi)[3], const P2Params<T>& 
   y[5][0] = T(4) * (ax + bx); y[5][1] = T(4) * (ay + by);
 }
 
+// y = K_T u for one triangle of orientation O.
+template <int O, class T>
+TOPO_HD void tri_apply(const T (&u)[6][2], const T (&xi)[3], const P2Params<T>& P, T (&y)[6][2]) {
+  T M[6];
+  tri_rmass(xi, P.pen, M);
+  tri_apply_m<O>(u, M, P, y);
+}
+
 // Diagonal of K_T for one triangle.
 template <class T>
 TOPO_HD void tri_diag(int o, const T (&xi)[3], const P2Params<T>& P, T (&d)[6][2]) {
@@ -175,96 +185,148 @@ TOPO_HD void tri_diag(int o, const T (&xi)[3], const P2Params<T>& P, T (&d)[6][2
 // ---------------------------------------------------------------------------
 constexpr int P2_TX = 32;  // owned cells per tile in x
 constexpr int P2_TY = 8;   // owned cells per tile in y
-constexpr int P2_THREADS = 256;
+constexpr int P2_THREADS = 320;  // one thread per computed cell (33 x 9 = 297)
 
 struct P2Tile {
   static constexpr int CX = P2_TX + 1, CY = P2_TY + 1;  // computed cells (1-cell halo at low side)
+  static constexpr int NCELL = CX * CY;
   static constexpr int NTX = 2 * CX + 1, NTY = 2 * CY + 1;
   static constexpr int VX = CX + 1, VY = CY + 1;
-  static constexpr int NTRI = CX * CY * 2;
 };
 
 template <class T>
 struct P2Smem {
   T u[P2Tile::NTY][P2Tile::NTX][2];
   T xi[P2Tile::VY][P2Tile::VX];
-  T out[P2Tile::NTRI][12];
+  T out[2][12][P2Tile::NCELL];  // per orientation, node x component, cell (conflict-free)
+};
+
+// What one launch of the tiled P2 kernel computes.
+enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2Post1 = 4, kP2Post2 = 5 };
+
+template <class T>
+struct P2Io {
+  int mode;
+  const T* u;          // kP2Apply / kP2Res input (x)
+  T* y;                // kP2Apply / kP2Diag output
+  SmoothBufs<T> B;     // smoothing modes (see P1Smooth for the formulas)
+  const T* xc;         // kP2Post1: coarse (P1) correction
+  Transfer X;          // kP2Post1: P2 -> P1 lattice transfer
 };
 
 template <class T>
 struct P2Kern {
   using Smem = P2Smem<T>;
 
+  // operand of the apply at node n = (a,b) for the launch's mode
+  TOPO_HD static void operand(const P2Io<T>& io, size_t n, int a, int b, T (&v)[2]) {
+    switch (io.mode) {
+      case kP2Pre: {
+        const T c0 = T(io.B.cheb[0]);
+        v[0] = c0 * io.B.dinv[2 * n] * io.B.b[2 * n];
+        v[1] = c0 * io.B.dinv[2 * n + 1] * io.B.b[2 * n + 1];
+        break;
+      }
+      case kP2Post1:
+        TransferKern<T, 2>::prolong_value(a, b, io.X, io.xc, v);
+        v[0] += io.B.x[2 * n];
+        v[1] += io.B.x[2 * n + 1];
+        break;
+      case kP2Post2:
+        v[0] = io.B.d[2 * n];
+        v[1] = io.B.d[2 * n + 1];
+        break;
+      default:
+        v[0] = io.u[2 * n];
+        v[1] = io.u[2 * n + 1];
+    }
+  }
+
   TOPO_HD static void load(int tid, int nt, int bx, int by, const P2Params<T>& P,
-                           const T* u, const T* xi, Smem& s) {
+                           const P2Io<T>& io, const T* xi, Smem& s) {
     const int i0 = bx * P2_TX, j0 = by * P2_TY;
     const int A0 = 2 * (i0 - 1), B0 = 2 * (j0 - 1);
     const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
-    if (u) {
+    if (io.mode != kP2Diag) {
       for (int idx = tid; idx < P2Tile::NTX * P2Tile::NTY; idx += nt) {
-        const int al = idx % P2Tile::NTX, bl = idx / P2Tile::NTX;
+        const int bl = idx / P2Tile::NTX, al = idx - bl * P2Tile::NTX;
         const int a = A0 + al, b = B0 + bl;
-        T v0 = T(0), v1 = T(0);
-        if (a >= 0 && a < NX && b >= 0 && b < NY && !is_clamped(P.dir, a, b)) {
-          const size_t n = size_t(b) * NX + a;
-          v0 = u[2 * n];
-          v1 = u[2 * n + 1];
-        }
-        s.u[bl][al][0] = v0;
-        s.u[bl][al][1] = v1;
+        T v[2] = {T(0), T(0)};
+        if (a >= 0 && a < NX && b >= 0 && b < NY && !is_clamped(P.dir, a, b))
+          operand(io, size_t(b) * NX + a, a, b, v);
+        s.u[bl][al][0] = v[0];
+        s.u[bl][al][1] = v[1];
       }
     }
     const int VXg = P.nx + 1, VYg = P.ny + 1;
     for (int idx = tid; idx < P2Tile::VX * P2Tile::VY; idx += nt) {
-      const int il = idx % P2Tile::VX, jl = idx / P2Tile::VX;
+      const int jl = idx / P2Tile::VX, il = idx - jl * P2Tile::VX;
       const int i = i0 - 1 + il, j = j0 - 1 + jl;
       s.xi[jl][il] = (i >= 0 && i < VXg && j >= 0 && j < VYg) ? xi[size_t(j) * VXg + i] : T(0);
     }
   }
 
-  // mode 0: operator apply, mode 1: diagonal
-  TOPO_HD static void compute(int tid, int nt, int bx, int by, const P2Params<T>& P, Smem& s,
-                              int mode) {
+  template <int O>
+  TOPO_HD static void tri(const P2Params<T>& P, const Smem& s, int ci, int cj, int ig, int jg, int mode,
+                          T (&y)[6][2]) {
+    T xe[3];
+    xe[0] = s.xi[cj + P1Off<O, 0>::b][ci + P1Off<O, 0>::a];
+    xe[1] = s.xi[cj + P1Off<O, 1>::b][ci + P1Off<O, 1>::a];
+    xe[2] = s.xi[cj + P1Off<O, 2>::b][ci + P1Off<O, 2>::a];
+    if (mode == 1) {
+      tri_diag(O, xe, P, y);
+      return;
+    }
+    const int a0 = 2 * ci, b0 = 2 * cj;
+    T ue[6][2];
+#define TOPO_LD(K)                                                           \
+  ue[K][0] = s.u[b0 + P2Off<O, K>::b][a0 + P2Off<O, K>::a][0];              \
+  ue[K][1] = s.u[b0 + P2Off<O, K>::b][a0 + P2Off<O, K>::a][1];
+    TOPO_LD(0) TOPO_LD(1) TOPO_LD(2) TOPO_LD(3) TOPO_LD(4) TOPO_LD(5)
+#undef TOPO_LD
+    if (P.rmass) {
+      const size_t nc = size_t(P.nx) * P.ny, c = size_t(jg) * P.nx + ig;
+      const T* m = P.rmass + size_t(O) * 6 * nc + c;
+      T M[6];
+      for (int k = 0; k < 6; ++k) M[k] = m[k * nc];
+      tri_apply_m<O>(ue, M, P, y);
+    } else {
+      tri_apply<O>(ue, xe, P, y);
+    }
+  }
+
+  // mode 0: operator apply, mode 1: diagonal.  One thread per computed cell,
+  // both triangles (orientation is a compile-time parameter: no divergence).
+  TOPO_HD static void compute(int tid, int nt, int bx, int by, const P2Params<T>& P, Smem& s, int mode) {
     const int i0 = bx * P2_TX, j0 = by * P2_TY;
-    for (int t = tid; t < P2Tile::NTRI; t += nt) {
-      const int o = t & 1, cell = t >> 1;
-      const int ci = cell % P2Tile::CX, cj = cell / P2Tile::CX;
+    for (int cell = tid; cell < P2Tile::NCELL; cell += nt) {
+      const int cj = cell / P2Tile::CX, ci = cell - cj * P2Tile::CX;
       const int ig = i0 - 1 + ci, jg = j0 - 1 + cj;
+      const bool valid = ig >= 0 && ig < P.nx && jg >= 0 && jg < P.ny;
       T y[6][2];
-      if (ig < 0 || ig >= P.nx || jg < 0 || jg >= P.ny) {
-        for (int k = 0; k < 6; ++k) y[k][0] = y[k][1] = T(0);
-      } else {
-        T xe[3];
-        for (int k = 0; k < 3; ++k) xe[k] = s.xi[cj + p1_off_b(o, k)][ci + p1_off_a(o, k)];
-        if (mode == 1) {
-          tri_diag(o, xe, P, y);
-        } else {
-          T ue[6][2];
-          for (int k = 0; k < 6; ++k) {
-            const int al = 2 * ci + p2_off_a(o, k), bl = 2 * cj + p2_off_b(o, k);
-            ue[k][0] = s.u[bl][al][0];
-            ue[k][1] = s.u[bl][al][1];
-          }
-          if (o == 0) tri_apply<0>(ue, xe, P, y);
-          else tri_apply<1>(ue, xe, P, y);
-        }
-      }
+      if (valid) tri<0>(P, s, ci, cj, ig, jg, mode, y);
       for (int k = 0; k < 6; ++k) {
-        s.out[t][2 * k] = y[k][0];
-        s.out[t][2 * k + 1] = y[k][1];
+        s.out[0][2 * k][cell] = valid ? y[k][0] : T(0);
+        s.out[0][2 * k + 1][cell] = valid ? y[k][1] : T(0);
+      }
+      if (valid) tri<1>(P, s, ci, cj, ig, jg, mode, y);
+      for (int k = 0; k < 6; ++k) {
+        s.out[1][2 * k][cell] = valid ? y[k][0] : T(0);
+        s.out[1][2 * k + 1][cell] = valid ? y[k][1] : T(0);
       }
     }
   }
 
   TOPO_HD static T tri_val(const Smem& s, int ci, int cj, int o, int k, int c) {
     if (ci < 0 || ci >= P2Tile::CX || cj < 0 || cj >= P2Tile::CY) return T(0);
-    return s.out[(cj * P2Tile::CX + ci) * 2 + o][2 * k + c];
+    return s.out[o][2 * k + c][cj * P2Tile::CX + ci];
   }
 
-  // Sum the per-triangle results onto the tile's owned nodes.
-  // mode 0: y = K u (clamped rows copy u);  mode 1: y = diag (clamped rows 1).
+  // Sum the per-triangle results onto the tile's owned nodes and finish the
+  // mode's update there (clamped rows act as identity rows).
   TOPO_HD static void gather(int tid, int nt, int bx, int by, const P2Params<T>& P,
-                             const Smem& s, const T* u, T* y, int mode) {
+                             const Smem& s, const P2Io<T>& io) {
+    const int mode = io.mode;
     const int i0 = bx * P2_TX, j0 = by * P2_TY;
     const int NX = 2 * P.nx + 1;
     const int a_beg = 2 * i0, b_beg = 2 * j0;
@@ -272,7 +334,8 @@ struct P2Kern {
     const int b_end = (j0 + P2_TY >= P.ny) ? 2 * P.ny + 1 : 2 * (j0 + P2_TY);
     const int na = a_end - a_beg, nb = b_end - b_beg;
     for (int idx = tid; idx < na * nb; idx += nt) {
-      const int a = a_beg + idx % na, b = b_beg + idx / na;
+      const int q = idx / na;
+      const int a = a_beg + (idx - q * na), b = b_beg + q;
       const int al = a - 2 * (i0 - 1), bl = b - 2 * (j0 - 1);
       const int I = al >> 1, J = bl >> 1, pa = al & 1, pb = bl & 1;
       const size_t n = size_t(b) * NX + a;
@@ -292,12 +355,40 @@ struct P2Kern {
         }
         r[c] = v;
       }
-      if (is_clamped(P.dir, a, b)) {
-        if (mode == 1) { r[0] = T(1); r[1] = T(1); }
-        else { r[0] = u[2 * n]; r[1] = u[2 * n + 1]; }
+      const bool cl = is_clamped(P.dir, a, b);
+      if (mode == kP2Diag) {
+        io.y[2 * n] = cl ? T(1) : r[0];
+        io.y[2 * n + 1] = cl ? T(1) : r[1];
+        continue;
       }
-      y[2 * n] = r[0];
-      y[2 * n + 1] = r[1];
+      T un[2];
+      operand(io, n, a, b, un);
+      if (cl) { r[0] = un[0]; r[1] = un[1]; }
+      const SmoothBufs<T>& B = io.B;
+      for (int c = 0; c < 2; ++c) {
+        const size_t i = 2 * n + c;
+        switch (mode) {
+          case kP2Apply: io.y[i] = r[c]; break;
+          case kP2Pre: {
+            const T rr = B.b[i] - r[c];
+            B.x[i] = un[c] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * rr;
+            break;
+          }
+          case kP2Res: B.r[i] = B.b[i] - r[c]; break;
+          case kP2Post1: {
+            const T r0 = B.b[i] - r[c];
+            const T d0 = T(B.cheb[0]) * B.dinv[i] * r0;
+            B.r[i] = r0;
+            B.d[i] = d0;
+            B.x2[i] = un[c] + d0;
+            break;
+          }
+          default: {  // kP2Post2
+            const T r1 = B.r[i] - r[c];
+            B.x[i] = B.x2[i] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * r1;
+          }
+        }
+      }
     }
   }
 };
@@ -305,6 +396,20 @@ struct P2Kern {
 // ---------------------------------------------------------------------------
 // per-triangle kernels (no tiling)
 // ---------------------------------------------------------------------------
+
+// r-weighted mass matrices of every triangle, layout [o][k][cell] (P2Params::rmass)
+template <class T>
+TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const double* xi, const Penal<double>& pen, T* out) {
+  const size_t nc = size_t(nx) * ny, c = size_t(j) * nx + i;
+  const int VX = nx + 1;
+  for (int o = 0; o < 2; ++o) {
+    double xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
+    double M[6];
+    tri_rmass(xe, pen, M);
+    for (int k = 0; k < 6; ++k) out[(size_t(o) * 6 + k) * nc + c] = T(M[k]);
+  }
+}
 
 // kappa_T = (1/|T|) int_T r(xi) with the 7-point rule: the Galerkin P1
 // coefficient of the P2 operator (P1 strains are constant per triangle).

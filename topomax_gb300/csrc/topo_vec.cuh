@@ -65,21 +65,29 @@ __global__ void k_recip(T* __restrict__ x, size_t n) {
   TOPO_GRID_STRIDE(i, n) x[i] = T(1) / x[i];
 }
 
-// Chebyshev smoother pieces (preconditioner Dinv).
-// first step: d = c0 * Dinv r ; x = (xzero ? 0 : x) + d
+// Chebyshev smoother pieces (preconditioner Dinv).  The coefficients live in
+// device memory (coef[0] = 1/theta, coef[2k-1], coef[2k] = step-k weights) so a
+// captured graph stays valid when a new set-up changes the eigenvalue bounds.
+// first step: r = b - t (t == nullptr: r = b, the x = 0 start)
+//             d = coef[0] Dinv r ; x = (xzero ? 0 : x) + d
 template <class T>
-__global__ void k_cheb_first(const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ d,
-                             T* __restrict__ x, T c0, int xzero, size_t n) {
+__global__ void k_cheb_first(const T* __restrict__ b, const T* __restrict__ t, T* __restrict__ r,
+                             const T* __restrict__ dinv, T* __restrict__ d, T* __restrict__ x,
+                             const double* __restrict__ coef, size_t n) {
+  const T c0 = T(coef[0]);
   TOPO_GRID_STRIDE(i, n) {
-    const T di = c0 * dinv[i] * r[i];
+    const T ri = t ? b[i] - t[i] : b[i];
+    r[i] = ri;
+    const T di = c0 * dinv[i] * ri;
     d[i] = di;
-    x[i] = xzero ? di : x[i] + di;
+    x[i] = t ? x[i] + di : di;
   }
 }
 // later steps: r -= t ; d = c1 d + c2 Dinv r ; x += d
 template <class T>
 __global__ void k_cheb_next(T* __restrict__ r, const T* __restrict__ t, const T* __restrict__ dinv,
-                            T* __restrict__ d, T* __restrict__ x, T c1, T c2, size_t n) {
+                            T* __restrict__ d, T* __restrict__ x, const double* __restrict__ coef, size_t n) {
+  const T c1 = T(coef[0]), c2 = T(coef[1]);
   TOPO_GRID_STRIDE(i, n) {
     const T ri = r[i] - t[i];
     r[i] = ri;
@@ -159,11 +167,13 @@ template <class T>
 __global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
                        const T* __restrict__ d, size_t n, double* partials, unsigned* counter,
                        double* out) {
-  double v[2] = {0.0, 0.0};
+  // per-thread partials in the input precision (a handful of terms), then FP64
+  T p0 = T(0), p1 = T(0);
   TOPO_GRID_STRIDE(i, n) {
-    v[0] += double(a[i]) * double(b[i]);
-    v[1] += double(c[i]) * double(d[i]);
+    p0 += a[i] * b[i];
+    p1 += c[i] * d[i];
   }
+  double v[2] = {double(p0), double(p1)};
   double tot[2];
   if (finish_reduction<2>(v, partials, counter, tot)) {
     out[0] = tot[0];
@@ -171,46 +181,64 @@ __global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T
   }
 }
 
-// up to kMaxMulti dot products against one vector: out[k] = V_k . w
+// Multi-vector kernels with a compile-time vector count C (host code
+// dispatches on the run-time count): out[k] = V_k . w and out[C] = w . w
 constexpr int kMaxMulti = 16;
 struct MultiCoef {
   double c[kMaxMulti];
 };
 
-template <class TV, class TW>
-__global__ void k_multidot(const TV* __restrict__ V, size_t stride, int count, const TW* __restrict__ w, size_t n,
+template <class TV, class TW, int C>
+__global__ void k_multidot(const TV* __restrict__ V, size_t stride, const TW* __restrict__ w, size_t n,
                            double* partials, unsigned* counter, double* out) {
-  double v[kMaxMulti];
-  for (int k = 0; k < kMaxMulti; ++k) v[k] = 0.0;
+  double v[C + 1];
+#pragma unroll
+  for (int k = 0; k <= C; ++k) v[k] = 0.0;
   TOPO_GRID_STRIDE(i, n) {
     const double wi = double(w[i]);
-    for (int k = 0; k < count; ++k) v[k] += double(V[size_t(k) * stride + i]) * wi;
+#pragma unroll
+    for (int k = 0; k < C; ++k) v[k] += double(V[size_t(k) * stride + i]) * wi;
+    v[C] += wi * wi;
   }
-  double tot[kMaxMulti];
-  if (finish_reduction<kMaxMulti>(v, partials, counter, tot))
-    for (int k = 0; k < count; ++k) out[k] = tot[k];
+  double tot[C + 1];
+  if (finish_reduction<C + 1>(v, partials, counter, tot))
+    for (int k = 0; k <= C; ++k) out[k] = tot[k];
 }
 
 // w -= sum_k c_k V_k
-template <class TV, class TW>
-__global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t stride, int count, MultiCoef c,
-                            size_t n) {
+template <class TV, class TW, int C>
+__global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t stride, MultiCoef c, size_t n) {
   TOPO_GRID_STRIDE(i, n) {
     double s = double(w[i]);
-    for (int k = 0; k < count; ++k) s -= c.c[k] * double(V[size_t(k) * stride + i]);
+#pragma unroll
+    for (int k = 0; k < C; ++k) s -= c.c[k] * double(V[size_t(k) * stride + i]);
     w[i] = TW(s);
   }
 }
 
 // x += sum_k c_k Z_k
-template <class TZ, class TX>
-__global__ void k_add_multi(TX* __restrict__ x, const TZ* __restrict__ Z, size_t stride, int count, MultiCoef c,
-                            size_t n) {
+template <class TZ, class TX, int C>
+__global__ void k_add_multi(TX* __restrict__ x, const TZ* __restrict__ Z, size_t stride, MultiCoef c, size_t n) {
   TOPO_GRID_STRIDE(i, n) {
     double s = double(x[i]);
-    for (int k = 0; k < count; ++k) s += c.c[k] * double(Z[size_t(k) * stride + i]);
+#pragma unroll
+    for (int k = 0; k < C; ++k) s += c.c[k] * double(Z[size_t(k) * stride + i]);
     x[i] = TX(s);
   }
 }
+
+// run-time count -> compile-time instance (1..9)
+#define TOPO_DISPATCH_COUNT(count, F) \
+  switch (count) {                    \
+    case 1: F(1); break;              \
+    case 2: F(2); break;              \
+    case 3: F(3); break;              \
+    case 4: F(4); break;              \
+    case 5: F(5); break;              \
+    case 6: F(6); break;              \
+    case 7: F(7); break;              \
+    case 8: F(8); break;              \
+    default: F(9); break;             \
+  }
 
 }  // namespace topo
