@@ -154,6 +154,16 @@ int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t st
  * FEM_src/elasisity_problem.py:104-132 after bc.apply). */
 int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y, topo_stream_t stream);
 
+/* Measurement hook (no counterpart in the reference): *ms = duration of ONE launch of the
+ * state operator y = K(xi) x on the design of the last topo_state_solve, timed with CUDA events
+ * on `stream` -- the FP32 matrix-free kernel for a TOPO_PREC_MIXED context, the FP64 one
+ * otherwise.  Synchronises the stream. */
+int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream);
+
+/* Measurement hook (no counterpart in the reference): kernels this context has launched so far
+ * (kernels executed inside CUDA graphs are counted per execution). */
+int topo_launch_count(const topo_ctx* ctx, int64_t* launches);
+
 /* Copy of the pre-assembled load vector (2*n_p2 entries, clamped dofs zero). */
 int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream);
 

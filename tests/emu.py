@@ -144,7 +144,7 @@ def vertex_weights(nx, ny, hx, hy):
     return w
 
 
-MODE = {"pre": 2, "res": 3, "post1": 4, "post2": 5}
+MODE = {"pre": 2, "res": 3, "first": 4, "post2": 5}
 
 
 def smooth(mode, p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, NXc=1, NYc=1, dirc=None,

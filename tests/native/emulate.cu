@@ -185,8 +185,6 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
     io.mode = mode;
     io.u = bufs[2];
     io.B = B;
-    io.xc = xc;
-    io.X = X;
     p2_run_io<double>(P, xi, io);
     return 0;
   }
@@ -206,15 +204,11 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
     P.kM = nullptr;
     P.kK_c = 0;
     P.kM_c = K == 1 ? 1.0 : 0.0;
-    if (mode == kP2Res) {
-      for (int J = 0; J < NYc; ++J)
-        for (int I = 0; I < NXc; ++I) P1Smooth<double, K>::resr(I, J, P, B, X, bc);
-      return;
-    }
     for (int b = 0; b <= ny; ++b)
       for (int a = 0; a <= nx; ++a) {
         if (mode == kP2Pre) P1Smooth<double, K>::pre(a, b, P, B);
-        else if (mode == kP2Post1) P1Smooth<double, K>::post1(a, b, P, B, xc, X);
+        else if (mode == kP2Res) P1Smooth<double, K>::res(a, b, P, B);
+        else if (mode == kP2First) P1Smooth<double, K>::first(a, b, P, B);
         else P1Smooth<double, K>::post2(a, b, P, B);
       }
   };

@@ -253,23 +253,16 @@ def test_fused_smoothing_steps_match_composition(level):
     d0 = cheb[0] * dinv * b
     ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
-    # RES (P2) / RESR (P1)
+    # RES
     bufs["x"] = x.copy()
-    cb = np.zeros(NC * c["NX"] * c["NY"])
-    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, c["NX"], c["NY"], c["dir"],
-               bc=cb)
+    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
     rr = b - A(x)
-    if p2:
-        assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
-    else:
-        ref_c = emu.restrict(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], rr)
-        assert np.max(np.abs(cb - ref_c)) <= 1e-12 * np.max(np.abs(ref_c))
-    # POST1 then POST2
+    assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
+    # FIRST (coarse correction already added to x) then POST2
     xc = rng.standard_normal(NC * c["NX"] * c["NY"]) * _free_rows(c["dir"], c["NX"], c["NY"], NC)
-    bufs["x"] = x.copy()
-    emu.smooth("post1", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, c["NX"], c["NY"], c["dir"],
-               xc=xc)
     u = x + emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
+    bufs["x"] = u.copy()
+    emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
     r0 = b - A(u)
     dd0 = cheb[0] * dinv * r0
     assert np.max(np.abs(bufs["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))

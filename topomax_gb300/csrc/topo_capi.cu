@@ -12,6 +12,7 @@
 #include "topomax_gb300.h"
 #include "topo_mg_impl.cuh"
 #include "topo_setup.h"
+#include "topo_sens.cuh"
 
 namespace topo {
 extern template class MG<float>;
@@ -77,51 +78,6 @@ __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf,
     const int o = int(t & 1);
     const size_t cell = t >> 1;
     kc[t] = coarsen_kappa(kf, nxf, nyf, int(cell % nxc), int(cell / nxc), o);
-  }
-}
-
-template <class TQ>
-__global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu, TQ area, Penal<TQ> pen,
-                           const double* __restrict__ u, const double* __restrict__ xi, TQ* __restrict__ out) {
-  const size_t nt = size_t(2) * nx * ny;
-  const int VX = nx + 1, NX = 2 * nx + 1;
-  TOPO_GRID_STRIDE(t, nt) {
-    const int o = int(t & 1);
-    const size_t cell = t >> 1;
-    const int i = int(cell % nx), j = int(cell / nx);
-    double ue[6][2];
-    for (int k = 0; k < 6; ++k) {
-      const size_t n = size_t(2 * j + p2_off_b(o, k)) * NX + 2 * i + p2_off_a(o, k);
-      ue[k][0] = u[2 * n];
-      ue[k][1] = u[2 * n + 1];
-    }
-    TQ xe[3];
-    for (int k = 0; k < 3; ++k) xe[k] = TQ(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
-    TQ c[3];
-    if (o == 0) tri_sensitivity<0, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
-    else tri_sensitivity<1, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
-    out[3 * t] = c[0];
-    out[3 * t + 1] = c[1];
-    out[3 * t + 2] = c[2];
-  }
-}
-
-template <class TQ>
-__global__ void k_vertex_gather3(int nx, int ny, const TQ* __restrict__ tri3, double* __restrict__ b) {
-  const int VX = nx + 1;
-  const size_t nv = size_t(nx + 1) * (ny + 1);
-  TOPO_GRID_STRIDE(v, nv) {
-    const int a = int(v % VX), bb = int(v / VX);
-    double s = 0.0;
-    for (int e = 0; e < 6; ++e) {
-      int dci, dcj, o, loc;
-      p1_incidence(e, dci, dcj, o, loc);
-      const int ci = a + dci, cj = bb + dcj;
-      if (ci < 0 || ci >= nx || cj < 0 || cj >= ny) continue;
-      const size_t t = (size_t(cj) * nx + ci) * 2 + o;
-      s += double(tri3[3 * t + loc]);
-    }
-    b[v] = s;
   }
 }
 
@@ -220,6 +176,8 @@ struct topo_ctx {
   double E = 0, nu = 0, lmbda = 0, mu = 0, eps = 0, pmin = 1e-6;
   bool penal_set = false;
   double p = 0;
+  long long launches = 0;          // kernels launched by the context itself
+  const double* xi_last = nullptr;  // design of the last state solve
   Dir dir_p2{};
   Arena arena;
   Reducer red;
@@ -237,8 +195,6 @@ struct topo_ctx {
   // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
-  float* rm_op32 = nullptr;
-  float* rm_pc32 = nullptr;
   double* r64 = nullptr;
   double* y64 = nullptr;
   float* d32 = nullptr;
@@ -427,6 +383,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
   double prev = 0.0;
   for (int cycle = 0; cycle < kMaxOuter; ++cycle) {
     double* r = W.V;
+    C->launches += 4;
     apply64(x, W.t, s);
     k_sub<double><<<g, kVecThreads, 0, s>>>(r, b, W.t, n);
     const double beta = std::sqrt(C->dot64(r, r, n, s));
@@ -443,6 +400,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     int k = 0;
     for (int j = 0; j < m; ++j) {
       st.outer += 1;
+      C->launches += 6;
       double* vj = W.V + size_t(j) * n;
       float* zj = W.Z + size_t(j) * n;
       k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, vj, 1.0, n);
@@ -538,6 +496,7 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const int L = int(C->sspec.size());
   Penal<double> pen = make_penal<double>(C->p, C->pmin, 1);
   k_kappa_p2<<<C->grid(C->sspec[1].ntri()), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->skK[1]);
+  C->launches += 2 + (L - 2);
   for (int l = 2; l < L; ++l) {
     const LevelSpec &F = C->sspec[l - 1], &Cc = C->sspec[l];
     k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->skK[l - 1], F.nx, F.ny, C->skK[l], Cc.nx, Cc.ny);
@@ -547,10 +506,10 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
   k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64);
   if (C->precision == TOPO_PREC_MIXED) {
+    // FP32 operators re-evaluate r(xi) per quadrature point: cheaper than reading
+    // 48 bytes of mass matrices per cell; the FP64 operator reads them instead
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
-    k_convert<float, double><<<C->grid(12 * ncell), kVecThreads, 0, s>>>(C->rm_op32, C->rm_op64, 1.0, 12 * ncell);
-    k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc32);
-    C->smg32.set_p2(C->p2params<float>(0, C->rm_op32), C->p2params<float>(1, C->rm_pc32), C->xi32);
+    C->smg32.set_p2(C->p2params<float>(0), C->p2params<float>(1), C->xi32);
     st = C->smg32.setup(s);
   } else {
     k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc64);
@@ -633,12 +592,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       const size_t n = 2 * C->nn2;
       const size_t ncell = size_t(C->nx) * C->ny;
       C->rm_op64 = C->arena.alloc_n<double>(12 * ncell);
-      if (precision == TOPO_PREC_MIXED) {
-        C->rm_op32 = C->arena.alloc_n<float>(12 * ncell);
-        C->rm_pc32 = C->arena.alloc_n<float>(12 * ncell);
-      } else {
-        C->rm_pc64 = C->arena.alloc_n<double>(12 * ncell);
-      }
+      if (precision == TOPO_PREC_FP64) C->rm_pc64 = C->arena.alloc_n<double>(12 * ncell);
       C->r64 = C->arena.alloc_n<double>(n);
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
@@ -719,6 +673,7 @@ int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, i
     if (!f || !xi || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid filter arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     filter_apply64(ctx, f, ctx->fb64, false, s);
+    ctx->launches += 1;
     return filter_solve_impl(ctx, ctx->fb64, xi, rtol, iters, s);
   });
 }
@@ -739,6 +694,7 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int rc = state_setup(ctx, xi, s);
     if (rc) return rc;
+    ctx->xi_last = xi;
     const size_t n = 2 * ctx->nn2;
     const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
     SolveStats st;
@@ -763,6 +719,7 @@ int topo_compliance(topo_ctx* ctx, const double* u, double* compliance, topo_str
     if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
     if (!u || !compliance) return ctx->fail(TOPO_ERR_ARG, "invalid compliance arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    ctx->launches += 1;
     k_dot<double, double><<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->load, u, 2 * ctx->nn2, ctx->red.partials,
                                                                 ctx->red.counter, compliance);
     return ctx->cuda_check("compliance");
@@ -777,6 +734,7 @@ int topo_sensitivity_rhs(topo_ctx* ctx, const double* u, const double* xi, doubl
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const size_t nt = size_t(2) * ctx->nx * ctx->ny;
     const double area = 0.5 * ctx->hx * ctx->hy;
+    ctx->launches += 2;
     if (ctx->precision == TOPO_PREC_MIXED) {
       float* tri = static_cast<float*>(ctx->sens_tri);
       k_sens_tri<float><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
@@ -812,6 +770,7 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const size_t n = ctx->nv;
     k_emd_half<<<ctx->grid(n), kVecThreads, 0, s>>>(psi_prev, g, alpha, ctx->half, n);
+    ctx->launches += 2;  // half step and the final update
     NewtonState init{};
     init.c = 0.0;
     cudaMemcpyAsync(ctx->nstate, &init, sizeof(init), cudaMemcpyHostToDevice, s);
@@ -819,6 +778,7 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
     const int maxit = 50;  // scipy.optimize.newton default
     for (int launched = 0; launched < maxit;) {
       const int chunk = std::min(8, maxit - launched);
+      ctx->launches += chunk;
       for (int k = 0; k < chunk; ++k)
         k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
                                                           ctx->red.partials, ctx->red.counter, ctx->nstate);
@@ -877,6 +837,7 @@ int topo_emd_finish(topo_ctx* ctx, const double* psi, const double* psi_prev, do
   return guarded(ctx, [&]() {
     if (!psi) return ctx->fail(TOPO_ERR_ARG, "invalid arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    ctx->launches += 1;
     k_emd_finish<<<ctx->red.blocks, kVecThreads, 0, s>>>(psi, psi_prev, ctx->vw, rho, ctx->nv, ctx->red.partials,
                                                          ctx->red.counter, ctx->red.out);
     if (psi_prev && delta) {
@@ -906,6 +867,42 @@ int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y
     p2_apply_f64(ctx->p2params<double>(), xi, u, y, reinterpret_cast<cudaStream_t>(stream));
     return ctx->cuda_check("apply");
   });
+}
+
+int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state || !ms) return ctx->fail(TOPO_ERR_ARG, "invalid arguments");
+    if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    if (ctx->precision == TOPO_PREC_MIXED) {
+      float* x = ctx->smg32.scratch0(7);
+      float* y = ctx->smg32.scratch0(8);
+      cudaEventRecord(e0, s);
+      p2_apply_f32(ctx->p2params<float>(0), ctx->xi32, x, y, s);
+      cudaEventRecord(e1, s);
+    } else {
+      cudaEventRecord(e0, s);
+      p2_apply_f64(ctx->p2params<double>(0, ctx->rm_op64), ctx->xi_last, ctx->r64, ctx->y64, s);
+      cudaEventRecord(e1, s);
+    }
+    ctx->launches += 1;
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t;
+    return ctx->cuda_check("time operator");
+  });
+}
+
+int topo_launch_count(const topo_ctx* ctx, int64_t* launches) {
+  if (!ctx || !launches) return TOPO_ERR_ARG;
+  *launches = ctx->launches + ctx->smg32.launches + ctx->smg64.launches + ctx->fmg32.launches + ctx->fmg64.launches;
+  return TOPO_OK;
 }
 
 int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream) {

@@ -182,6 +182,10 @@ class MG {
     long long prologue_nodes = 0, body_nodes = 0;
   } graph_[2];
   bool graph_valid_ = false;
+  void build_tail(Arena& arena);
+  int tail_ = -1;              // first level run by the one-CTA shared-memory tail kernel
+  void* tail_desc_ = nullptr;  // TailDesc<T, NC> (device)
+  size_t tail_smem_ = 0;
 
   T* pcg_[kScratch] = {};
   Reducer* red_ = nullptr;

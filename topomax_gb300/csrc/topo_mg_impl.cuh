@@ -37,17 +37,19 @@ __global__ void __launch_bounds__(P2_THREADS)
 }
 
 template <class T, int NC, int MODE>
-__global__ void __launch_bounds__(kRowThreads_)
-    k_p1_smooth(P1Params<T, NC> P, SmoothBufs<T> B, const T* __restrict__ xc, Transfer X, T* __restrict__ bc) {
+__global__ void __launch_bounds__(kRowThreads_) k_p1_smooth(P1Params<T, NC> P, SmoothBufs<T> B) {
   const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
-  if (MODE == 3) {  // residual + restriction, grid over coarse nodes
-    if (a < X.NXc) P1Smooth<T, NC>::resr(a, b, P, B, X, bc);
-    return;
-  }
   if (a > P.nx) return;
-  if (MODE == 2) P1Smooth<T, NC>::pre(a, b, P, B);
-  else if (MODE == 4) P1Smooth<T, NC>::post1(a, b, P, B, xc, X);
+  if (MODE == kP2Pre) P1Smooth<T, NC>::pre(a, b, P, B);
+  else if (MODE == kP2Res) P1Smooth<T, NC>::res(a, b, P, B);
+  else if (MODE == kP2First) P1Smooth<T, NC>::first(a, b, P, B);
   else P1Smooth<T, NC>::post2(a, b, P, B);
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(kRowThreads_) k_prolong_add(Transfer X, const T* __restrict__ xc, T* __restrict__ xf) {
+  const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
+  if (a < X.NXf) TransferKern<T, NC>::node_prolong_add(a, b, X, xc, xf);
 }
 
 template <class T, int NC>
@@ -156,6 +158,110 @@ __global__ void k_dense_matvec(const T* __restrict__ Ainv, const T* __restrict__
     T s = T(0);
     for (int j = 0; j < n; ++j) s += Ainv[size_t(i) * n + j] * b[j];
     x[i] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// coarse-level tail: the V-cycle over the smallest levels runs in one CTA with
+// every work vector resident in shared memory (one launch for ~6 x levels
+// phases; read-only data -- coefficients, D^-1, element matrices -- via L1)
+// ---------------------------------------------------------------------------
+constexpr int kTailThreads = 1024;
+constexpr int kTailMaxLevels = 10;
+constexpr int kTailMaxNodes = 4096;
+constexpr size_t kTailSmemBudget = 160 * 1024;
+
+template <class T, int NC>
+struct TailLevel {
+  P1Params<T, NC> P;
+  Transfer X;  // to the next coarser level
+  const T* dinv;
+  const double* cheb;
+  int NX, nn, off;  // off: first of this level's five shared vectors x, b, r, d, x2 (NC*nn each)
+};
+
+template <class T, int NC>
+struct TailDesc {
+  int nlev, smem_elems;
+  const T* cinv;
+  TailLevel<T, NC> lv[kTailMaxLevels];
+};
+
+template <class T, int NC>
+__global__ void __launch_bounds__(kTailThreads)
+    k_tail_vcycle(const TailDesc<T, NC>* __restrict__ D, const T* __restrict__ b_in, T* __restrict__ x_out) {
+  extern __shared__ __align__(16) unsigned char tail_raw[];
+  T* sm = reinterpret_cast<T*>(tail_raw);
+  const int nlev = D->nlev;
+  auto bufs = [&](int l) {
+    const TailLevel<T, NC>& L = D->lv[l];
+    const int m = NC * L.nn;
+    T* base = sm + L.off;
+    return SmoothBufs<T>{base + m, L.dinv, base, base + 4 * m, base + 2 * m, base + 3 * m, L.cheb};
+  };
+  {
+    const int m = NC * D->lv[0].nn;
+    T* b0 = sm + D->lv[0].off + m;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) b0[i] = b_in[i];
+  }
+  __syncthreads();
+  for (int l = 0; l + 1 < nlev; ++l) {
+    const TailLevel<T, NC>& L = D->lv[l];
+    const SmoothBufs<T> B = bufs(l);
+    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+      const int b = n / L.NX, a = n - b * L.NX;
+      P1Smooth<T, NC>::pre(a, b, L.P, B);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+      const int b = n / L.NX, a = n - b * L.NX;
+      P1Smooth<T, NC>::res(a, b, L.P, B);
+    }
+    __syncthreads();
+    const TailLevel<T, NC>& C = D->lv[l + 1];
+    T* bc = sm + C.off + NC * C.nn;
+    for (int n = threadIdx.x; n < C.nn; n += blockDim.x) {
+      const int J = n / C.NX, I = n - J * C.NX;
+      TransferKern<T, NC>::node_restrict(I, J, L.X, B.r, bc);
+    }
+    __syncthreads();
+  }
+  {
+    const TailLevel<T, NC>& C = D->lv[nlev - 1];
+    const int m = NC * C.nn;
+    const T* bc = sm + C.off + m;
+    T* xc = sm + C.off;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      T acc = T(0);
+      for (int j = 0; j < m; ++j) acc += D->cinv[size_t(i) * m + j] * bc[j];
+      xc[i] = acc;
+    }
+    __syncthreads();
+  }
+  for (int l = nlev - 2; l >= 0; --l) {
+    const TailLevel<T, NC>& L = D->lv[l];
+    const SmoothBufs<T> B = bufs(l);
+    const T* xc = sm + D->lv[l + 1].off;
+    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+      const int b = n / L.NX, a = n - b * L.NX;
+      TransferKern<T, NC>::node_prolong_add(a, b, L.X, xc, B.x);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+      const int b = n / L.NX, a = n - b * L.NX;
+      P1Smooth<T, NC>::first(a, b, L.P, B);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+      const int b = n / L.NX, a = n - b * L.NX;
+      P1Smooth<T, NC>::post2(a, b, L.P, B);
+    }
+    __syncthreads();
+  }
+  {
+    const int m = NC * D->lv[0].nn;
+    const T* x0 = sm + D->lv[0].off;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) x_out[i] = x0[i];
   }
 }
 
@@ -325,6 +431,60 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
     if (!c) cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
   set_p2_smem_attr<T>();
   graph_valid_ = false;
+  build_tail(arena);
+}
+
+// Chooses the tail levels (smallest levels whose shared vectors fit the
+// budget, never level 0) and uploads their descriptor.
+template <class T>
+void MG<T>::build_tail(Arena& arena) {
+  tail_ = -1;
+  tail_desc_ = nullptr;
+  tail_smem_ = 0;
+  const int L = levels();
+  size_t bytes = 0;
+  int first = L;
+  for (int l = L - 1; l >= 1; --l) {
+    const size_t add = 5 * specs_[l].ndof() * sizeof(T);
+    if (specs_[l].nn() > size_t(kTailMaxNodes) || bytes + add > kTailSmemBudget || L - l > kTailMaxLevels) break;
+    bytes += add;
+    first = l;
+  }
+  if (first >= L - 1) return;  // fewer than two levels: nothing to gain
+  auto build = [&](auto nc_tag) {
+    constexpr int NC = decltype(nc_tag)::value;
+    TailDesc<T, NC> h;
+    std::memset(&h, 0, sizeof(h));
+    h.nlev = L - first;
+    h.cinv = cinv_;
+    int off = 0;
+    for (int k = 0; k < h.nlev; ++k) {
+      const int l = first + k;
+      TailLevel<T, NC>& d = h.lv[k];
+      d.P = make_p1<T, NC>(specs_[l], refs_[l], lv_[l].kK, NC == 1 ? lv_[l].kM : nullptr);
+      if (l + 1 < L) d.X = make_transfer(specs_[l], specs_[l + 1]);
+      d.dinv = lv_[l].dinv;
+      d.cheb = cheb_ + 8 * l;
+      d.NX = specs_[l].NX;
+      d.nn = int(specs_[l].nn());
+      d.off = off;
+      off += 5 * NC * d.nn;
+    }
+    h.smem_elems = off;
+    void* p = arena.alloc(sizeof(h));
+    if (!p) return;
+    cudaMemcpy(p, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (cudaFuncSetAttribute(k_tail_vcycle<T, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(size_t(off) * sizeof(T))) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    tail_desc_ = p;
+    tail_smem_ = size_t(off) * sizeof(T);
+    tail_ = first;
+  };
+  if (specs_[first].NC == 2) build(std::integral_constant<int, 2>{});
+  else build(std::integral_constant<int, 1>{});
 }
 
 template <class T>
@@ -470,6 +630,14 @@ void MG<T>::vcycle_level(int l, const T* b, T* x, cudaStream_t s) {
   Lev& v = lv_[l];
   const int L = levels();
   const LevelSpec& S = specs_[l];
+  if (l == tail_ && tail_desc_) {
+    if (S.NC == 2)
+      k_tail_vcycle<T, 2><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);
+    else
+      k_tail_vcycle<T, 1><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 1>*>(tail_desc_), b, x);
+    ++launches;
+    return;
+  }
   if (l == L - 1) {
     k_dense_matvec<T><<<1, 256, 0, s>>>(cinv_, b, x, int(S.ndof()));
     ++launches;
@@ -478,38 +646,39 @@ void MG<T>::vcycle_level(int l, const T* b, T* x, cudaStream_t s) {
   SmoothBufs<T> B{b, v.dinv, x, v.x2, v.r, v.d, cheb_ + 8 * l};
   const Transfer X = make_transfer(S, specs_[l + 1]);
   Lev& c = lv_[l + 1];
+  const dim3 gf = row_grid(S.NX, S.NY), gc = row_grid(X.NXc, X.NYc);
   if (S.p2) {
     P2Io<T> io;
     std::memset(&io, 0, sizeof(io));
     io.B = B;
+    io.u = x;
     io.mode = kP2Pre;
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Res;
-    io.u = x;
     launch_p2_tile<T>(p2_, xi_, io, s);
-    k_restrict<T, 2><<<row_grid(X.NXc, X.NYc), kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    k_restrict<T, 2><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    io.mode = kP2Post1;
-    io.xc = c.x;
-    io.X = X;
+    k_prolong_add<T, 2><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
+    io.mode = kP2First;
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Post2;
     launch_p2_tile<T>(p2_, xi_, io, s);
-    launches += 2;
+    launches += 3;
     return;
   }
-  const dim3 gf = row_grid(S.NX, S.NY), gc = row_grid(X.NXc, X.NYc);
   auto run = [&](auto nc_tag) {
     constexpr int NC = decltype(nc_tag)::value;
     const auto P = make_p1<T, NC>(S, refs_[l], v.kK, NC == 1 ? v.kM : nullptr);
-    k_p1_smooth<T, NC, 2><<<gf, kRowThreads, 0, s>>>(P, B, nullptr, X, nullptr);
-    k_p1_smooth<T, NC, 3><<<gc, kRowThreads, 0, s>>>(P, B, nullptr, X, c.b);
-    launches += 2;
+    k_p1_smooth<T, NC, kP2Pre><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_p1_smooth<T, NC, kP2Res><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_restrict<T, NC><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    k_p1_smooth<T, NC, 4><<<gf, kRowThreads, 0, s>>>(P, B, c.x, X, nullptr);
-    k_p1_smooth<T, NC, 5><<<gf, kRowThreads, 0, s>>>(P, B, nullptr, X, nullptr);
-    launches += 2;
+    k_prolong_add<T, NC><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
+    k_p1_smooth<T, NC, kP2First><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_p1_smooth<T, NC, kP2Post2><<<gf, kRowThreads, 0, s>>>(P, B);
+    launches += 3;
   };
   if (S.NC == 2) run(std::integral_constant<int, 2>{});
   else run(std::integral_constant<int, 1>{});

@@ -247,18 +247,6 @@ struct FetchPre {
   }
 };
 
-// POST1 input: x + P x_c (coarse-grid correction applied on the fly)
-template <class T, int NC>
-struct FetchCorr {
-  const T* x;
-  const T* xc;
-  Transfer X;
-  TOPO_HD void operator()(size_t m, int a, int b, T (&v)[NC]) const {
-    TransferKern<T, NC>::prolong_value(a, b, X, xc, v);
-    for (int d = 0; d < NC; ++d) v[d] += x[NC * m + d];
-  }
-};
-
 template <class T, int NC>
 struct P1Smooth {
   // PRE: x = d0 + d1 with d0 = c0 Dinv b, r1 = b - A d0, d1 = c1 d0 + c2 Dinv r1
@@ -277,24 +265,31 @@ struct P1Smooth {
       B.x[i] = u[c] + c1 * u[c] + c2 * B.dinv[i] * r1;
     }
   }
-  // POST1: u = x + P xc ; r0 = b - A u ; d0 = c0 Dinv r0 ; x2 = u + d0 (writes r, d, x2)
-  TOPO_HD static void post1(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B, const T* xc,
-                            const Transfer& X) {
+  // RES: r = b - A x
+  TOPO_HD static void res(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+    const int NX = P.nx + 1;
+    const size_t n = size_t(b) * NX + a;
+    T t[NC];
+    if (!P1Kern<T, NC>::node_eval(a, b, P, FetchArray<T, NC>{B.x}, t))
+      for (int c = 0; c < NC; ++c) t[c] = B.x[NC * n + c];
+    for (int c = 0; c < NC; ++c) B.r[NC * n + c] = B.b[NC * n + c] - t[c];
+  }
+  // FIRST (after the coarse correction was added to x):
+  // r0 = b - A x ; d0 = c0 Dinv r0 ; x2 = x + d0 (writes r, d, x2)
+  TOPO_HD static void first(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     const T c0 = T(B.cheb[0]);
-    const FetchCorr<T, NC> f{B.x, xc, X};
-    T t[NC], u[NC];
-    f(n, a, b, u);
-    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
-      for (int c = 0; c < NC; ++c) t[c] = u[c];
+    T t[NC];
+    if (!P1Kern<T, NC>::node_eval(a, b, P, FetchArray<T, NC>{B.x}, t))
+      for (int c = 0; c < NC; ++c) t[c] = B.x[NC * n + c];
     for (int c = 0; c < NC; ++c) {
       const size_t i = NC * n + c;
       const T r0 = B.b[i] - t[c];
       const T d0 = c0 * B.dinv[i] * r0;
       B.r[i] = r0;
       B.d[i] = d0;
-      B.x2[i] = u[c] + d0;
+      B.x2[i] = B.x[i] + d0;
     }
   }
   // POST2: r1 = r0 - A d0 ; d1 = c1 d0 + c2 Dinv r1 ; x = x2 + d1
@@ -311,33 +306,6 @@ struct P1Smooth {
       const T r1 = B.r[i] - t[c];
       B.x[i] = B.x2[i] + c1 * B.d[i] + c2 * B.dinv[i] * r1;
     }
-  }
-  // RESR: coarse b(I,J) = P^T (b - A x), the fine residual evaluated on the fly
-  // at the seven fine nodes of the coarse hat function
-  TOPO_HD static void resr(int I, int J, const P1Params<T, NC>& P, const SmoothBufs<T>& B, const Transfer& X,
-                           T* bc) {
-    const size_t nc = size_t(J) * X.NXc + I;
-    if (is_clamped(X.dirc, I, J)) {
-      for (int c = 0; c < NC; ++c) bc[NC * nc + c] = T(0);
-      return;
-    }
-    const FetchArray<T, NC> f{B.x};
-    const int a0 = 2 * I, b0 = 2 * J;
-    const int nb[7][2] = {{a0, b0}, {a0 - 1, b0}, {a0 + 1, b0}, {a0, b0 - 1},
-                          {a0, b0 + 1}, {a0 + 1, b0 + 1}, {a0 - 1, b0 - 1}};
-    T acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    for (int k = 0; k < 7; ++k) {
-      const int a = nb[k][0], b = nb[k][1];
-      if (a < 0 || a >= X.NXf || b < 0 || b >= X.NYf) continue;
-      const size_t m = size_t(b) * X.NXf + a;
-      T t[NC];
-      if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
-        for (int c = 0; c < NC; ++c) t[c] = B.x[NC * m + c];
-      const T w = (k == 0) ? T(1) : T(0.5);
-      for (int c = 0; c < NC; ++c) acc[c] += w * (B.b[NC * m + c] - t[c]);
-    }
-    for (int c = 0; c < NC; ++c) bc[NC * nc + c] = acc[c];
   }
 };
 

@@ -202,16 +202,14 @@ struct P2Smem {
 };
 
 // What one launch of the tiled P2 kernel computes.
-enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2Post1 = 4, kP2Post2 = 5 };
+enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2First = 4, kP2Post2 = 5 };
 
 template <class T>
 struct P2Io {
   int mode;
-  const T* u;          // kP2Apply / kP2Res input (x)
+  const T* u;          // kP2Apply / kP2Res / kP2First input (x)
   T* y;                // kP2Apply / kP2Diag output
   SmoothBufs<T> B;     // smoothing modes (see P1Smooth for the formulas)
-  const T* xc;         // kP2Post1: coarse (P1) correction
-  Transfer X;          // kP2Post1: P2 -> P1 lattice transfer
 };
 
 template <class T>
@@ -227,11 +225,6 @@ struct P2Kern {
         v[1] = c0 * io.B.dinv[2 * n + 1] * io.B.b[2 * n + 1];
         break;
       }
-      case kP2Post1:
-        TransferKern<T, 2>::prolong_value(a, b, io.X, io.xc, v);
-        v[0] += io.B.x[2 * n];
-        v[1] += io.B.x[2 * n + 1];
-        break;
       case kP2Post2:
         v[0] = io.B.d[2 * n];
         v[1] = io.B.d[2 * n + 1];
@@ -375,7 +368,7 @@ struct P2Kern {
             break;
           }
           case kP2Res: B.r[i] = B.b[i] - r[c]; break;
-          case kP2Post1: {
+          case kP2First: {
             const T r0 = B.b[i] - r[c];
             const T d0 = T(B.cheb[0]) * B.dinv[i] * r0;
             B.r[i] = r0;
