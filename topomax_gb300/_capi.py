@@ -30,7 +30,7 @@ EXPORTED = [
     "topo_set_penalization", "topo_filter_apply", "topo_filter_solve", "topo_state_solve",
     "topo_compliance", "topo_sensitivity_rhs", "topo_sensitivity", "topo_emd_step",
     "topo_emd_finish", "topo_integrate", "topo_apply_state", "topo_load_vector", "topo_time_operator",
-    "topo_launch_count",
+    "topo_launch_count", "topo_sensitivity_rhs_noalloc",
 ]
 
 
@@ -103,6 +103,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_load_vector.argtypes = [P, P, P]
     lib.topo_time_operator.argtypes = [P, PD, P]
     lib.topo_launch_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    lib.topo_sensitivity_rhs_noalloc.argtypes = [ctypes.POINTER(GridDesc), D, D, D, D, P, P, P, P]
     for name in EXPORTED:
         if name not in ("topo_create", "topo_create_filter", "topo_destroy", "topo_last_error"):
             getattr(lib, name).restype = I
