@@ -42,16 +42,49 @@ void dir_to(const Dir& r, int* d) {
   for (int k = 0; k < 2 * kMaxDirPoints; ++k) d[5 + k] = r.pts[k];
 }
 
+// Runs the column-march P2 kernel on the CPU: the 32 lanes of a warp execute
+// each phase in turn and the shuffles become copies between lane states.
 template <class T>
-void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io) {
-  auto s = std::make_unique<P2Smem<T>>();
-  const int gx = (P.nx + P2_TX - 1) / P2_TX, gy = (P.ny + P2_TY - 1) / P2_TY;
-  for (int by = 0; by < gy; ++by)
-    for (int bx = 0; bx < gx; ++bx) {
-      std::memset(s.get(), 0xff, sizeof(P2Smem<T>));  // poison: unwritten smem shows up as NaN
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::load(t, P2_THREADS, bx, by, P, io, xi, *s);
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::compute(t, P2_THREADS, bx, by, P, *s, io.mode == kP2Diag ? 1 : 0);
-      for (int t = 0; t < P2_THREADS; ++t) P2Kern<T>::gather(t, P2_THREADS, bx, by, P, *s, io);
+void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0) {
+  if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4);
+  const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
+  const bool operand = io.mode != kP2Diag;
+  std::vector<P2Lane<T>> L(32);
+  auto down = [&](int r0) {
+    for (int l = 0; l < 32; ++l) {
+      const int src = l < 31 ? l + 1 : l;  // a shuffle from beyond the warp returns the own value
+      if (L[l].edge) continue;
+      if (operand)
+        for (int r = r0; r <= 2; ++r)
+          for (int c = 0; c < 2; ++c) L[l].U[r][2][c] = L[src].U[r][0][c];
+      for (int r = (r0 == 0 ? 0 : 1); r <= 1; ++r) L[l].X[r][1] = L[src].X[r][0];
+    }
+  };
+  auto up = [&]() {
+    for (int l = 31; l >= 1; --l)
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 2; ++c) L[l].A[r][0][c] += L[l - 1].A[r][2][c];
+  };
+  for (int w = 0; w < nxw; ++w)
+    for (int js = 0; js < P.ny; js += seg) {
+      const int je = std::min(js + seg, P.ny);
+      for (int l = 0; l < 32; ++l) P2March<T>::begin(L[l], w * P2M_OWN - 1 + l, l == 31);
+      int j = js > 0 ? js - 1 : 0;
+      for (int l = 0; l < 32; ++l) P2March<T>::template load<0>(P, io, xi, L[l], j);
+      down(0);
+      for (;;) {
+        for (int l = 0; l < 32; ++l) P2March<T>::compute(P, L[l], j, io.mode);
+        up();
+        if (j >= js)
+          for (int l = 1; l < 32; ++l)
+            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2);
+        if (++j >= je) break;
+        for (int l = 0; l < 32; ++l) {
+          P2March<T>::advance(L[l]);
+          P2March<T>::template load<1>(P, io, xi, L[l], j);
+        }
+        down(1);
+      }
     }
 }
 
@@ -169,7 +202,7 @@ int emu_transfer(int NC, int NXf, int NYf, const int* dirf, int NXc, int NYc, co
 // xc / dirc / NXc, NYc: the next coarser lattice (post1 source, resr target bc)
 int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, double lam, double mu, double p,
                double pmin, const int* dir, const double* xi, const double* kK, double* const* bufs,
-               const double* cheb, int NXc, int NYc, const int* dirc, const double* xc, double* bc) {
+               const double* cheb, int NXc, int NYc, const int* dirc, const double* xc, double* bc, int stencil) {
   SmoothBufs<double> B{bufs[0], bufs[1], bufs[2], bufs[3], bufs[4], bufs[5], cheb};
   Transfer X;
   X.NXf = p2 ? 2 * nx + 1 : nx + 1;
@@ -204,13 +237,25 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
     P.kM = nullptr;
     P.kK_c = 0;
     P.kM_c = K == 1 ? 1.0 : 0.0;
-    for (int b = 0; b <= ny; ++b)
-      for (int a = 0; a <= nx; ++a) {
-        if (mode == kP2Pre) P1Smooth<double, K>::pre(a, b, P, B);
-        else if (mode == kP2Res) P1Smooth<double, K>::res(a, b, P, B);
-        else if (mode == kP2First) P1Smooth<double, K>::first(a, b, P, B);
-        else P1Smooth<double, K>::post2(a, b, P, B);
-      }
+    auto sweep = [&](const auto& Q) {
+      for (int b = 0; b <= ny; ++b)
+        for (int a = 0; a <= nx; ++a) {
+          if (mode == kP2Pre) P1Smooth<double, K>::pre(a, b, Q, B);
+          else if (mode == kP2Res) P1Smooth<double, K>::res(a, b, Q, B);
+          else if (mode == kP2First) P1Smooth<double, K>::first(a, b, Q, B);
+          else P1Smooth<double, K>::post2(a, b, Q, B);
+        }
+    };
+    if (stencil) {
+      // the assembled-stencil representation of the same level
+      constexpr int SW = StencilLayout<K>::stride;
+      std::vector<double> st(size_t(nx + 1) * (ny + 1) * SW);
+      for (int b = 0; b <= ny; ++b)
+        for (int a = 0; a <= nx; ++a) p1_stencil_node<double, K>(a, b, P, st.data() + (size_t(b) * (nx + 1) + a) * SW);
+      sweep(P1Stencil<double, K>{nx, ny, P.dir, st.data()});
+    } else {
+      sweep(P);
+    }
   };
   if (NC == 2) {
     P1Params<double, 2> P;

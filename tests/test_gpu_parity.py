@@ -219,3 +219,26 @@ def test_large_grid_properties(precision):
     rhs = torch.dot(u, prob.apply_operator(xi, v)).item()
     assert abs(lhs - rhs) <= 1e-12 * (v.norm() * Ku.norm()).item()
     assert prob.filtered_rho.tensor.min().item() > 0.0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_tail_matches_level_kernels(precision, monkeypatch):
+    """The one-CTA coarse tail (all vectors and stencils in shared memory) runs
+    the same per-node steps as the per-level kernels: the solves agree to
+    rounding of the final refinement and take the same number of iterations."""
+    import torch
+    from topomax_gb300 import fem as F
+    d = _design()
+    results = []
+    for tail in ("1", "0"):
+        monkeypatch.setenv("TOPO_TAIL", tail)
+        prob, V = _gpu_problem(d, 200, 100, precision=precision, rtol=1e-10)
+        prob.set_penalization(3.0)
+        g = torch.Generator().manual_seed(3)
+        xi = F.Function(V, (torch.rand(V.dim(), generator=g, dtype=torch.float64) * 0.99 + 0.01).cuda())
+        u = prob.forward(xi)
+        results.append((prob.stats["state_iterations"], u.tensor.cpu().numpy()))
+        del prob
+    assert results[0][0] == results[1][0], [r[0] for r in results]
+    ref = results[1][1]
+    assert np.max(np.abs(results[0][1] - ref)) <= 1e-13 * np.max(np.abs(ref))

@@ -1,9 +1,10 @@
 """Kernel phase logic (run on the CPU through the emulator) against the FP64 oracle.
 
-The GPU kernels are load / compute / gather phases shared with the host; here
-they run tile by tile on the CPU so the tiling, halo and index logic is
-checked bit-for-bit-close against the oracle's assembled operators before any
-GPU run.  The same comparisons run on the GPU in ``test_gpu_parity.py``.
+The GPU kernels are built from phases shared with the host (the P2 column
+march: load / compute / finish per lane, with the warp shuffles replaced by
+copies between lane states); here they run on the CPU so the segment, halo
+and index logic is checked against the oracle's assembled operators before
+any GPU run.  The same comparisons run on the GPU in ``test_gpu_parity.py``.
 """
 import numpy as np
 import pytest
@@ -25,7 +26,7 @@ CASES = [
     # (W, H, nx, ny, sides, p)
     (1.0, 1.0, 3, 2, ["Left"], 3.0),
     (1.0, 1.0, 10, 10, ["Bottom"], 3.0),
-    (2.0, 1.0, 33, 9, ["Left", "Right", "Top"], 3.0),      # 2x2 tiles, ragged
+    (2.0, 1.0, 33, 9, ["Left", "Right", "Top"], 3.0),      # 2 warps x 2 row segments, ragged
     (2.0, 1.0, 70, 17, [], 3.5),                            # non-integer p, no clamping
     (3.0, 1.0, 65, 24, ["Bottom", "Right"], 4.0),
 ]
@@ -216,9 +217,12 @@ def test_level_chain_shapes():
     assert c2["nx"] == 3 and c2["dir"][2] == 2
 
 
-@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1"])
+@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil"])
 def test_fused_smoothing_steps_match_composition(level):
-    """PRE / RES(R) / POST1 / POST2 against the same steps composed from plain applies."""
+    """PRE / RES / FIRST / POST2 against the same steps composed from plain applies
+    (P1 levels also through their assembled 7-point stencil)."""
+    stencil = level.endswith("-stencil")
+    level = level.replace("-stencil", "")
     nx, ny, hx, hy, p = 34, 10, 0.05, 0.05, 3.0
     lam, mu = lame(1.0, 0.3)
     rng = np.random.default_rng(21)
@@ -249,25 +253,25 @@ def test_fused_smoothing_steps_match_composition(level):
     cheb = np.array([0.7, 0.3, 0.9])
     bufs = dict(b=b.copy(), dinv=dinv.copy(), x=x.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
     # PRE
-    emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
     d0 = cheb[0] * dinv * b
     ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
     # RES
     bufs["x"] = x.copy()
-    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
     rr = b - A(x)
     assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
     # FIRST (coarse correction already added to x) then POST2
     xc = rng.standard_normal(NC * c["NX"] * c["NY"]) * _free_rows(c["dir"], c["NX"], c["NY"], NC)
     u = x + emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
     bufs["x"] = u.copy()
-    emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
     r0 = b - A(u)
     dd0 = cheb[0] * dinv * r0
     assert np.max(np.abs(bufs["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
     assert np.max(np.abs(bufs["x2"] - (u + dd0))) <= 1e-12 * np.max(np.abs(u))
-    emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb)
+    emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
     r1 = r0 - A(dd0)
     ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))

@@ -216,6 +216,35 @@ struct topo_ctx {
   double* cfix = nullptr;
 
   ~topo_ctx() {
+    if (std::getenv("TOPO_PROFILE")) {
+      auto dump = [](const char* name, auto& mg) {
+        mg.flush_level_profile();
+        for (size_t l = 0; l < mg.level_ms.size(); ++l)
+          if (mg.level_calls[l])
+            std::fprintf(stderr, "[topo profile] %s level %zu (%dx%d nodes): %lld V-cycle visits, %.3f ms incl, %.2f us/visit\n",
+                         name, l, mg.spec(int(l)).NX, mg.spec(int(l)).NY, mg.level_calls[l], mg.level_ms[l],
+                         1e3 * mg.level_ms[l] / mg.level_calls[l]);
+        std::vector<long long> cyc;
+        mg.tail_profile(cyc);
+        if (!cyc.empty() && cyc.back() > 0) {
+          const int nl = mg.levels() - mg.tail_level();
+          std::fprintf(stderr, "[topo profile] %s tail: levels %d.., %d levels, %lld launches; k-cycles per phase:",
+                       name, mg.tail_level(), nl, cyc.back());
+          int slot = 1;
+          auto pr = [&](const char* what, int l) {
+            std::fprintf(stderr, " %s%d=%.2f", what, l, 1e-3 * double(cyc[slot++]) / double(cyc.back()));
+          };
+          for (int l = 0; l + 1 < nl; ++l) { pr("pre", l); pr("res", l); pr("restr", l); }
+          pr("coarse", nl - 1);
+          for (int l = nl - 2; l >= 0; --l) { pr("prol", l); pr("first", l); pr("post", l); }
+          std::fprintf(stderr, "\n");
+        }
+      };
+      dump("state32", smg32);
+      dump("state64", smg64);
+      dump("filter32", fmg32);
+      dump("filter64", fmg64);
+    }
     if (red.host) cudaFreeHost(red.host);
   }
 
@@ -266,6 +295,10 @@ namespace {
 bool graphs_enabled() {
   const char* e = std::getenv("TOPO_GRAPHS");
   return !(e && e[0] == '0');
+}
+bool env_flag(const char* name, bool dflt) {
+  const char* e = std::getenv(name);
+  return e ? e[0] != '0' : dflt;
 }
 
 int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
@@ -325,6 +358,8 @@ int init_filter(topo_ctx* C, double eps) {
   int st;
   if (C->precision == TOPO_PREC_MIXED) {
     C->fmg32.use_graphs = graphs_enabled();
+    C->fmg32.use_tail = env_flag("TOPO_TAIL", true);
+    C->fmg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg32.set_coefficients(kK, kM);
     C->fd32 = C->arena.alloc_n<float>(C->nv);
@@ -333,6 +368,8 @@ int init_filter(topo_ctx* C, double eps) {
     st = C->fmg32.setup(s);
   } else {
     C->fmg64.use_graphs = graphs_enabled();
+    C->fmg64.use_tail = env_flag("TOPO_TAIL", true);
+    C->fmg64.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg64.set_coefficients(kK, kM);
     if (C->arena.failed()) return C->fail(TOPO_ERR_CUDA, "out of device memory");
@@ -597,6 +634,8 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
         C->smg32.use_graphs = graphs_enabled();
+        C->smg32.use_tail = env_flag("TOPO_TAIL", true);
+        C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg32.set_coefficients(kK, kM);
         C->xi32 = C->arena.alloc_n<float>(C->nv);
@@ -605,6 +644,8 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->sens_tri = C->arena.alloc_n<float>(size_t(3) * C->sspec[0].ntri());
       } else {
         C->smg64.use_graphs = graphs_enabled();
+        C->smg64.use_tail = env_flag("TOPO_TAIL", true);
+        C->smg64.profile_levels = env_flag("TOPO_PROFILE", false);
     C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg64.set_coefficients(kK, kM);
         C->sens_tri = C->arena.alloc_n<double>(size_t(3) * C->sspec[0].ntri());

@@ -44,13 +44,26 @@ TOPO_HD bool is_clamped(const Dir& d, int a, int b) {
   return false;
 }
 
+// Quick rejection: true when (a,b) is at least one node away from every
+// clamped column/row and no clamped points exist (then is_clamped is false).
+TOPO_HD bool surely_free(const Dir& d, int a, int b) {
+  return d.npts == 0 && !(d.x_lo && a == 0) && !(d.y_lo && b == 0) && a < d.x_hi_from && b < d.y_hi_from;
+}
+
 TOPO_HD float topo_pow(float x, float p) { return powf(x, p); }
 TOPO_HD double topo_pow(double x, double p) { return pow(x, p); }
 
-// x^p, by repeated products when p is a small positive integer (ip > 0).
+// x^p, by products when p is a small positive integer (ip > 0): branch-free
+// for ip <= 4 (the penalties of every design), a loop above.
 template <class T>
 TOPO_HD T pow_p(T x, int ip, T p) {
-  if (ip > 0) {
+  if (ip > 0 && ip <= 4) {
+    const T x2 = x * x;
+    const T lo = ip == 1 ? x : x2;
+    const T hi = ip == 4 ? x2 : x;
+    return ip <= 2 ? lo : x2 * hi;
+  }
+  if (ip > 4) {
     T r = x;
     for (int k = 1; k < ip; ++k) r *= x;
     return r;

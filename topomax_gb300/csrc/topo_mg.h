@@ -143,6 +143,16 @@ class MG {
   // record the CG loop as a CUDA graph with a device-side WHILE node (default);
   // false runs the same kernels from a host loop
   bool use_graphs = true;
+  bool use_tail = true;  // run the smallest levels in the one-CTA shared-memory kernel
+  // opt-in level timing (host-driven mode only): inclusive ms per level, summed
+  bool profile_levels = false;
+  std::vector<double> level_ms;
+  std::vector<long long> level_calls;
+  void flush_level_profile();
+  // tail phase timing (profile_levels only): SM cycles summed per phase in
+  // execution order, last entry = launches; empty without a tail
+  void tail_profile(std::vector<long long>& cycles) const;
+  int tail_level() const { return tail_; }
 
  private:
   struct Lev {
@@ -151,10 +161,13 @@ class MG {
     T* dinv = nullptr;
     T* kK = nullptr;
     T* kM = nullptr;
+    T* st = nullptr;  // assembled stencil (levels with at most kStencilMaxNodes nodes)
     double lmax = 1.0;
     bool bound = false;  // lmax is a guaranteed upper bound (no safety factor)
   };
   void vcycle_level(int l, const T* b, T* x, cudaStream_t s);
+  void vcycle_level_body(int l, const T* b, T* x, cudaStream_t s);
+  int prof_depth_ = 0;
   int capture_pcg(bool warm);
   void pcg_prologue(bool warm, cudaStream_t s);
   void pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond);
@@ -183,9 +196,11 @@ class MG {
   } graph_[2];
   bool graph_valid_ = false;
   void build_tail(Arena& arena);
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events_;
   int tail_ = -1;              // first level run by the one-CTA shared-memory tail kernel
   void* tail_desc_ = nullptr;  // TailDesc<T, NC> (device)
   size_t tail_smem_ = 0;
+  long long* tail_trace_ = nullptr;
 
   T* pcg_[kScratch] = {};
   Reducer* red_ = nullptr;

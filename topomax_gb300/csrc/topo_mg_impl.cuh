@@ -2,9 +2,12 @@
 // Included by topo_mg_f32.cu / topo_mg_f64.cu, which instantiate MG<T>.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "topo_mg.h"
 #include "topo_p1.cuh"
@@ -18,26 +21,80 @@ namespace topo {
 // ---------------------------------------------------------------------------
 // Lattice kernels use a 2D grid: blockIdx.y is the row, x covers the columns.
 constexpr int kRowThreads = 128;
+// P1 levels with at most this many nodes keep an assembled stencil (it fits
+// in L2 beside the vectors; larger levels are bandwidth-bound and evaluate
+// their element matrices on the fly)
+constexpr size_t kStencilMaxNodes = size_t(1) << 18;
 #define kRowThreads_ 128
 inline dim3 row_grid(int NX, int NY) { return dim3((NX + kRowThreads - 1) / kRowThreads, NY); }
 
-// The tiled P2 kernel: load the operand tile, per-triangle element work,
-// gather onto owned nodes with the mode's epilogue (apply, diagonal or one of
-// the fused Chebyshev smoothing steps).
+// The column-march P2 kernel (see P2March): each warp marches over one
+// segment of cell rows; operand, density and element results move between
+// lanes by shuffles.
 template <class T>
-__global__ void __launch_bounds__(P2_THREADS)
-    k_p2_tile(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& s = *reinterpret_cast<P2Smem<T>*>(smem_raw);
-  P2Kern<T>::load(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, io, xi, s);
-  __syncthreads();
-  P2Kern<T>::compute(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, io.mode == kP2Diag ? 1 : 0);
-  __syncthreads();
-  P2Kern<T>::gather(threadIdx.x, blockDim.x, blockIdx.x, blockIdx.y, P, s, io);
+__device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+template <class T>
+__device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+
+// column 2 of rows R0..2 (operand) and of density rows from lane L+1
+template <class T, int R0, bool OPERAND>
+__device__ __forceinline__ void p2m_exchange_down(P2Lane<T>& L) {
+  if (OPERAND) {
+#pragma unroll
+    for (int r = R0; r <= 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const T v = shfl_down1(L.U[r][0][c]);
+        if (!L.edge) L.U[r][2][c] = v;
+      }
+  }
+#pragma unroll
+  for (int r = (R0 == 0 ? 0 : 1); r <= 1; ++r) {
+    const T v = shfl_down1(L.X[r][0]);
+    if (!L.edge) L.X[r][1] = v;
+  }
 }
 
-template <class T, int NC, int MODE>
-__global__ void __launch_bounds__(kRowThreads_) k_p1_smooth(P1Params<T, NC> P, SmoothBufs<T> B) {
+// element results of column 2 to lane L+1's column 0
+template <class T>
+__device__ __forceinline__ void p2m_exchange_up(P2Lane<T>& L, int lane) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const T v = shfl_up1(L.A[r][2][c]);
+      if (lane > 0) L.A[r][0][c] += v;
+    }
+}
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
+    k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
+  io.mode = MODE;  // compile-time mode: the per-node switches fold
+  constexpr bool OPERAND = MODE != kP2Diag;
+  const int lane = threadIdx.x & 31;
+  const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
+  if (js >= P.ny) return;  // whole warp
+  const int je = min(js + seg, P.ny);
+  P2Lane<T> L;
+  P2March<T>::begin(L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
+  const bool owner = lane > 0 && L.i <= P.nx;
+  int j = js > 0 ? js - 1 : 0;
+  P2March<T>::template load<0>(P, io, xi, L, j);
+  p2m_exchange_down<T, 0, OPERAND>(L);
+  for (;;) {
+    P2March<T>::compute(P, L, j, MODE);
+    p2m_exchange_up<T>(L, lane);
+    if (owner && j >= js) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2);
+    if (++j >= je) break;
+    P2March<T>::advance(L);
+    P2March<T>::template load<1>(P, io, xi, L, j);
+    p2m_exchange_down<T, 1, OPERAND>(L);
+  }
+}
+
+template <class T, int NC, int MODE, class PP>
+__global__ void __launch_bounds__(kRowThreads_) k_p1_smooth(PP P, SmoothBufs<T> B) {
   const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
   if (a > P.nx) return;
   if (MODE == kP2Pre) P1Smooth<T, NC>::pre(a, b, P, B);
@@ -62,6 +119,12 @@ template <class T, int NC>
 __global__ void __launch_bounds__(kRowThreads) k_p1_diag(P1Params<T, NC> P, T* __restrict__ d) {
   const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
   if (a <= P.nx) P1Kern<T, NC>::node_diag(a, b, P, d);
+}
+
+template <class T, int NC>
+__global__ void __launch_bounds__(kRowThreads) k_p1_stencil(P1Params<T, NC> P, T* __restrict__ st) {
+  const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
+  if (a <= P.nx) p1_stencil_node<T, NC>(a, b, P, st + (size_t(b) * (P.nx + 1) + a) * StencilLayout<NC>::stride);
 }
 
 template <class T, int NC>
@@ -163,125 +226,172 @@ __global__ void k_dense_matvec(const T* __restrict__ Ainv, const T* __restrict__
 
 // ---------------------------------------------------------------------------
 // coarse-level tail: the V-cycle over the smallest levels runs in one CTA with
-// every work vector resident in shared memory (one launch for ~6 x levels
-// phases; read-only data -- coefficients, D^-1, element matrices -- via L1)
+// every work vector, the stencils and D^-1 resident in shared memory (one
+// launch instead of ~6 x levels; the phases touch no global memory)
 // ---------------------------------------------------------------------------
 constexpr int kTailThreads = 1024;
 constexpr int kTailMaxLevels = 10;
-constexpr int kTailMaxNodes = 4096;
-constexpr size_t kTailSmemBudget = 160 * 1024;
+constexpr size_t kTailSmemBudget = 196 * 1024;
+constexpr int kTailTraceSlots = 64;  // [0, 62]: SM cycles per phase, [63]: launches
 
 template <class T, int NC>
 struct TailLevel {
-  P1Params<T, NC> P;
+  P1Stencil<T, NC> S;
   Transfer X;  // to the next coarser level
   const T* dinv;
   const double* cheb;
   int NX, nn, off;  // off: first of this level's five shared vectors x, b, r, d, x2 (NC*nn each)
+  int soff, doff;   // shared copies of the stencil (stride*nn) and of dinv (NC*nn)
 };
 
 template <class T, int NC>
 struct TailDesc {
   int nlev, smem_elems;
   const T* cinv;
+  long long* trace;  // opt-in phase timing (null: off)
   TailLevel<T, NC> lv[kTailMaxLevels];
 };
 
 template <class T, int NC>
 __global__ void __launch_bounds__(kTailThreads)
     k_tail_vcycle(const TailDesc<T, NC>* __restrict__ D, const T* __restrict__ b_in, T* __restrict__ x_out) {
+  __shared__ TailLevel<T, NC> lv[kTailMaxLevels];
+  __shared__ T cinv[kCoarseMaxDofs * kCoarseMaxDofs];
   extern __shared__ __align__(16) unsigned char tail_raw[];
   T* sm = reinterpret_cast<T*>(tail_raw);
+  const int tid = threadIdx.x, nt = blockDim.x;
   const int nlev = D->nlev;
-  auto bufs = [&](int l) {
-    const TailLevel<T, NC>& L = D->lv[l];
-    const int m = NC * L.nn;
-    T* base = sm + L.off;
-    return SmoothBufs<T>{base + m, L.dinv, base, base + 4 * m, base + 2 * m, base + 3 * m, L.cheb};
-  };
   {
-    const int m = NC * D->lv[0].nn;
-    T* b0 = sm + D->lv[0].off + m;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) b0[i] = b_in[i];
+    const int* src = reinterpret_cast<const int*>(D->lv);
+    int* dst = reinterpret_cast<int*>(lv);
+    const int words = int(sizeof(TailLevel<T, NC>) / sizeof(int)) * nlev;
+    for (int i = tid; i < words; i += nt) dst[i] = src[i];
   }
   __syncthreads();
+  for (int l = 0; l < nlev; ++l) {
+    const TailLevel<T, NC>& L = lv[l];
+    const int ns = StencilLayout<NC>::stride * L.nn;
+    for (int i = tid; i < ns; i += nt) sm[L.soff + i] = L.S.s[i];
+    for (int i = tid; i < NC * L.nn; i += nt) sm[L.doff + i] = L.dinv[i];
+  }
+  {
+    const int mc = NC * lv[nlev - 1].nn;
+    for (int i = tid; i < mc * mc; i += nt) cinv[i] = D->cinv[i];
+    const int m = NC * lv[0].nn;
+    T* b0 = sm + lv[0].off + m;
+    for (int i = tid; i < m; i += nt) b0[i] = b_in[i];
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int l = 0; l < nlev; ++l) {
+      lv[l].S.s = sm + lv[l].soff;
+      lv[l].dinv = sm + lv[l].doff;
+    }
+  __syncthreads();
+  // opt-in timing: SM cycles of every phase in execution order
+  long long* const trace = tid == 0 ? D->trace : nullptr;
+  long long t_prev = clock64();
+  int slot = 1;
+  auto mark = [&]() {
+    __syncthreads();
+    if (!trace) return;
+    const long long t = clock64();
+    if (slot < kTailTraceSlots - 1) trace[slot++] += t - t_prev;
+    t_prev = t;
+  };
+  auto bufs = [&](int l) {
+    const int m = NC * lv[l].nn;
+    T* base = sm + lv[l].off;
+    return SmoothBufs<T>{base + m, lv[l].dinv, base, base + 4 * m, base + 2 * m, base + 3 * m, lv[l].cheb};
+  };
   for (int l = 0; l + 1 < nlev; ++l) {
-    const TailLevel<T, NC>& L = D->lv[l];
+    const TailLevel<T, NC>& L = lv[l];
     const SmoothBufs<T> B = bufs(l);
-    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+    for (int n = tid; n < L.nn; n += nt) {
       const int b = n / L.NX, a = n - b * L.NX;
-      P1Smooth<T, NC>::pre(a, b, L.P, B);
+      P1Smooth<T, NC>::pre(a, b, L.S, B);
     }
-    __syncthreads();
-    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+    mark();
+    for (int n = tid; n < L.nn; n += nt) {
       const int b = n / L.NX, a = n - b * L.NX;
-      P1Smooth<T, NC>::res(a, b, L.P, B);
+      P1Smooth<T, NC>::res(a, b, L.S, B);
     }
-    __syncthreads();
-    const TailLevel<T, NC>& C = D->lv[l + 1];
+    mark();
+    const TailLevel<T, NC>& C = lv[l + 1];
     T* bc = sm + C.off + NC * C.nn;
-    for (int n = threadIdx.x; n < C.nn; n += blockDim.x) {
+    for (int n = tid; n < C.nn; n += nt) {
       const int J = n / C.NX, I = n - J * C.NX;
       TransferKern<T, NC>::node_restrict(I, J, L.X, B.r, bc);
     }
-    __syncthreads();
+    mark();
   }
-  {
-    const TailLevel<T, NC>& C = D->lv[nlev - 1];
+  {  // coarsest level: dense inverse
+    const TailLevel<T, NC>& C = lv[nlev - 1];
     const int m = NC * C.nn;
     const T* bc = sm + C.off + m;
     T* xc = sm + C.off;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    for (int i = tid; i < m; i += nt) {
       T acc = T(0);
-      for (int j = 0; j < m; ++j) acc += D->cinv[size_t(i) * m + j] * bc[j];
+#pragma unroll 8
+      for (int j = 0; j < m; ++j) acc += cinv[i * m + j] * bc[j];
       xc[i] = acc;
     }
-    __syncthreads();
+    mark();
   }
   for (int l = nlev - 2; l >= 0; --l) {
-    const TailLevel<T, NC>& L = D->lv[l];
+    const TailLevel<T, NC>& L = lv[l];
     const SmoothBufs<T> B = bufs(l);
-    const T* xc = sm + D->lv[l + 1].off;
-    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+    const T* xc = sm + lv[l + 1].off;
+    for (int n = tid; n < L.nn; n += nt) {
       const int b = n / L.NX, a = n - b * L.NX;
       TransferKern<T, NC>::node_prolong_add(a, b, L.X, xc, B.x);
     }
-    __syncthreads();
-    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+    mark();
+    for (int n = tid; n < L.nn; n += nt) {
       const int b = n / L.NX, a = n - b * L.NX;
-      P1Smooth<T, NC>::first(a, b, L.P, B);
+      P1Smooth<T, NC>::first(a, b, L.S, B);
     }
-    __syncthreads();
-    for (int n = threadIdx.x; n < L.nn; n += blockDim.x) {
+    mark();
+    for (int n = tid; n < L.nn; n += nt) {
       const int b = n / L.NX, a = n - b * L.NX;
-      P1Smooth<T, NC>::post2(a, b, L.P, B);
+      P1Smooth<T, NC>::post2(a, b, L.S, B);
+      if (l == 0)
+        for (int c = 0; c < NC; ++c) x_out[NC * n + c] = B.x[NC * n + c];
     }
-    __syncthreads();
+    mark();
   }
-  {
-    const int m = NC * D->lv[0].nn;
-    const T* x0 = sm + D->lv[0].off;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) x_out[i] = x0[i];
-  }
+  if (trace) trace[kTailTraceSlots - 1] += 1;
 }
 
 // ---------------------------------------------------------------------------
 // host helpers
 // ---------------------------------------------------------------------------
-template <class T>
-inline void set_p2_smem_attr() {
-  static bool done = false;
-  if (!done) {
-    cudaFuncSetAttribute(k_p2_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(P2Smem<T>)));
-    done = true;
+inline int device_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 1;
   }
+  return cached[dev];
 }
 
 template <class T>
 inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
-  set_p2_smem_attr<T>();
-  dim3 g((P.nx + P2_TX - 1) / P2_TX, (P.ny + P2_TY - 1) / P2_TY);
-  k_p2_tile<T><<<g, P2_THREADS, sizeof(P2Smem<T>), s>>>(P, xi, io);
+  const int seg = p2_march_segment(P.nx, P.ny, device_sms());
+  const int nseg = (P.ny + seg - 1) / seg;
+  const dim3 g((P.nx + 1 + P2M_OWN - 1) / P2M_OWN, (nseg + P2M_WARPS - 1) / P2M_WARPS);
+  switch (io.mode) {
+    case kP2Apply: k_p2_march<T, kP2Apply><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    case kP2Diag: k_p2_march<T, kP2Diag><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    case kP2Pre: k_p2_march<T, kP2Pre><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    case kP2Res: k_p2_march<T, kP2Res><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    case kP2First: k_p2_march<T, kP2First><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    default: k_p2_march<T, kP2Post2><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+  }
 }
 
 template <class T>
@@ -417,6 +527,8 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
     if (!specs[l].p2) {
       v.kK = arena.alloc_n<T>(specs[l].ntri());
       if (specs[l].NC == 1) v.kM = arena.alloc_n<T>(specs[l].ntri());
+      if (specs[l].nn() <= kStencilMaxNodes)
+        v.st = arena.alloc_n<T>(specs[l].nn() * (specs[l].NC == 2 ? StencilLayout<2>::stride : StencilLayout<1>::stride));
     }
   }
   const size_t n0 = specs[0].ndof();
@@ -429,7 +541,6 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   if (!hdev_) cudaMallocHost(&hdev_, sizeof(PcgDev));
   for (auto& c : cap_)
     if (!c) cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
-  set_p2_smem_attr<T>();
   graph_valid_ = false;
   build_tail(arena);
 }
@@ -442,11 +553,13 @@ void MG<T>::build_tail(Arena& arena) {
   tail_desc_ = nullptr;
   tail_smem_ = 0;
   const int L = levels();
+  const int stride = specs_[L - 1].NC == 2 ? StencilLayout<2>::stride : StencilLayout<1>::stride;
   size_t bytes = 0;
   int first = L;
   for (int l = L - 1; l >= 1; --l) {
-    const size_t add = 5 * specs_[l].ndof() * sizeof(T);
-    if (specs_[l].nn() > size_t(kTailMaxNodes) || bytes + add > kTailSmemBudget || L - l > kTailMaxLevels) break;
+    // five vectors, the inverse diagonal and the stencil
+    const size_t add = (6 * specs_[l].ndof() + size_t(stride) * specs_[l].nn()) * sizeof(T);
+    if (specs_[l].p2 || !lv_[l].st || bytes + add > kTailSmemBudget || L - l > kTailMaxLevels) break;
     bytes += add;
     first = l;
   }
@@ -461,7 +574,7 @@ void MG<T>::build_tail(Arena& arena) {
     for (int k = 0; k < h.nlev; ++k) {
       const int l = first + k;
       TailLevel<T, NC>& d = h.lv[k];
-      d.P = make_p1<T, NC>(specs_[l], refs_[l], lv_[l].kK, NC == 1 ? lv_[l].kM : nullptr);
+      d.S = P1Stencil<T, NC>{specs_[l].nx, specs_[l].ny, specs_[l].dir, lv_[l].st};
       if (l + 1 < L) d.X = make_transfer(specs_[l], specs_[l + 1]);
       d.dinv = lv_[l].dinv;
       d.cheb = cheb_ + 8 * l;
@@ -470,7 +583,20 @@ void MG<T>::build_tail(Arena& arena) {
       d.off = off;
       off += 5 * NC * d.nn;
     }
+    for (int k = 0; k < h.nlev; ++k) {
+      TailLevel<T, NC>& d = h.lv[k];
+      d.soff = off;
+      off += StencilLayout<NC>::stride * d.nn;
+      d.doff = off;
+      off += NC * d.nn;
+    }
     h.smem_elems = off;
+    h.trace = nullptr;
+    if (profile_levels) {
+      h.trace = static_cast<long long*>(arena.alloc(kTailTraceSlots * sizeof(long long)));
+      if (h.trace) cudaMemset(h.trace, 0, kTailTraceSlots * sizeof(long long));
+      tail_trace_ = h.trace;
+    }
     void* p = arena.alloc(sizeof(h));
     if (!p) return;
     cudaMemcpy(p, &h, sizeof(h), cudaMemcpyHostToDevice);
@@ -576,6 +702,12 @@ int MG<T>::setup(cudaStream_t s) {
       k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kK, kK64_[l], 1.0, S.ntri());
       if (v.kM) k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kM, kM64_[l], 1.0, S.ntri());
       launches += v.kM ? 2 : 1;
+      if (v.st) {
+        const dim3 gr = row_grid(S.NX, S.NY);
+        if (S.NC == 2) k_p1_stencil<T, 2><<<gr, kRowThreads, 0, s>>>(make_p1<T, 2>(S, refs_[l], v.kK, nullptr), v.st);
+        else k_p1_stencil<T, 1><<<gr, kRowThreads, 0, s>>>(make_p1<T, 1>(S, refs_[l], v.kK, v.kM), v.st);
+        launches += 1;
+      }
     }
   }
   for (int l = 0; l < L; ++l) {
@@ -626,11 +758,56 @@ int MG<T>::setup(cudaStream_t s) {
 // One V-cycle from level l down: fused degree-2 Chebyshev pre-smoothing from
 // x = 0, residual restriction, coarse correction, fused post-smoothing.
 template <class T>
+void MG<T>::tail_profile(std::vector<long long>& cycles) const {
+  cycles.clear();
+  if (!tail_trace_) return;
+  cycles.resize(kTailTraceSlots);
+  cudaMemcpy(cycles.data(), tail_trace_, kTailTraceSlots * sizeof(long long), cudaMemcpyDeviceToHost);
+}
+
+template <class T>
+void MG<T>::flush_level_profile() {
+  if (prof_events_.empty()) return;
+  cudaDeviceSynchronize();
+  if (level_ms.size() < specs_.size()) {
+    level_ms.assign(specs_.size(), 0.0);
+    level_calls.assign(specs_.size(), 0);
+  }
+  for (auto& pe : prof_events_) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, pe.second.first, pe.second.second);
+    level_ms[pe.first] += ms;
+    level_calls[pe.first] += 1;
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  prof_events_.clear();
+}
+
+template <class T>
 void MG<T>::vcycle_level(int l, const T* b, T* x, cudaStream_t s) {
+  if (profile_levels && !use_graphs) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    prof_depth_ += 1;
+    vcycle_level_body(l, b, x, s);
+    prof_depth_ -= 1;
+    cudaEventRecord(e1, s);
+    prof_events_.push_back({l, {e0, e1}});
+    if (prof_events_.size() > 4096) flush_level_profile();
+    return;
+  }
+  vcycle_level_body(l, b, x, s);
+}
+
+template <class T>
+void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   Lev& v = lv_[l];
   const int L = levels();
   const LevelSpec& S = specs_[l];
-  if (l == tail_ && tail_desc_) {
+  if (l == tail_ && tail_desc_ && use_tail) {
     if (S.NC == 2)
       k_tail_vcycle<T, 2><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);
     else
@@ -667,21 +844,29 @@ void MG<T>::vcycle_level(int l, const T* b, T* x, cudaStream_t s) {
     launches += 3;
     return;
   }
-  auto run = [&](auto nc_tag) {
+  // the level's operator: assembled stencil when there is one, else on the fly
+  auto run = [&](auto nc_tag, const auto& P) {
     constexpr int NC = decltype(nc_tag)::value;
-    const auto P = make_p1<T, NC>(S, refs_[l], v.kK, NC == 1 ? v.kM : nullptr);
-    k_p1_smooth<T, NC, kP2Pre><<<gf, kRowThreads, 0, s>>>(P, B);
-    k_p1_smooth<T, NC, kP2Res><<<gf, kRowThreads, 0, s>>>(P, B);
+    using PP = std::decay_t<decltype(P)>;
+    k_p1_smooth<T, NC, kP2Pre, PP><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_p1_smooth<T, NC, kP2Res, PP><<<gf, kRowThreads, 0, s>>>(P, B);
     k_restrict<T, NC><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
     k_prolong_add<T, NC><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
-    k_p1_smooth<T, NC, kP2First><<<gf, kRowThreads, 0, s>>>(P, B);
-    k_p1_smooth<T, NC, kP2Post2><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_p1_smooth<T, NC, kP2First, PP><<<gf, kRowThreads, 0, s>>>(P, B);
+    k_p1_smooth<T, NC, kP2Post2, PP><<<gf, kRowThreads, 0, s>>>(P, B);
     launches += 3;
   };
-  if (S.NC == 2) run(std::integral_constant<int, 2>{});
-  else run(std::integral_constant<int, 1>{});
+  using I2 = std::integral_constant<int, 2>;
+  using I1 = std::integral_constant<int, 1>;
+  if (S.NC == 2) {
+    if (v.st) run(I2{}, P1Stencil<T, 2>{S.nx, S.ny, S.dir, v.st});
+    else run(I2{}, make_p1<T, 2>(S, refs_[l], v.kK, nullptr));
+  } else {
+    if (v.st) run(I1{}, P1Stencil<T, 1>{S.nx, S.ny, S.dir, v.st});
+    else run(I1{}, make_p1<T, 1>(S, refs_[l], v.kK, v.kM));
+  }
 }
 
 template <class T>

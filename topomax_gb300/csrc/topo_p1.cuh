@@ -222,6 +222,105 @@ struct TransferKern {
 namespace topo {
 
 // ---------------------------------------------------------------------------
+// assembled 7-point stencil of a P1 level
+// ---------------------------------------------------------------------------
+// On the right-diagonal triangulation node (a,b) couples to itself and to
+// (a+-1,b), (a,b+-1), (a+1,b+1), (a-1,b-1).  For the small levels the NC x NC
+// coupling blocks are assembled once per coefficient update, so that a node
+// evaluation is seven independent block products instead of a chain through
+// six incidences' element matrices, coefficients and clamping tests (the
+// smallest levels are bound by that chain's latency, not by bandwidth).
+// Columns of clamped nodes are zero; a clamped node's own row is the
+// identity (its evaluation reports "clamped" as P1Kern does).
+template <int NC>
+struct StencilLayout {
+  static constexpr int stride = NC == 2 ? 28 : 8;  // values per node: 7 blocks, padded to 16 bytes
+};
+TOPO_HD constexpr int st_da(int k) { return k == 1 ? 1 : k == 2 ? -1 : k == 5 ? 1 : k == 6 ? -1 : 0; }
+TOPO_HD constexpr int st_db(int k) { return k == 3 ? 1 : k == 4 ? -1 : k == 5 ? 1 : k == 6 ? -1 : 0; }
+// block of offset (da, db): 0 self, 1 E, 2 W, 3 N, 4 S, 5 NE, 6 SW
+TOPO_HD int st_block(int da, int db) {
+  if (da == 0) return db == 0 ? 0 : db == 1 ? 3 : 4;
+  if (db == 0) return da == 1 ? 1 : 2;
+  return da == 1 ? 5 : 6;
+}
+
+template <class T, int NC>
+struct P1Stencil {
+  int nx, ny;  // cells of this level
+  Dir dir;
+  const T* s;  // node n, block k, row c, column d at s[n*stride + k*NC*NC + c*NC + d]
+};
+
+// Stencil row of node (a,b) assembled from the level's coefficients (the
+// same incidences and clamping rules as P1Kern::node_eval).
+template <class T, int NC>
+TOPO_HD void p1_stencil_node(int a, int b, const P1Params<T, NC>& P, T* out) {
+  constexpr int SB = NC * NC;
+  T blk[7 * SB];
+  for (int i = 0; i < 7 * SB; ++i) blk[i] = T(0);
+  for (int i = 7 * SB; i < StencilLayout<NC>::stride; ++i) out[i] = T(0);
+  if (is_clamped(P.dir, a, b)) {
+    for (int c = 0; c < NC; ++c) blk[c * NC + c] = T(1);
+  } else {
+    const bool chk = P1Kern<T, NC>::near_clamped(P.dir, a, b);
+    for (int e = 0; e < 6; ++e) {
+      int dci, dcj, o, loc;
+      p1_incidence(e, dci, dcj, o, loc);
+      const int ci = a + dci, cj = b + dcj;
+      if (ci < 0 || ci >= P.nx || cj < 0 || cj >= P.ny) continue;
+      const size_t t = (size_t(cj) * P.nx + ci) * 2 + o;
+      const T kk = P.kK ? P.kK[t] : P.kK_c;
+      const T km = (NC == 1) ? (P.kM ? P.kM[t] : P.kM_c) : T(0);
+      for (int L = 0; L < 3; ++L) {
+        const int al = ci + p1_off_a(o, L), bl = cj + p1_off_b(o, L);
+        if (chk && is_clamped(P.dir, al, bl)) continue;
+        T* bk = blk + st_block(al - a, bl - b) * SB;
+        for (int c = 0; c < NC; ++c)
+          for (int d = 0; d < NC; ++d) {
+            bk[c * NC + d] += kk * P.K[o][loc * NC + c][L * NC + d];
+            if (NC == 1) bk[0] += km * P.Mm[o][loc][L];
+          }
+      }
+    }
+  }
+  for (int i = 0; i < 7 * SB; ++i) out[i] = blk[i];
+}
+
+template <class T, int NC>
+struct P1StencilKern {
+  template <class F>
+  TOPO_HD static bool node_eval(int a, int b, const P1Stencil<T, NC>& P, const F& fetch, T (&acc)[NC]) {
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    if (!surely_free(P.dir, a, b) && is_clamped(P.dir, a, b)) return false;
+    const int NX = P.nx + 1, NY = P.ny + 1;
+    const T* sn = P.s + (size_t(b) * NX + a) * StencilLayout<NC>::stride;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int k = 0; k < 7; ++k) {
+      const int al = a + st_da(k), bl = b + st_db(k);
+      if (al < 0 || al >= NX || bl < 0 || bl >= NY) continue;
+      T ul[NC];
+      fetch(size_t(bl) * NX + al, al, bl, ul);
+      for (int c = 0; c < NC; ++c)
+        for (int d = 0; d < NC; ++d) acc[c] += sn[k * NC * NC + c * NC + d] * ul[d];
+    }
+    return true;
+  }
+};
+
+// node evaluation through either representation of a level
+template <class T, int NC, class F>
+TOPO_HD bool p1_node_eval(int a, int b, const P1Params<T, NC>& P, const F& f, T (&acc)[NC]) {
+  return P1Kern<T, NC>::node_eval(a, b, P, f, acc);
+}
+template <class T, int NC, class F>
+TOPO_HD bool p1_node_eval(int a, int b, const P1Stencil<T, NC>& P, const F& f, T (&acc)[NC]) {
+  return P1StencilKern<T, NC>::node_eval(a, b, P, f, acc);
+}
+
+// ---------------------------------------------------------------------------
 // fused degree-2 Chebyshev smoothing steps of one P1 level (node-centric)
 // ---------------------------------------------------------------------------
 // Buffers of one level for the fused V-cycle.
@@ -250,14 +349,15 @@ struct FetchPre {
 template <class T, int NC>
 struct P1Smooth {
   // PRE: x = d0 + d1 with d0 = c0 Dinv b, r1 = b - A d0, d1 = c1 d0 + c2 Dinv r1
-  TOPO_HD static void pre(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+  template <class PP>
+  TOPO_HD static void pre(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     const T c0 = T(B.cheb[0]), c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
     const FetchPre<T, NC> f{B.b, B.dinv, c0};
     T t[NC], u[NC];
     f(n, a, b, u);
-    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+    if (!p1_node_eval<T, NC>(a, b, P, f, t))
       for (int c = 0; c < NC; ++c) t[c] = u[c];
     for (int c = 0; c < NC; ++c) {
       const size_t i = NC * n + c;
@@ -266,22 +366,24 @@ struct P1Smooth {
     }
   }
   // RES: r = b - A x
-  TOPO_HD static void res(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+  template <class PP>
+  TOPO_HD static void res(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     T t[NC];
-    if (!P1Kern<T, NC>::node_eval(a, b, P, FetchArray<T, NC>{B.x}, t))
+    if (!p1_node_eval<T, NC>(a, b, P, FetchArray<T, NC>{B.x}, t))
       for (int c = 0; c < NC; ++c) t[c] = B.x[NC * n + c];
     for (int c = 0; c < NC; ++c) B.r[NC * n + c] = B.b[NC * n + c] - t[c];
   }
   // FIRST (after the coarse correction was added to x):
   // r0 = b - A x ; d0 = c0 Dinv r0 ; x2 = x + d0 (writes r, d, x2)
-  TOPO_HD static void first(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+  template <class PP>
+  TOPO_HD static void first(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     const T c0 = T(B.cheb[0]);
     T t[NC];
-    if (!P1Kern<T, NC>::node_eval(a, b, P, FetchArray<T, NC>{B.x}, t))
+    if (!p1_node_eval<T, NC>(a, b, P, FetchArray<T, NC>{B.x}, t))
       for (int c = 0; c < NC; ++c) t[c] = B.x[NC * n + c];
     for (int c = 0; c < NC; ++c) {
       const size_t i = NC * n + c;
@@ -293,13 +395,14 @@ struct P1Smooth {
     }
   }
   // POST2: r1 = r0 - A d0 ; d1 = c1 d0 + c2 Dinv r1 ; x = x2 + d1
-  TOPO_HD static void post2(int a, int b, const P1Params<T, NC>& P, const SmoothBufs<T>& B) {
+  template <class PP>
+  TOPO_HD static void post2(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     const T c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
     const FetchArray<T, NC> f{B.d};
     T t[NC];
-    if (!P1Kern<T, NC>::node_eval(a, b, P, f, t))
+    if (!p1_node_eval<T, NC>(a, b, P, f, t))
       for (int c = 0; c < NC; ++c) t[c] = B.d[NC * n + c];
     for (int c = 0; c < NC; ++c) {
       const size_t i = NC * n + c;

@@ -181,27 +181,28 @@ TOPO_HD void tri_diag(int o, const T (&xi)[3], const P2Params<T>& P, T (&d)[6][2
 }
 
 // ---------------------------------------------------------------------------
-// tiled kernel phases
+// column-march kernel phases
 // ---------------------------------------------------------------------------
-constexpr int P2_TX = 32;  // owned cells per tile in x
-constexpr int P2_TY = 8;   // owned cells per tile in y
-constexpr int P2_THREADS = 320;  // one thread per computed cell (33 x 9 = 297)
+// One warp covers 32 consecutive cell columns i = i0-1 .. i0+30 and marches
+// upward through a segment of cell rows.  At step j, lane L works on cell
+// (i0-1+L, j): it holds the operand at the cell's 3x3 nodes (2i+c, 2j+r),
+// the density at its 2x2 vertices and the element results at the same nodes.
+//  * column 2 of a lane is column 0 of the next lane: operand and density
+//    come down from lane L+1 by a shuffle (the last lane loads its own);
+//  * row 2 of a step is row 0 of the next step: kept in registers;
+//  * element results of column 2 go up to lane L+1, which adds them to its
+//    column 0; results of row 2 are carried to the next step.
+// After a step a lane therefore holds the complete sums at its nodes of rows
+// 0,1 and columns 0,1 and finishes them (apply, diagonal or a smoothing
+// update).  Lane 0 only feeds lane 1 (its own nodes belong to the previous
+// warp), and the first step of a segment recomputes the cell row below it
+// (whose results only complete row 0).  No shared memory, no block barriers:
+// the nodes move through registers once per launch.
+constexpr int P2M_OWN = 31;                   // owned cell columns per warp
+constexpr int P2M_WARPS = 4;                  // warps per block, one row segment each
+constexpr int P2M_THREADS = 32 * P2M_WARPS;
 
-struct P2Tile {
-  static constexpr int CX = P2_TX + 1, CY = P2_TY + 1;  // computed cells (1-cell halo at low side)
-  static constexpr int NCELL = CX * CY;
-  static constexpr int NTX = 2 * CX + 1, NTY = 2 * CY + 1;
-  static constexpr int VX = CX + 1, VY = CY + 1;
-};
-
-template <class T>
-struct P2Smem {
-  T u[P2Tile::NTY][P2Tile::NTX][2];
-  T xi[P2Tile::VY][P2Tile::VX];
-  T out[2][12][P2Tile::NCELL];  // per orientation, node x component, cell (conflict-free)
-};
-
-// What one launch of the tiled P2 kernel computes.
+// What one launch of the P2 kernel computes.
 enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2First = 4, kP2Post2 = 5 };
 
 template <class T>
@@ -213,11 +214,18 @@ struct P2Io {
 };
 
 template <class T>
-struct P2Kern {
-  using Smem = P2Smem<T>;
+struct P2Lane {
+  int i;          // cell column
+  bool edge;      // last lane of the warp: loads its column 2 itself
+  T U[3][3][2];   // operand at nodes (2i+c, 2j+r), zero at clamped nodes
+  T X[2][2];      // density at vertices (i+c, j+r)
+  T A[3][3][2];   // element results at the same nodes
+};
 
-  // operand of the apply at node n = (a,b) for the launch's mode
-  TOPO_HD static void operand(const P2Io<T>& io, size_t n, int a, int b, T (&v)[2]) {
+template <class T>
+struct P2March {
+  // operand of the apply at node n for the launch's mode
+  TOPO_HD static void operand(const P2Io<T>& io, size_t n, T (&v)[2]) {
     switch (io.mode) {
       case kP2Pre: {
         const T c0 = T(io.B.cheb[0]);
@@ -235,156 +243,178 @@ struct P2Kern {
     }
   }
 
-  TOPO_HD static void load(int tid, int nt, int bx, int by, const P2Params<T>& P,
-                           const P2Io<T>& io, const T* xi, Smem& s) {
-    const int i0 = bx * P2_TX, j0 = by * P2_TY;
-    const int A0 = 2 * (i0 - 1), B0 = 2 * (j0 - 1);
+  // operand at node (a,b); zero outside the lattice and at clamped nodes
+  TOPO_HD static void fetch(const P2Params<T>& P, const P2Io<T>& io, int a, int b, T (&v)[2]) {
     const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+    v[0] = v[1] = T(0);
+    if (a >= 0 && a < NX && b >= 0 && b < NY && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b)))
+      operand(io, size_t(b) * NX + a, v);
+  }
+
+  TOPO_HD static T density(const P2Params<T>& P, const T* xi, int i, int j) {
+    const int VX = P.nx + 1, VY = P.ny + 1;
+    return (i >= 0 && i < VX && j >= 0 && j < VY) ? xi[size_t(j) * VX + i] : T(0);
+  }
+
+  // loads of step j: operand rows R0..2 and density rows (R0 == 0 ? 0 : 1)..1,
+  // columns 0 (and, on the edge lane, the last column)
+  template <int R0>
+  TOPO_HD static void load(const P2Params<T>& P, const P2Io<T>& io, const T* xi, P2Lane<T>& L, int j) {
     if (io.mode != kP2Diag) {
-      for (int idx = tid; idx < P2Tile::NTX * P2Tile::NTY; idx += nt) {
-        const int bl = idx / P2Tile::NTX, al = idx - bl * P2Tile::NTX;
-        const int a = A0 + al, b = B0 + bl;
-        T v[2] = {T(0), T(0)};
-        if (a >= 0 && a < NX && b >= 0 && b < NY && !is_clamped(P.dir, a, b))
-          operand(io, size_t(b) * NX + a, a, b, v);
-        s.u[bl][al][0] = v[0];
-        s.u[bl][al][1] = v[1];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+      for (int r = R0; r <= 2; ++r) {
+        const int b = 2 * j + r;
+        fetch(P, io, 2 * L.i, b, L.U[r][0]);
+        fetch(P, io, 2 * L.i + 1, b, L.U[r][1]);
+        if (L.edge) fetch(P, io, 2 * L.i + 2, b, L.U[r][2]);
       }
     }
-    const int VXg = P.nx + 1, VYg = P.ny + 1;
-    for (int idx = tid; idx < P2Tile::VX * P2Tile::VY; idx += nt) {
-      const int jl = idx / P2Tile::VX, il = idx - jl * P2Tile::VX;
-      const int i = i0 - 1 + il, j = j0 - 1 + jl;
-      s.xi[jl][il] = (i >= 0 && i < VXg && j >= 0 && j < VYg) ? xi[size_t(j) * VXg + i] : T(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = (R0 == 0 ? 0 : 1); r <= 1; ++r) {
+      L.X[r][0] = density(P, xi, L.i, j + r);
+      if (L.edge) L.X[r][1] = density(P, xi, L.i + 1, j + r);
     }
   }
 
   template <int O>
-  TOPO_HD static void tri(const P2Params<T>& P, const Smem& s, int ci, int cj, int ig, int jg, int mode,
-                          T (&y)[6][2]) {
-    T xe[3];
-    xe[0] = s.xi[cj + P1Off<O, 0>::b][ci + P1Off<O, 0>::a];
-    xe[1] = s.xi[cj + P1Off<O, 1>::b][ci + P1Off<O, 1>::a];
-    xe[2] = s.xi[cj + P1Off<O, 2>::b][ci + P1Off<O, 2>::a];
-    if (mode == 1) {
+  TOPO_HD static void tri(const P2Params<T>& P, P2Lane<T>& L, int j, int mode) {
+    const T xe[3] = {L.X[P1Off<O, 0>::b][P1Off<O, 0>::a], L.X[P1Off<O, 1>::b][P1Off<O, 1>::a],
+                     L.X[P1Off<O, 2>::b][P1Off<O, 2>::a]};
+    T y[6][2];
+    if (mode == kP2Diag) {
       tri_diag(O, xe, P, y);
+    } else {
+      T ue[6][2];
+#define TOPO_LD(K)                                             \
+  ue[K][0] = L.U[P2Off<O, K>::b][P2Off<O, K>::a][0];           \
+  ue[K][1] = L.U[P2Off<O, K>::b][P2Off<O, K>::a][1];
+      TOPO_LD(0) TOPO_LD(1) TOPO_LD(2) TOPO_LD(3) TOPO_LD(4) TOPO_LD(5)
+#undef TOPO_LD
+      if (P.rmass) {
+        const size_t nc = size_t(P.nx) * P.ny, c = size_t(j) * P.nx + L.i;
+        const T* m = P.rmass + size_t(O) * 6 * nc + c;
+        T M[6];
+        for (int k = 0; k < 6; ++k) M[k] = m[k * nc];
+        tri_apply_m<O>(ue, M, P, y);
+      } else {
+        tri_apply<O>(ue, xe, P, y);
+      }
+    }
+#define TOPO_ST(K)                                             \
+  L.A[P2Off<O, K>::b][P2Off<O, K>::a][0] += y[K][0];           \
+  L.A[P2Off<O, K>::b][P2Off<O, K>::a][1] += y[K][1];
+    TOPO_ST(0) TOPO_ST(1) TOPO_ST(2) TOPO_ST(3) TOPO_ST(4) TOPO_ST(5)
+#undef TOPO_ST
+  }
+
+  // element results of cell (L.i, j), both triangles
+  TOPO_HD static void compute(const P2Params<T>& P, P2Lane<T>& L, int j, int mode) {
+    if (L.i < 0 || L.i >= P.nx || j < 0 || j >= P.ny) return;
+    tri<0>(P, L, j, mode);
+    tri<1>(P, L, j, mode);
+  }
+
+  // finish node (a,b) with the complete sum r (clamped rows act as identity rows)
+  TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, const T (&sum)[2],
+                                  const T (&u)[2]) {
+    const int NX = 2 * P.nx + 1;
+    const size_t n = size_t(b) * NX + a;
+    const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
+    if (io.mode == kP2Diag) {
+      io.y[2 * n] = cl ? T(1) : sum[0];
+      io.y[2 * n + 1] = cl ? T(1) : sum[1];
       return;
     }
-    const int a0 = 2 * ci, b0 = 2 * cj;
-    T ue[6][2];
-#define TOPO_LD(K)                                                           \
-  ue[K][0] = s.u[b0 + P2Off<O, K>::b][a0 + P2Off<O, K>::a][0];              \
-  ue[K][1] = s.u[b0 + P2Off<O, K>::b][a0 + P2Off<O, K>::a][1];
-    TOPO_LD(0) TOPO_LD(1) TOPO_LD(2) TOPO_LD(3) TOPO_LD(4) TOPO_LD(5)
-#undef TOPO_LD
-    if (P.rmass) {
-      const size_t nc = size_t(P.nx) * P.ny, c = size_t(jg) * P.nx + ig;
-      const T* m = P.rmass + size_t(O) * 6 * nc + c;
-      T M[6];
-      for (int k = 0; k < 6; ++k) M[k] = m[k * nc];
-      tri_apply_m<O>(ue, M, P, y);
-    } else {
-      tri_apply<O>(ue, xe, P, y);
+    T un[2] = {u[0], u[1]}, r[2] = {sum[0], sum[1]};
+    if (cl) {
+      operand(io, n, un);  // the loaded copy is zero at clamped nodes
+      r[0] = un[0];
+      r[1] = un[1];
     }
-  }
-
-  // mode 0: operator apply, mode 1: diagonal.  One thread per computed cell,
-  // both triangles (orientation is a compile-time parameter: no divergence).
-  TOPO_HD static void compute(int tid, int nt, int bx, int by, const P2Params<T>& P, Smem& s, int mode) {
-    const int i0 = bx * P2_TX, j0 = by * P2_TY;
-    for (int cell = tid; cell < P2Tile::NCELL; cell += nt) {
-      const int cj = cell / P2Tile::CX, ci = cell - cj * P2Tile::CX;
-      const int ig = i0 - 1 + ci, jg = j0 - 1 + cj;
-      const bool valid = ig >= 0 && ig < P.nx && jg >= 0 && jg < P.ny;
-      T y[6][2];
-      if (valid) tri<0>(P, s, ci, cj, ig, jg, mode, y);
-      for (int k = 0; k < 6; ++k) {
-        s.out[0][2 * k][cell] = valid ? y[k][0] : T(0);
-        s.out[0][2 * k + 1][cell] = valid ? y[k][1] : T(0);
-      }
-      if (valid) tri<1>(P, s, ci, cj, ig, jg, mode, y);
-      for (int k = 0; k < 6; ++k) {
-        s.out[1][2 * k][cell] = valid ? y[k][0] : T(0);
-        s.out[1][2 * k + 1][cell] = valid ? y[k][1] : T(0);
-      }
-    }
-  }
-
-  TOPO_HD static T tri_val(const Smem& s, int ci, int cj, int o, int k, int c) {
-    if (ci < 0 || ci >= P2Tile::CX || cj < 0 || cj >= P2Tile::CY) return T(0);
-    return s.out[o][2 * k + c][cj * P2Tile::CX + ci];
-  }
-
-  // Sum the per-triangle results onto the tile's owned nodes and finish the
-  // mode's update there (clamped rows act as identity rows).
-  TOPO_HD static void gather(int tid, int nt, int bx, int by, const P2Params<T>& P,
-                             const Smem& s, const P2Io<T>& io) {
-    const int mode = io.mode;
-    const int i0 = bx * P2_TX, j0 = by * P2_TY;
-    const int NX = 2 * P.nx + 1;
-    const int a_beg = 2 * i0, b_beg = 2 * j0;
-    const int a_end = (i0 + P2_TX >= P.nx) ? 2 * P.nx + 1 : 2 * (i0 + P2_TX);
-    const int b_end = (j0 + P2_TY >= P.ny) ? 2 * P.ny + 1 : 2 * (j0 + P2_TY);
-    const int na = a_end - a_beg, nb = b_end - b_beg;
-    for (int idx = tid; idx < na * nb; idx += nt) {
-      const int q = idx / na;
-      const int a = a_beg + (idx - q * na), b = b_beg + q;
-      const int al = a - 2 * (i0 - 1), bl = b - 2 * (j0 - 1);
-      const int I = al >> 1, J = bl >> 1, pa = al & 1, pb = bl & 1;
-      const size_t n = size_t(b) * NX + a;
-      T r[2];
-      for (int c = 0; c < 2; ++c) {
-        T v;
-        if (!pa && !pb) {
-          v = tri_val(s, I - 1, J - 1, 0, 2, c) + tri_val(s, I - 1, J - 1, 1, 2, c) +
-              tri_val(s, I, J - 1, 1, 1, c) + tri_val(s, I - 1, J, 0, 1, c) +
-              tri_val(s, I, J, 0, 0, c) + tri_val(s, I, J, 1, 0, c);
-        } else if (pa && !pb) {
-          v = tri_val(s, I, J, 0, 5, c) + tri_val(s, I, J - 1, 1, 3, c);
-        } else if (!pa && pb) {
-          v = tri_val(s, I, J, 1, 5, c) + tri_val(s, I - 1, J, 0, 3, c);
-        } else {
-          v = tri_val(s, I, J, 0, 4, c) + tri_val(s, I, J, 1, 4, c);
+    const SmoothBufs<T>& B = io.B;
+    for (int c = 0; c < 2; ++c) {
+      const size_t i = 2 * n + c;
+      switch (io.mode) {
+        case kP2Apply: io.y[i] = r[c]; break;
+        case kP2Pre: {
+          const T rr = B.b[i] - r[c];
+          B.x[i] = un[c] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * rr;
+          break;
         }
-        r[c] = v;
-      }
-      const bool cl = is_clamped(P.dir, a, b);
-      if (mode == kP2Diag) {
-        io.y[2 * n] = cl ? T(1) : r[0];
-        io.y[2 * n + 1] = cl ? T(1) : r[1];
-        continue;
-      }
-      T un[2];
-      operand(io, n, a, b, un);
-      if (cl) { r[0] = un[0]; r[1] = un[1]; }
-      const SmoothBufs<T>& B = io.B;
-      for (int c = 0; c < 2; ++c) {
-        const size_t i = 2 * n + c;
-        switch (mode) {
-          case kP2Apply: io.y[i] = r[c]; break;
-          case kP2Pre: {
-            const T rr = B.b[i] - r[c];
-            B.x[i] = un[c] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * rr;
-            break;
-          }
-          case kP2Res: B.r[i] = B.b[i] - r[c]; break;
-          case kP2First: {
-            const T r0 = B.b[i] - r[c];
-            const T d0 = T(B.cheb[0]) * B.dinv[i] * r0;
-            B.r[i] = r0;
-            B.d[i] = d0;
-            B.x2[i] = un[c] + d0;
-            break;
-          }
-          default: {  // kP2Post2
-            const T r1 = B.r[i] - r[c];
-            B.x[i] = B.x2[i] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * r1;
-          }
+        case kP2Res: B.r[i] = B.b[i] - r[c]; break;
+        case kP2First: {
+          const T r0 = B.b[i] - r[c];
+          const T d0 = T(B.cheb[0]) * B.dinv[i] * r0;
+          B.r[i] = r0;
+          B.d[i] = d0;
+          B.x2[i] = un[c] + d0;
+          break;
+        }
+        default: {  // kP2Post2
+          const T r1 = B.r[i] - r[c];
+          B.x[i] = B.x2[i] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * r1;
         }
       }
     }
+  }
+
+  // finish the lane's nodes of rows 0 .. nrows-1 (nrows = 3 on the last cell row)
+  TOPO_HD static void finish(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, int nrows) {
+    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = 0; r < 3; ++r) {
+      if (r >= nrows || 2 * j + r >= NY) continue;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+      for (int c = 0; c < 2; ++c)
+        if (2 * L.i + c < NX) finish_node(P, io, 2 * L.i + c, 2 * j + r, L.A[r][c], L.U[r][c]);
+    }
+  }
+
+  // row 2 becomes row 0 of the next step
+  TOPO_HD static void advance(P2Lane<T>& L) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 2; ++d) {
+        L.U[0][c][d] = L.U[2][c][d];
+        L.A[0][c][d] = c < 2 ? L.A[2][c][d] : T(0);  // column 2 went to the next lane
+        L.A[1][c][d] = T(0);
+        L.A[2][c][d] = T(0);
+      }
+    L.X[0][0] = L.X[1][0];
+    L.X[0][1] = L.X[1][1];
+  }
+
+  TOPO_HD static void begin(P2Lane<T>& L, int i, bool edge) {
+    L.i = i;
+    L.edge = edge;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 2; ++d) L.U[r][c][d] = L.A[r][c][d] = T(0);
+    L.X[0][0] = L.X[0][1] = L.X[1][0] = L.X[1][1] = T(0);
   }
 };
+
+// Cell rows per warp segment: enough segments to fill every SM with the 20
+// warps its registers allow, at least 4 rows so that the recomputed row below
+// a segment stays a bounded share.
+inline int p2_march_segment(int nx, int ny, int sms) {
+  const long nxw = (nx + 1 + P2M_OWN - 1) / P2M_OWN;
+  const long want = long(sms) * 20;
+  long seg = (long(ny) * nxw + want - 1) / want;
+  if (seg < 4) seg = 4;
+  if (seg > ny) seg = ny;
+  return int(seg < 1 ? 1 : seg);
+}
 
 // ---------------------------------------------------------------------------
 // per-triangle kernels (no tiling)
