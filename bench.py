@@ -382,7 +382,7 @@ def main():
         "compliance_rel_diff_mixed_vs_fp64": comp_rel,
         "e2e": {"value": e2e_value * world, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                 "d2h_bytes_per_step": 2 * nbytes + 8},
-        "roofline": {"bound": "hbm", "kernel": "k_p2_tile<float> (FP32 matrix-free P2 operator)",
+        "roofline": {"bound": "hbm", "kernel": "k_p2_march<float, Apply> (FP32 matrix-free P2 operator)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
                      "launch_ms": op},

@@ -195,6 +195,8 @@ struct topo_ctx {
   // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
+  float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
+  float* rm_pc32 = nullptr;
   double* r64 = nullptr;
   double* y64 = nullptr;
   float* d32 = nullptr;
@@ -543,10 +545,17 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
   k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64);
   if (C->precision == TOPO_PREC_MIXED) {
-    // FP32 operators re-evaluate r(xi) per quadrature point: cheaper than reading
-    // 48 bytes of mass matrices per cell; the FP64 operator reads them instead
+    // optional (TOPO_RMASS32=1): the r-weighted mass matrices (12 values per
+    // cell, evaluated in FP64) read by the FP32 operator instead of seven r(xi)
+    // evaluations per triangle; the evaluation costs more per design iteration
+    // than the reads save, so the default evaluates on the fly
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
-    C->smg32.set_p2(C->p2params<float>(0), C->p2params<float>(1), C->xi32);
+    if (C->rm_op32) {
+      k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op32);
+      k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc32);
+      C->launches += 2;
+    }
+    C->smg32.set_p2(C->p2params<float>(0, C->rm_op32), C->p2params<float>(1, C->rm_pc32), C->xi32);
     st = C->smg32.setup(s);
   } else {
     k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc64);
@@ -630,6 +639,10 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       const size_t ncell = size_t(C->nx) * C->ny;
       C->rm_op64 = C->arena.alloc_n<double>(12 * ncell);
       if (precision == TOPO_PREC_FP64) C->rm_pc64 = C->arena.alloc_n<double>(12 * ncell);
+      if (precision == TOPO_PREC_MIXED && env_flag("TOPO_RMASS32", false)) {
+        C->rm_op32 = C->arena.alloc_n<float>(12 * ncell);
+        C->rm_pc32 = C->arena.alloc_n<float>(12 * ncell);
+      }
       C->r64 = C->arena.alloc_n<double>(n);
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
@@ -922,7 +935,7 @@ int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream) {
       float* x = ctx->smg32.scratch0(7);
       float* y = ctx->smg32.scratch0(8);
       cudaEventRecord(e0, s);
-      p2_apply_f32(ctx->p2params<float>(0), ctx->xi32, x, y, s);
+      p2_apply_f32(ctx->p2params<float>(0, ctx->rm_op32), ctx->xi32, x, y, s);
       cudaEventRecord(e1, s);
     } else {
       cudaEventRecord(e0, s);
