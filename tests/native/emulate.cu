@@ -50,6 +50,7 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   const bool operand = io.mode != kP2Diag;
   std::vector<P2Lane<T>> L(32);
+  T acc[2] = {T(0), T(0)};
   auto down = [&](int r0) {
     for (int l = 0; l < 32; ++l) {
       const int src = l < 31 ? l + 1 : l;  // a shuffle from beyond the warp returns the own value
@@ -77,7 +78,7 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
         up();
         if (j >= js)
           for (int l = 1; l < 32; ++l)
-            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2);
+            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, acc);
         if (++j >= je) break;
         for (int l = 0; l < 32; ++l) {
           P2March<T>::advance(L[l]);
@@ -218,6 +219,7 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
     io.mode = mode;
     io.u = bufs[2];
     io.B = B;
+    io.xc = mode == kP2First ? xc : nullptr;  // optional fused prolongation
     p2_run_io<double>(P, xi, io);
     return 0;
   }

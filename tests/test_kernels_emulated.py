@@ -275,3 +275,11 @@ def test_fused_smoothing_steps_match_composition(level):
     r1 = r0 - A(dd0)
     ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
+    if p2:
+        # FIRST with the coarse correction prolonged on the fly (x itself not updated)
+        bufs2 = dict(b=b.copy(), dinv=dinv.copy(), x=x.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
+        emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs2, cheb,
+                   NXc=c["NX"], NYc=c["NY"], dirc=c["dir"], xc=xc)
+        assert np.max(np.abs(bufs2["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
+        assert np.max(np.abs(bufs2["x2"] - (u + dd0))) <= 1e-12 * np.max(np.abs(u))
+        assert np.array_equal(bufs2["x"], x)

@@ -195,6 +195,8 @@ struct topo_ctx {
   // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
+  double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
+  double* fst64_mass = nullptr;
   float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
   float* rm_pc32 = nullptr;
   double* r64 = nullptr;
@@ -332,6 +334,8 @@ int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
   return TOPO_OK;
 }
 
+int filter_stencils64(topo_ctx* C);
+
 int init_filter(topo_ctx* C, double eps) {
   C->eps = eps;
   const Dir nd = no_dir(C->nx + 1, C->ny + 1);
@@ -378,15 +382,32 @@ int init_filter(topo_ctx* C, double eps) {
     st = C->fmg64.setup(s);
   }
   if (st) return C->fail(st == -5 ? TOPO_ERR_CUDA : TOPO_ERR_NOT_CONVERGED, "filter multigrid set-up failed (%d)", st);
+  if (int rc = filter_stencils64(C)) return rc;
   return C->cuda_check("filter set-up");
 }
 
 // FP64 filter operator y = (eps^2 K1 + M1) x  (or M1 x when stiff == 0)
+// The filter's FP64 operators (eps^2 K + M, and M for the right-hand side) do
+// not depend on the design: their 7-point stencils are assembled once.
 void filter_apply64(topo_ctx* C, const double* x, double* y, bool stiff, cudaStream_t s) {
-  auto P = make_p1<double, 1>(C->fspec[0], C->frefs[0], nullptr, nullptr);
-  P.kK_c = stiff ? C->eps * C->eps : 0.0;
-  P.kM_c = 1.0;
-  k_p1_apply<double, 1><<<row_grid(C->nx + 1, C->ny + 1), kRowThreads, 0, s>>>(P, x, y);
+  const LevelSpec& F = C->fspec[0];
+  const P1Stencil<double, 1> S{F.nx, F.ny, F.dir, stiff ? C->fst64_stiff : C->fst64_mass};
+  k_p1_apply<double, 1><<<row_grid(C->nx + 1, C->ny + 1), kRowThreads, 0, s>>>(S, x, y);
+}
+
+int filter_stencils64(topo_ctx* C) {
+  const LevelSpec& F = C->fspec[0];
+  const size_t len = F.nn() * StencilLayout<1>::stride;
+  C->fst64_stiff = C->arena.alloc_n<double>(len);
+  C->fst64_mass = C->arena.alloc_n<double>(len);
+  if (!C->fst64_stiff || !C->fst64_mass) return C->fail(TOPO_ERR_CUDA, "out of device memory");
+  for (int stiff = 0; stiff < 2; ++stiff) {
+    auto P = make_p1<double, 1>(F, C->frefs[0], nullptr, nullptr);
+    P.kK_c = stiff ? C->eps * C->eps : 0.0;
+    P.kM_c = 1.0;
+    k_p1_stencil<double, 1><<<row_grid(F.NX, F.NY), kRowThreads>>>(P, stiff ? C->fst64_stiff : C->fst64_mass);
+  }
+  return C->cuda_check("filter stencils");
 }
 
 // FP32 multigrid Krylov solves inside an FP64 flexible GMRES (right

@@ -161,7 +161,7 @@ class MG {
     T* dinv = nullptr;
     T* kK = nullptr;
     T* kM = nullptr;
-    T* st = nullptr;  // assembled stencil (levels with at most kStencilMaxNodes nodes)
+    T* st = nullptr;  // assembled stencil (levels up to stencil_max_nodes(NC) nodes)
     double lmax = 1.0;
     bool bound = false;  // lmax is a guaranteed upper bound (no safety factor)
   };
@@ -186,7 +186,8 @@ class MG {
   const T* xi_ = nullptr;
   T* cinv_ = nullptr;  // dense coarsest inverse
   int* cstat_ = nullptr;
-  double* cheb_ = nullptr;  // Chebyshev coefficients, 8 per level (device)
+  T* cheb_ = nullptr;  // Chebyshev coefficients, 8 per level (device, level precision)
+  std::vector<T> cheb_host_;
   PcgDev* dev_ = nullptr;   // device scalars of the graph solve
   PcgDev* hdev_ = nullptr;  // pinned mirror
   cudaStream_t cap_[2] = {nullptr, nullptr};  // owned streams: graph recording only
@@ -201,6 +202,12 @@ class MG {
   void* tail_desc_ = nullptr;  // TailDesc<T, NC> (device)
   size_t tail_smem_ = 0;
   long long* tail_trace_ = nullptr;
+  // set by pcg_body around its V-cycle: the level-0 post-smoothing launch also
+  // reduces r.r, r.z and runs the iteration's test
+  bool stencils_ready_ = false;  // set once setup() has assembled the stencils
+  bool fuse_rz_ = false;
+  unsigned long long fuse_cond_ = 0;
+  int fuse_use_cond_ = 0;
 
   T* pcg_[kScratch] = {};
   Reducer* red_ = nullptr;

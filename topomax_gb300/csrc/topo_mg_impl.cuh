@@ -21,10 +21,14 @@ namespace topo {
 // ---------------------------------------------------------------------------
 // Lattice kernels use a 2D grid: blockIdx.y is the row, x covers the columns.
 constexpr int kRowThreads = 128;
-// P1 levels with at most this many nodes keep an assembled stencil (it fits
-// in L2 beside the vectors; larger levels are bandwidth-bound and evaluate
-// their element matrices on the fly)
-constexpr size_t kStencilMaxNodes = size_t(1) << 18;
+// P1 levels keep an assembled stencil up to a node count: elasticity levels
+// up to 2^18 nodes (a larger one streams 112 B per node per pass, more than
+// evaluating its element matrices on the fly costs), filter levels always
+// (32 B per node).  TOPO_STENCIL_NODES overrides both limits.
+inline size_t stencil_max_nodes(int NC) {
+  if (const char* e = std::getenv("TOPO_STENCIL_NODES")) return size_t(std::strtoull(e, nullptr, 10));
+  return NC == 2 ? (size_t(1) << 18) : (size_t(1) << 40);
+}
 #define kRowThreads_ 128
 inline dim3 row_grid(int NX, int NY) { return dim3((NX + kRowThreads - 1) / kRowThreads, NY); }
 
@@ -67,6 +71,23 @@ __device__ __forceinline__ void p2m_exchange_up(P2Lane<T>& L, int lane) {
     }
 }
 
+// End of one CG iteration: convergence / cap / breakdown test and beta (run by
+// one thread: the reduction's last block, or k_pcg_check).
+__device__ inline void pcg_check_dev(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
+  dv->it += 1;
+  const double pq = dv->pq, rr = dv->rr, rzn = dv->rz_new;
+  dv->relres = sqrt(rr / dv->bb);
+  int st = 1;
+  if (!isfinite(pq) || !isfinite(rr) || !isfinite(rzn)) st = 4;
+  else if (!(pq > 0.0) || !(dv->rz > 0.0)) st = 3;
+  else if (rr <= dv->tol2) st = 0;
+  else if (dv->it >= dv->maxit) st = 2;
+  dv->beta = (st == 1) ? rzn / dv->rz : 0.0;
+  dv->rz = rzn;
+  dv->status = st;
+  if (use_cond) cudaGraphSetConditional(h, st == 1 ? 1u : 0u);
+}
+
 template <class T, int MODE>
 __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
@@ -74,22 +95,38 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
   constexpr bool OPERAND = MODE != kP2Diag;
   const int lane = threadIdx.x & 31;
   const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
-  if (js >= P.ny) return;  // whole warp
-  const int je = min(js + seg, P.ny);
-  P2Lane<T> L;
-  P2March<T>::begin(L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
-  const bool owner = lane > 0 && L.i <= P.nx;
-  int j = js > 0 ? js - 1 : 0;
-  P2March<T>::template load<0>(P, io, xi, L, j);
-  p2m_exchange_down<T, 0, OPERAND>(L);
-  for (;;) {
-    P2March<T>::compute(P, L, j, MODE);
-    p2m_exchange_up<T>(L, lane);
-    if (owner && j >= js) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2);
-    if (++j >= je) break;
-    P2March<T>::advance(L);
-    P2March<T>::template load<1>(P, io, xi, L, j);
-    p2m_exchange_down<T, 1, OPERAND>(L);
+  T acc[2] = {T(0), T(0)};  // fused CG reductions (P2Io::fuse)
+  if (js < P.ny) {  // whole warp: warps past the last segment only join the reduction
+    const int je = min(js + seg, P.ny);
+    P2Lane<T> L;
+    P2March<T>::begin(L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
+    const bool owner = lane > 0 && L.i <= P.nx;
+    int j = js > 0 ? js - 1 : 0;
+    P2March<T>::template load<0>(P, io, xi, L, j);
+    p2m_exchange_down<T, 0, OPERAND>(L);
+    for (;;) {
+      P2March<T>::compute(P, L, j, MODE);
+      p2m_exchange_up<T>(L, lane);
+      if (owner && j >= js) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2, acc);
+      if (++j >= je) break;
+      P2March<T>::advance(L);
+      P2March<T>::template load<1>(P, io, xi, L, j);
+      p2m_exchange_down<T, 1, OPERAND>(L);
+    }
+  }
+  if constexpr (MODE == kP2Apply || MODE == kP2Post2) {
+    if (io.fuse != kFuseNone) {
+      double tot[2];
+      if (finish_reduction<2>(acc, io.partials, io.counter, tot)) {
+        if (io.fuse == kFusePQ) {
+          io.pcg->pq = tot[0];
+        } else {
+          io.pcg->rr = tot[0];
+          io.pcg->rz_new = tot[1];
+          pcg_check_dev(io.pcg, cudaGraphConditionalHandle(io.cond), io.use_cond);
+        }
+      }
+    }
   }
 }
 
@@ -109,10 +146,10 @@ __global__ void __launch_bounds__(kRowThreads_) k_prolong_add(Transfer X, const 
   if (a < X.NXf) TransferKern<T, NC>::node_prolong_add(a, b, X, xc, xf);
 }
 
-template <class T, int NC>
-__global__ void __launch_bounds__(kRowThreads) k_p1_apply(P1Params<T, NC> P, const T* __restrict__ u, T* __restrict__ y) {
+template <class T, int NC, class PP>
+__global__ void __launch_bounds__(kRowThreads) k_p1_apply(PP P, const T* __restrict__ u, T* __restrict__ y) {
   const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
-  if (a <= P.nx) P1Kern<T, NC>::node_apply(a, b, P, u, y);
+  if (a <= P.nx) p1_node_apply<T, NC>(a, b, P, u, y);
 }
 
 template <class T, int NC>
@@ -239,7 +276,7 @@ struct TailLevel {
   P1Stencil<T, NC> S;
   Transfer X;  // to the next coarser level
   const T* dinv;
-  const double* cheb;
+  const T* cheb;
   int NX, nn, off;  // off: first of this level's five shared vectors x, b, r, d, x2 (NC*nn each)
   int soff, doff;   // shared copies of the stencil (stride*nn) and of dinv (NC*nn)
 };
@@ -379,11 +416,16 @@ inline int device_sms() {
   return cached[dev];
 }
 
+inline dim3 p2_march_grid(int nx, int ny, int& seg) {
+  seg = p2_march_segment(nx, ny, device_sms());
+  const int nseg = (ny + seg - 1) / seg;
+  return dim3((nx + 1 + P2M_OWN - 1) / P2M_OWN, (nseg + P2M_WARPS - 1) / P2M_WARPS);
+}
+
 template <class T>
 inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
-  const int seg = p2_march_segment(P.nx, P.ny, device_sms());
-  const int nseg = (P.ny + seg - 1) / seg;
-  const dim3 g((P.nx + 1 + P2M_OWN - 1) / P2M_OWN, (nseg + P2M_WARPS - 1) / P2M_WARPS);
+  int seg = 0;
+  const dim3 g = p2_march_grid(P.nx, P.ny, seg);
   switch (io.mode) {
     case kP2Apply: k_p2_march<T, kP2Apply><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
     case kP2Diag: k_p2_march<T, kP2Diag><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
@@ -439,12 +481,20 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 // graph-resident CG scalars
 // ---------------------------------------------------------------------------
 // x += alpha p ; r -= alpha q with alpha = rz / pq read from device memory
+// (evaluated once per block: an FP64 division per thread is not free here)
 template <class T>
 __global__ void k_pcg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
                          const PcgDev* __restrict__ dv, size_t n) {
-  const double pq = dv->pq;
-  if (!(pq > 0.0) || !isfinite(pq)) return;
-  const T alpha = T(dv->rz / pq);
+  __shared__ T alpha_s;
+  __shared__ bool ok_s;
+  if (threadIdx.x == 0) {
+    const double pq = dv->pq;
+    ok_s = (pq > 0.0) && isfinite(pq);
+    alpha_s = ok_s ? T(dv->rz / pq) : T(0);
+  }
+  __syncthreads();
+  if (!ok_s) return;
+  const T alpha = alpha_s;
   TOPO_GRID_STRIDE(i, n) {
     x[i] += alpha * p[i];
     r[i] -= alpha * q[i];
@@ -454,7 +504,10 @@ __global__ void k_pcg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restri
 // p = z + beta p
 template <class T>
 __global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, const PcgDev* __restrict__ dv, size_t n) {
-  const T beta = T(dv->beta);
+  __shared__ T beta_s;
+  if (threadIdx.x == 0) beta_s = T(dv->beta);
+  __syncthreads();
+  const T beta = beta_s;
   TOPO_GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
 }
 
@@ -475,18 +528,7 @@ static __global__ void k_pcg_start(PcgDev* dv, cudaGraphConditionalHandle h, int
 
 // end of one iteration: convergence / cap / breakdown test and beta
 static __global__ void k_pcg_check(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
-  dv->it += 1;
-  const double pq = dv->pq, rr = dv->rr, rzn = dv->rz_new;
-  dv->relres = sqrt(rr / dv->bb);
-  int st = 1;
-  if (!isfinite(pq) || !isfinite(rr) || !isfinite(rzn)) st = 4;
-  else if (!(pq > 0.0) || !(dv->rz > 0.0)) st = 3;
-  else if (rr <= dv->tol2) st = 0;
-  else if (dv->it >= dv->maxit) st = 2;
-  dv->beta = (st == 1) ? rzn / dv->rz : 0.0;
-  dv->rz = rzn;
-  dv->status = st;
-  if (use_cond) cudaGraphSetConditional(h, st == 1 ? 1u : 0u);
+  pcg_check_dev(dv, h, use_cond);
 }
 
 // ---------------------------------------------------------------------------
@@ -527,7 +569,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
     if (!specs[l].p2) {
       v.kK = arena.alloc_n<T>(specs[l].ntri());
       if (specs[l].NC == 1) v.kM = arena.alloc_n<T>(specs[l].ntri());
-      if (specs[l].nn() <= kStencilMaxNodes)
+      if (specs[l].nn() <= stencil_max_nodes(specs[l].NC))
         v.st = arena.alloc_n<T>(specs[l].nn() * (specs[l].NC == 2 ? StencilLayout<2>::stride : StencilLayout<1>::stride));
     }
   }
@@ -536,7 +578,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   const int nc = int(specs.back().ndof());
   cinv_ = arena.alloc_n<T>(size_t(nc) * nc);
   cstat_ = arena.alloc_n<int>(1);
-  cheb_ = arena.alloc_n<double>(8 * specs.size());
+  cheb_ = arena.alloc_n<T>(8 * specs.size());
   dev_ = arena.alloc_n<PcgDev>(1);
   if (!hdev_) cudaMallocHost(&hdev_, sizeof(PcgDev));
   for (auto& c : cap_)
@@ -622,12 +664,17 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
     return;
   }
   const dim3 g = row_grid(L.NX, L.NY);
+  const Lev& v = lv_[l];
   if (L.NC == 2) {
-    auto P = make_p1<T, 2>(L, refs_[l], lv_[l].kK, nullptr);
-    k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(P, x, y);
+    if (v.st && stencils_ready_)
+      k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st}, x, y);
+    else
+      k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(make_p1<T, 2>(L, refs_[l], v.kK, nullptr), x, y);
   } else {
-    auto P = make_p1<T, 1>(L, refs_[l], lv_[l].kK, lv_[l].kM);
-    k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(P, x, y);
+    if (v.st && stencils_ready_)
+      k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st}, x, y);
+    else
+      k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(make_p1<T, 1>(L, refs_[l], v.kK, v.kM), x, y);
   }
 }
 
@@ -710,6 +757,7 @@ int MG<T>::setup(cudaStream_t s) {
       }
     }
   }
+  stencils_ready_ = true;
   for (int l = 0; l < L; ++l) {
     const size_t n = specs_[l].ndof();
     const int g = vec_grid(n, sms_);
@@ -740,7 +788,10 @@ int MG<T>::setup(cudaStream_t s) {
       rho_old = rho_new;
     }
   }
-  cudaMemcpyAsync(cheb_, cc.data(), cc.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+  // stored in the levels' precision: the kernels use them without conversion
+  // (an FP64 load and convert per node costs FP64-pipe time on this GPU)
+  cheb_host_.assign(cc.begin(), cc.end());
+  cudaMemcpyAsync(cheb_, cheb_host_.data(), cheb_host_.size() * sizeof(T), cudaMemcpyHostToDevice, s);
   const LevelSpec& C = specs_[L - 1];
   if (C.NC == 2)
     k_coarse_inverse<T, 2><<<1, 256, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
@@ -836,12 +887,20 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     k_restrict<T, 2><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    k_prolong_add<T, 2><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
-    io.mode = kP2First;
+    io.mode = kP2First;  // adds the prolonged coarse correction to its operand on the fly
+    io.xc = c.x;
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Post2;
+    if (l == 0 && fuse_rz_) {  // the CG's r.r, r.z and test (see pcg_body)
+      io.fuse = kFuseRZ;
+      io.partials = red_->partials;
+      io.counter = red_->counter;
+      io.pcg = dev_;
+      io.cond = fuse_cond_;
+      io.use_cond = fuse_use_cond_;
+    }
     launch_p2_tile<T>(p2_, xi_, io, s);
-    launches += 3;
+    launches += 2;
     return;
   }
   // the level's operator: assembled stencil when there is one, else on the fly
@@ -906,6 +965,31 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   const size_t n = specs_[0].ndof();
   const int g = vec_grid(n, sms_);
   T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  int seg = 0;
+  const dim3 mg = p2_march_grid(specs_[0].nx, specs_[0].ny, seg);
+  if (specs_[0].p2 && size_t(mg.x) * mg.y * 2 <= size_t(red_->blocks) * 16) {
+    // P2 level 0: p.q is reduced inside the operator launch, r.r / r.z and the
+    // iteration's test inside the V-cycle's last post-smoothing launch
+    P2Io<T> io;
+    std::memset(&io, 0, sizeof(io));
+    io.mode = kP2Apply;
+    io.u = p;
+    io.y = q;
+    io.fuse = kFusePQ;
+    io.partials = red_->partials;
+    io.counter = red_->counter;
+    io.pcg = dev_;
+    launch_p2_tile<T>(p2_op_, xi_, io, s);
+    k_pcg_xr<T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
+    fuse_rz_ = true;
+    fuse_cond_ = (unsigned long long)h;
+    fuse_use_cond_ = use_cond;
+    vcycle(r, z, s);
+    fuse_rz_ = false;
+    k_pcg_p<T><<<g, kVecThreads, 0, s>>>(p, z, dev_, n);
+    launches += 3;
+    return;
+  }
   apply(0, p, q, s, true);
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(p, q, n, red_->partials, red_->counter, &dev_->pq);
   k_pcg_xr<T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);

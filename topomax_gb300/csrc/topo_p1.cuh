@@ -231,7 +231,8 @@ namespace topo {
 // six incidences' element matrices, coefficients and clamping tests (the
 // smallest levels are bound by that chain's latency, not by bandwidth).
 // Columns of clamped nodes are zero; a clamped node's own row is the
-// identity (its evaluation reports "clamped" as P1Kern does).
+// identity (its evaluation reports "clamped" as P1Kern does).  Block 0 is
+// stored as the row sum (difference form, see p1_stencil_node).
 template <int NC>
 struct StencilLayout {
   static constexpr int stride = NC == 2 ? 28 : 8;  // values per node: 7 blocks, padded to 16 bytes
@@ -249,19 +250,27 @@ template <class T, int NC>
 struct P1Stencil {
   int nx, ny;  // cells of this level
   Dir dir;
-  const T* s;  // node n, block k, row c, column d at s[n*stride + k*NC*NC + c*NC + d]
+  const T* s;  // node n, block k, row c, column d at s[n*stride + k*NC*NC + c*NC + d]; block 0: row sum
 };
 
 // Stencil row of node (a,b) assembled from the level's coefficients (the
-// same incidences and clamping rules as P1Kern::node_eval).
+// same incidences and clamping rules as P1Kern::node_eval), in difference
+// form: block 0 holds the row sum S_0 = sum_k A_(n,k) (accumulated in FP64),
+// blocks 1..6 the neighbour couplings, and
+//     (A u)_n = S_0 u_n + sum_(k>=1) A_(n,k) (u_k - u_n).
+// The row sum of an elasticity or filter row is small against its entries
+// (zero for rigid translations, the mass for the filter), so summing rounded
+// entries at run time would lose the smooth modes' accuracy in FP32.
 template <class T, int NC>
 TOPO_HD void p1_stencil_node(int a, int b, const P1Params<T, NC>& P, T* out) {
   constexpr int SB = NC * NC;
   T blk[7 * SB];
+  double rs[SB];
   for (int i = 0; i < 7 * SB; ++i) blk[i] = T(0);
+  for (int i = 0; i < SB; ++i) rs[i] = 0.0;
   for (int i = 7 * SB; i < StencilLayout<NC>::stride; ++i) out[i] = T(0);
   if (is_clamped(P.dir, a, b)) {
-    for (int c = 0; c < NC; ++c) blk[c * NC + c] = T(1);
+    for (int c = 0; c < NC; ++c) rs[c * NC + c] = 1.0;
   } else {
     const bool chk = P1Kern<T, NC>::near_clamped(P.dir, a, b);
     for (int e = 0; e < 6; ++e) {
@@ -270,20 +279,23 @@ TOPO_HD void p1_stencil_node(int a, int b, const P1Params<T, NC>& P, T* out) {
       const int ci = a + dci, cj = b + dcj;
       if (ci < 0 || ci >= P.nx || cj < 0 || cj >= P.ny) continue;
       const size_t t = (size_t(cj) * P.nx + ci) * 2 + o;
-      const T kk = P.kK ? P.kK[t] : P.kK_c;
-      const T km = (NC == 1) ? (P.kM ? P.kM[t] : P.kM_c) : T(0);
+      const double kk = P.kK ? double(P.kK[t]) : double(P.kK_c);
+      const double km = (NC == 1) ? (P.kM ? double(P.kM[t]) : double(P.kM_c)) : 0.0;
       for (int L = 0; L < 3; ++L) {
         const int al = ci + p1_off_a(o, L), bl = cj + p1_off_b(o, L);
         if (chk && is_clamped(P.dir, al, bl)) continue;
         T* bk = blk + st_block(al - a, bl - b) * SB;
         for (int c = 0; c < NC; ++c)
           for (int d = 0; d < NC; ++d) {
-            bk[c * NC + d] += kk * P.K[o][loc * NC + c][L * NC + d];
-            if (NC == 1) bk[0] += km * P.Mm[o][loc][L];
+            double v = kk * double(P.K[o][loc * NC + c][L * NC + d]);
+            if (NC == 1) v += km * double(P.Mm[o][loc][L]);
+            bk[c * NC + d] += T(v);
+            rs[c * NC + d] += v;
           }
       }
     }
   }
+  for (int i = 0; i < SB; ++i) blk[i] = T(rs[i]);
   for (int i = 0; i < 7 * SB; ++i) out[i] = blk[i];
 }
 
@@ -294,17 +306,22 @@ struct P1StencilKern {
     for (int c = 0; c < NC; ++c) acc[c] = T(0);
     if (!surely_free(P.dir, a, b) && is_clamped(P.dir, a, b)) return false;
     const int NX = P.nx + 1, NY = P.ny + 1;
-    const T* sn = P.s + (size_t(b) * NX + a) * StencilLayout<NC>::stride;
+    const size_t n = size_t(b) * NX + a;
+    const T* sn = P.s + n * StencilLayout<NC>::stride;
+    T un[NC];
+    fetch(n, a, b, un);
+    for (int c = 0; c < NC; ++c)
+      for (int d = 0; d < NC; ++d) acc[c] += sn[c * NC + d] * un[d];
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 1; k < 7; ++k) {
       const int al = a + st_da(k), bl = b + st_db(k);
       if (al < 0 || al >= NX || bl < 0 || bl >= NY) continue;
       T ul[NC];
       fetch(size_t(bl) * NX + al, al, bl, ul);
       for (int c = 0; c < NC; ++c)
-        for (int d = 0; d < NC; ++d) acc[c] += sn[k * NC * NC + c * NC + d] * ul[d];
+        for (int d = 0; d < NC; ++d) acc[c] += sn[k * NC * NC + c * NC + d] * (ul[d] - un[d]);
     }
     return true;
   }
@@ -320,6 +337,16 @@ TOPO_HD bool p1_node_eval(int a, int b, const P1Stencil<T, NC>& P, const F& f, T
   return P1StencilKern<T, NC>::node_eval(a, b, P, f, acc);
 }
 
+// y = A u at node (a,b) (clamped rows: identity)
+template <class T, int NC, class PP>
+TOPO_HD void p1_node_apply(int a, int b, const PP& P, const T* u, T* y) {
+  const size_t n = size_t(b) * (P.nx + 1) + a;
+  T acc[NC];
+  if (!p1_node_eval<T, NC>(a, b, P, FetchArray<T, NC>{u}, acc))
+    for (int c = 0; c < NC; ++c) acc[c] = u[NC * n + c];
+  for (int c = 0; c < NC; ++c) y[NC * n + c] = acc[c];
+}
+
 // ---------------------------------------------------------------------------
 // fused degree-2 Chebyshev smoothing steps of one P1 level (node-centric)
 // ---------------------------------------------------------------------------
@@ -332,7 +359,7 @@ struct SmoothBufs {
   T* x2;           // intermediate solution of post-smoothing
   T* r;            // residual
   T* d;            // Chebyshev direction
-  const double* cheb;  // c0 = 1/theta, c1, c2 of the second step
+  const T* cheb;   // c0 = 1/theta, c1, c2 of the second step (in the level's precision)
 };
 
 // PRE input: first step from x = 0, d0 = c0 Dinv b, computed per node
@@ -353,7 +380,7 @@ struct P1Smooth {
   TOPO_HD static void pre(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
-    const T c0 = T(B.cheb[0]), c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
+    const T c0 = B.cheb[0], c1 = B.cheb[1], c2 = B.cheb[2];
     const FetchPre<T, NC> f{B.b, B.dinv, c0};
     T t[NC], u[NC];
     f(n, a, b, u);
@@ -381,7 +408,7 @@ struct P1Smooth {
   TOPO_HD static void first(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
-    const T c0 = T(B.cheb[0]);
+    const T c0 = B.cheb[0];
     T t[NC];
     if (!p1_node_eval<T, NC>(a, b, P, FetchArray<T, NC>{B.x}, t))
       for (int c = 0; c < NC; ++c) t[c] = B.x[NC * n + c];
@@ -399,7 +426,7 @@ struct P1Smooth {
   TOPO_HD static void post2(int a, int b, const PP& P, const SmoothBufs<T>& B) {
     const int NX = P.nx + 1;
     const size_t n = size_t(b) * NX + a;
-    const T c1 = T(B.cheb[1]), c2 = T(B.cheb[2]);
+    const T c1 = B.cheb[1], c2 = B.cheb[2];
     const FetchArray<T, NC> f{B.d};
     T t[NC];
     if (!p1_node_eval<T, NC>(a, b, P, f, t))

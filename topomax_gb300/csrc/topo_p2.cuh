@@ -205,12 +205,30 @@ constexpr int P2M_THREADS = 32 * P2M_WARPS;
 // What one launch of the P2 kernel computes.
 enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2First = 4, kP2Post2 = 5 };
 
+struct PcgDev;
+
+// Reductions of the state CG fused into a P2 launch (P2Io::fuse):
+enum P2Fuse {
+  kFuseNone = 0,
+  kFusePQ = 1,    // apply q = A p: p.q -> PcgDev::pq
+  kFuseRZ = 2,    // last post-smoothing step of the V-cycle (z = B.x, r = B.b):
+                  // r.r, r.z -> PcgDev::rr, rz_new, then the iteration's test
+};
+
 template <class T>
 struct P2Io {
   int mode;
   const T* u;          // kP2Apply / kP2Res / kP2First input (x)
   T* y;                // kP2Apply / kP2Diag output
   SmoothBufs<T> B;     // smoothing modes (see P1Smooth for the formulas)
+  const T* xc;         // kP2First: coarse correction on the P1 vertex lattice, added to the
+                       // operand x at free nodes on the fly (the prolongation, not stored)
+  int fuse;            // P2Fuse
+  double* partials;    // per-block partial sums (2 per block)
+  unsigned* counter;   // last-block counter
+  PcgDev* pcg;         // CG scalars
+  unsigned long long cond;  // graph conditional handle of the CG loop
+  int use_cond;
 };
 
 template <class T>
@@ -228,7 +246,7 @@ struct P2March {
   TOPO_HD static void operand(const P2Io<T>& io, size_t n, T (&v)[2]) {
     switch (io.mode) {
       case kP2Pre: {
-        const T c0 = T(io.B.cheb[0]);
+        const T c0 = io.B.cheb[0];
         v[0] = c0 * io.B.dinv[2 * n] * io.B.b[2 * n];
         v[1] = c0 * io.B.dinv[2 * n + 1] * io.B.b[2 * n + 1];
         break;
@@ -243,12 +261,27 @@ struct P2March {
     }
   }
 
+  // P1 -> P2 prolongation of the coarse correction at node (a,b): the coarse
+  // hat functions are 1 at vertex (a/2, b/2) and 1/2 at the edge midpoints
+  TOPO_HD static void prolong(const P2Params<T>& P, const T* xc, int a, int b, T (&v)[2]) {
+    const int NXc = P.nx + 1;
+    const int pa = a & 1, pb = b & 1, I0 = a >> 1, J0 = b >> 1;
+    const size_t m0 = size_t(J0) * NXc + I0;
+    const size_t m1 = size_t(J0 + pb) * NXc + I0 + pa;
+    for (int c = 0; c < 2; ++c) {
+      const T x00 = xc[2 * m0 + c];
+      v[c] += (pa | pb) ? T(0.5) * (x00 + xc[2 * m1 + c]) : x00;
+    }
+  }
+
   // operand at node (a,b); zero outside the lattice and at clamped nodes
   TOPO_HD static void fetch(const P2Params<T>& P, const P2Io<T>& io, int a, int b, T (&v)[2]) {
     const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
     v[0] = v[1] = T(0);
-    if (a >= 0 && a < NX && b >= 0 && b < NY && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b)))
+    if (a >= 0 && a < NX && b >= 0 && b < NY && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b))) {
       operand(io, size_t(b) * NX + a, v);
+      if (io.mode == kP2First && io.xc) prolong(P, io.xc, a, b, v);
+    }
   }
 
   TOPO_HD static T density(const P2Params<T>& P, const T* xi, int i, int j) {
@@ -320,7 +353,7 @@ struct P2March {
 
   // finish node (a,b) with the complete sum r (clamped rows act as identity rows)
   TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, const T (&sum)[2],
-                                  const T (&u)[2]) {
+                                  const T (&u)[2], T (&acc)[2]) {
     const int NX = 2 * P.nx + 1;
     const size_t n = size_t(b) * NX + a;
     const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
@@ -339,16 +372,19 @@ struct P2March {
     for (int c = 0; c < 2; ++c) {
       const size_t i = 2 * n + c;
       switch (io.mode) {
-        case kP2Apply: io.y[i] = r[c]; break;
+        case kP2Apply:
+          io.y[i] = r[c];
+          if (io.fuse == kFusePQ) acc[0] += un[c] * r[c];
+          break;
         case kP2Pre: {
           const T rr = B.b[i] - r[c];
-          B.x[i] = un[c] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * rr;
+          B.x[i] = un[c] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * rr;
           break;
         }
         case kP2Res: B.r[i] = B.b[i] - r[c]; break;
         case kP2First: {
           const T r0 = B.b[i] - r[c];
-          const T d0 = T(B.cheb[0]) * B.dinv[i] * r0;
+          const T d0 = B.cheb[0] * B.dinv[i] * r0;
           B.r[i] = r0;
           B.d[i] = d0;
           B.x2[i] = un[c] + d0;
@@ -356,14 +392,23 @@ struct P2March {
         }
         default: {  // kP2Post2
           const T r1 = B.r[i] - r[c];
-          B.x[i] = B.x2[i] + T(B.cheb[1]) * un[c] + T(B.cheb[2]) * B.dinv[i] * r1;
+          const T z = B.x2[i] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
+          B.x[i] = z;
+          if (io.fuse == kFuseRZ) {
+            const T bi = B.b[i];
+            acc[0] += bi * bi;
+            acc[1] += bi * z;
+          }
         }
       }
     }
   }
 
   // finish the lane's nodes of rows 0 .. nrows-1 (nrows = 3 on the last cell row)
-  TOPO_HD static void finish(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, int nrows) {
+  // acc: the lane's partial sums of the fused reductions, in the operator's
+  // precision (a few dozen terms; blocks combine them in FP64)
+  TOPO_HD static void finish(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, int nrows,
+                             T (&acc)[2]) {
     const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
@@ -374,7 +419,7 @@ struct P2March {
 #pragma unroll
 #endif
       for (int c = 0; c < 2; ++c)
-        if (2 * L.i + c < NX) finish_node(P, io, 2 * L.i + c, 2 * j + r, L.A[r][c], L.U[r][c]);
+        if (2 * L.i + c < NX) finish_node(P, io, 2 * L.i + c, 2 * j + r, L.A[r][c], L.U[r][c], acc);
     }
   }
 

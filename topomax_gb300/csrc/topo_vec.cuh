@@ -101,45 +101,50 @@ __global__ void k_cheb_next(T* __restrict__ r, const T* __restrict__ t, const T*
 // reductions: per-block partial sums, the last block to finish adds the
 // partials in block order (deterministic) and stores the result.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum(double v) {
+template <class R>
+__device__ __forceinline__ R warp_sum(R v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
+template <class R>
+__device__ __forceinline__ R block_sum(R v, R* sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   v = warp_sum(v);
   if (lane == 0) sh[w] = v;
   __syncthreads();
   const int nw = (blockDim.x + 31) >> 5;
-  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : R(0);
   if (w == 0) v = warp_sum(v);
   __syncthreads();
   return v;  // valid in thread 0
 }
 
-// Finishes a reduction of NV values per block.  Returns true in thread 0 of
-// the last block, with the totals in tot[].
-template <int NV>
-__device__ bool finish_reduction(const double (&v)[NV], double* partials, unsigned* counter,
-                                 double (&tot)[NV]) {
+// Finishes a reduction of NV values per block (1D or 2D grids).  Returns true
+// in thread 0 of the last block, with the totals in tot[].  The in-block tree
+// runs in R (float for FP32 data: FP64 arithmetic is scarce on this GPU), the
+// per-block partials and their final combination in FP64.
+template <int NV, class R>
+__device__ bool finish_reduction(const R (&v)[NV], double* partials, unsigned* counter, double (&tot)[NV]) {
+  __shared__ R shr[32];
   __shared__ double sh[32];
   __shared__ bool last;
+  const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x, nb = gridDim.x * gridDim.y;
   for (int k = 0; k < NV; ++k) {
-    const double s = block_sum(v[k], sh);
-    if (threadIdx.x == 0) partials[size_t(blockIdx.x) * NV + k] = s;
+    const R s = block_sum(v[k], shr);
+    if (threadIdx.x == 0) partials[size_t(bid) * NV + k] = double(s);
   }
   __threadfence();
   if (threadIdx.x == 0) {
     const unsigned prev = atomicAdd(counter, 1u);
-    last = (prev == gridDim.x - 1);
+    last = (prev == nb - 1);
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
   for (int k = 0; k < NV; ++k) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    for (unsigned b = threadIdx.x; b < nb; b += blockDim.x)
       s += ((volatile double*)partials)[size_t(b) * NV + k];
     // fixed-order combine: strided per-thread sums then a tree
     s = block_sum(s, sh);
@@ -157,7 +162,7 @@ __global__ void k_dot(const TA* __restrict__ a, const TB* __restrict__ b, size_t
   using Acc = typename std::conditional<sizeof(TA) == 4 && sizeof(TB) == 4, float, double>::type;
   Acc acc = Acc(0);
   TOPO_GRID_STRIDE(i, n) acc += b ? Acc(a[i]) * Acc(b[i]) : Acc(a[i]) * Acc(a[i]);
-  double v[1] = {double(acc)};
+  const Acc v[1] = {acc};
   double tot[1];
   if (finish_reduction<1>(v, partials, counter, tot)) out[0] = tot[0];
 }
@@ -173,7 +178,7 @@ __global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T
     p0 += a[i] * b[i];
     p1 += c[i] * d[i];
   }
-  double v[2] = {double(p0), double(p1)};
+  const T v[2] = {p0, p1};
   double tot[2];
   if (finish_reduction<2>(v, partials, counter, tot)) {
     out[0] = tot[0];
