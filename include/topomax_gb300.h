@@ -184,6 +184,71 @@ int topo_sensitivity_rhs_noalloc(const topo_grid_desc* grid, double young_modulu
                                  double penalization, double penal_min, const double* u, const double* xi,
                                  double* b, topo_stream_t stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Deep-energy-method (DEM) strain energy on the structured quadrilateral mesh
+ * ---------------------------------------------------------------------------------------
+ * The energy functional of DEM_src/elasisity_problem.py:79-129 (StrainEnergy) evaluated with
+ * the 2x2 Gauss rule of DEM_src/objective_calculator.py:19-125 (ObjectiveCalculator), the
+ * Dirichlet mask of DEM_src/dirichlet_enforcer.py:14-56 (ElasticityEnforcer) and the external
+ * work of DEM_src/integrator.py:44-99 (boundary_integral, circular_integral), which is linear
+ * in u and is passed in as per-node weights (the host precomputes them from the traction
+ * intervals and the circle-cell areas of DEM_src/domains.py).
+ * Layouts (the reference's): u float32 [(nx+1)*(ny+1)][2] with node (ix, iy) at
+ * ix*(ny+1)+iy (DEM_src/utils.py:34-45 flatten order); density float32 [ny][nx] (cell (ix, iy)
+ * at iy*nx+ix).  All arrays are device pointers unless stated otherwise. */
+typedef struct topo_dem_ctx topo_dem_ctx;
+
+typedef struct {
+  int nx, ny;                /* cells in x and y (Mesh.Nx, Mesh.Ny) */
+  float dshape[4][4][2];     /* Jinv * dN_i at Gauss point g: [node i][point g][x or y], nodes in the
+                                order (ix,iy), (ix,iy+1), (ix+1,iy), (ix+1,iy+1) of
+                                ObjectiveCalculator.get_gauss_points; float32 as torch rounds them */
+  float detJ;                /* dx*dy/4 */
+  float lame_lambda;         /* StrainEnergy.lame_lda, float32 */
+  float two_mu;              /* 2 * StrainEnergy.lame_mu, float32 */
+} topo_dem_desc;
+
+/* Replaces StrainEnergy.__init__ / ObjectiveCalculator.__init__ (DEM_src/elasisity_problem.py:
+ * 63-77, DEM_src/objective_calculator.py:19-23). */
+topo_dem_ctx* topo_dem_create(const topo_dem_desc* desc, int* status);
+void topo_dem_destroy(topo_dem_ctx* ctx);
+const char* topo_dem_last_error(const topo_dem_ctx* ctx);
+
+/* ObjectiveCalculator.set_penalization (DEM_src/objective_calculator.py:25-26). */
+int topo_dem_set_penalization(topo_dem_ctx* ctx, double p);
+
+/* External work weights: host float32 [(nx+1)*(ny+1)][2]; the external energy is
+ * sum_n w[n][0]*u[n][0] + w[n][1]*u[n][1] (calculate_traction_integral +
+ * calculate_body_force_integral, DEM_src/elasisity_problem.py:31-60).  NULL clears them. */
+int topo_dem_set_external(topo_dem_ctx* ctx, const float* weights_host);
+
+/* Dirichlet mask: host float32 [(nx+1)*(ny+1)][2] (ElasticityEnforcer.zero_enforcer).  NULL
+ * clears it. */
+int topo_dem_set_mask(topo_dem_ctx* ctx, const float* mask_host);
+
+/* ElasticityEnforcer.__call__ (DEM_src/dirichlet_enforcer.py:55-56): u = u_hat * mask. */
+int topo_dem_enforce(topo_dem_ctx* ctx, const float* u_hat, float* u, topo_stream_t stream);
+
+/* StrainEnergy.calculate_energy (DEM_src/elasisity_problem.py:97-118):
+ * psi = 0.5 * sum_cells r(rho) SE detJ - external work, SE = sum over the 4 Gauss points of
+ * sigma:eps.  With masked != 0, u is the network output u_hat and the mask is applied on the
+ * fly (the enforcer fused into the energy).  energy: device double scalar. */
+int topo_dem_energy(topo_dem_ctx* ctx, const float* u, const float* density, int masked, double* energy,
+                    topo_stream_t stream);
+
+/* Gradient of topo_dem_energy times the device float scalar *scale: du float32 [nn][2]
+ * (d psi / d u, or d psi / d u_hat when masked) and/or ddensity float32 [ny][nx]
+ * (0.5 r'(rho) SE detJ); either may be NULL.  No counterpart in the reference (torch autograd
+ * of calculate_energy there). */
+int topo_dem_energy_backward(topo_dem_ctx* ctx, const float* u, const float* density, int masked,
+                             const float* scale, float* du, float* ddensity, topo_stream_t stream);
+
+/* StrainEnergy.calculate_objective_and_gradient (DEM_src/elasisity_problem.py:120-129):
+ * objective = sum r(rho) SE detJ (device double scalar), gradient = -r'(rho) SE detJ
+ * (device float32 [ny][nx]). */
+int topo_dem_objective_gradient(topo_dem_ctx* ctx, const float* u, const float* density, double* objective,
+                                float* gradient, topo_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,9 @@ EXPORTED = [
     "topo_compliance", "topo_sensitivity_rhs", "topo_sensitivity", "topo_emd_step",
     "topo_emd_finish", "topo_integrate", "topo_apply_state", "topo_load_vector", "topo_time_operator",
     "topo_launch_count", "topo_sensitivity_rhs_noalloc",
+    "topo_dem_create", "topo_dem_destroy", "topo_dem_last_error", "topo_dem_set_penalization",
+    "topo_dem_set_external", "topo_dem_set_mask", "topo_dem_enforce", "topo_dem_energy",
+    "topo_dem_energy_backward", "topo_dem_objective_gradient",
 ]
 
 
@@ -59,6 +62,11 @@ class LoadDesc(ctypes.Structure):
                 ("center_y", ctypes.c_double), ("radius", ctypes.c_double),
                 ("value_x", ctypes.c_double), ("value_y", ctypes.c_double),
                 ("n_tractions", ctypes.c_int), ("tractions", ctypes.POINTER(Traction))]
+
+
+class DemDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("dshape", ctypes.c_float * 32),
+                ("detJ", ctypes.c_float), ("lame_lambda", ctypes.c_float), ("two_mu", ctypes.c_float)]
 
 
 _lib = None
@@ -104,8 +112,23 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_time_operator.argtypes = [P, PD, P]
     lib.topo_launch_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.topo_sensitivity_rhs_noalloc.argtypes = [ctypes.POINTER(GridDesc), D, D, D, D, P, P, P, P]
+    lib.topo_dem_create.restype = P
+    lib.topo_dem_create.argtypes = [ctypes.POINTER(DemDesc), PI]
+    lib.topo_dem_destroy.restype = None
+    lib.topo_dem_destroy.argtypes = [P]
+    lib.topo_dem_last_error.restype = ctypes.c_char_p
+    lib.topo_dem_last_error.argtypes = [P]
+    lib.topo_dem_set_penalization.argtypes = [P, D]
+    lib.topo_dem_set_external.argtypes = [P, P]
+    lib.topo_dem_set_mask.argtypes = [P, P]
+    lib.topo_dem_enforce.argtypes = [P, P, P, P]
+    lib.topo_dem_energy.argtypes = [P, P, P, I, P, P]
+    lib.topo_dem_energy_backward.argtypes = [P, P, P, I, P, P, P, P]
+    lib.topo_dem_objective_gradient.argtypes = [P, P, P, P, P, P]
+    no_int = ("topo_create", "topo_create_filter", "topo_destroy", "topo_last_error", "topo_dem_create",
+              "topo_dem_destroy", "topo_dem_last_error")
     for name in EXPORTED:
-        if name not in ("topo_create", "topo_create_filter", "topo_destroy", "topo_last_error"):
+        if name not in no_int:
             getattr(lib, name).restype = I
     if path is None:
         _lib = lib
