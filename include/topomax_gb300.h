@@ -164,6 +164,13 @@ int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream);
  * (kernels executed inside CUDA graphs are counted per execution). */
 int topo_launch_count(const topo_ctx* ctx, int64_t* launches);
 
+/* y = M1 x with M1 the consistent CG1 mass matrix (the assembled (x, v) form, as the filter's
+ * right-hand side FEM_src/filter.py:30-37 assembles it), FP64.  No counterpart as a function in
+ * the reference: the Euclidean gradient of the compliance with respect to the nodal design is
+ * M1 g, g the CG1 Riesz representative topo_sensitivity returns
+ * (FEM_src/elasisity_problem.py:134-150). */
+int topo_mass_apply(topo_ctx* ctx, const double* x, double* y, topo_stream_t stream);
+
 /* Copy of the pre-assembled load vector (2*n_p2 entries, clamped dofs zero). */
 int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream);
 

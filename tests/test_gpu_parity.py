@@ -242,3 +242,18 @@ def test_tail_matches_level_kernels(precision, monkeypatch):
     assert results[0][0] == results[1][0], [r[0] for r in results]
     ref = results[1][1]
     assert np.max(np.abs(results[0][1] - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_contexts_of_different_sizes_interleave():
+    """Kernel attributes are process-wide: a context created later (here a smaller
+    mesh) must not break the launches of an earlier one."""
+    import torch
+    from topomax_gb300 import fem as F
+    d = _design()
+    big, Vb = _gpu_problem(d, 120, 60, rtol=1e-8)
+    small, Vs = _gpu_problem(d, 40, 20, rtol=1e-8)
+    for prob, V in ((big, Vb), (small, Vs), (big, Vb)):
+        prob.set_penalization(3.0)
+        xi = F.Function(V, torch.full((V.dim(),), 0.5, dtype=torch.float64, device="cuda"))
+        c = prob.calculate_objective(xi)
+        assert np.isfinite(c) and c > 0

@@ -610,6 +610,7 @@ extern "C" {
 
 topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, const topo_bc_desc* bc,
                       const topo_load_desc* load, int precision, int* status) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());  // set-up allocates and frees
   topo_ctx* C = nullptr;
   int rc = TOPO_OK;
   try {
@@ -703,6 +704,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
 }
 
 topo_ctx* topo_create_filter(const topo_grid_desc* grid, double epsilon, int precision, int* status) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());  // set-up allocates and frees
   topo_ctx* C = nullptr;
   int rc = TOPO_OK;
   try {
@@ -722,7 +724,10 @@ topo_ctx* topo_create_filter(const topo_grid_desc* grid, double epsilon, int pre
   return C;
 }
 
-void topo_destroy(topo_ctx* ctx) { delete ctx; }
+void topo_destroy(topo_ctx* ctx) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());
+  delete ctx;
+}
 
 const char* topo_last_error(const topo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
@@ -750,6 +755,15 @@ int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, i
     filter_apply64(ctx, f, ctx->fb64, false, s);
     ctx->launches += 1;
     return filter_solve_impl(ctx, ctx->fb64, xi, rtol, iters, s);
+  });
+}
+
+int topo_mass_apply(topo_ctx* ctx, const double* x, double* y, topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!x || !y) return ctx->fail(TOPO_ERR_ARG, "invalid mass-apply arguments");
+    filter_apply64(ctx, x, y, false, reinterpret_cast<cudaStream_t>(stream));
+    ctx->launches += 1;
+    return ctx->cuda_check("mass apply");
   });
 }
 

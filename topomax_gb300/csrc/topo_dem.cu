@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <string>
 
+#include "topo_mg.h"
 #include "topo_vec.cuh"
 #include "topomax_gb300.h"
 
@@ -50,6 +51,7 @@ struct topo_dem_ctx {
     return TOPO_OK;
   }
   ~topo_dem_ctx() {
+    std::lock_guard<std::recursive_mutex> lock(device_lock());
     cudaFree(wext);
     cudaFree(mask);
     cudaFree(partials);
@@ -288,6 +290,7 @@ int guarded(topo_dem_ctx* C, F&& f) {
 }
 
 int upload(topo_dem_ctx* C, float*& dst, const float* host) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());
   const size_t n = 2 * size_t(C->d.nx + 1) * (C->d.ny + 1);
   if (!host) {
     cudaFree(dst);
@@ -305,6 +308,7 @@ int upload(topo_dem_ctx* C, float*& dst, const float* host) {
 extern "C" {
 
 topo_dem_ctx* topo_dem_create(const topo_dem_desc* desc, int* status) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());
   auto set = [&](int s) {
     if (status) *status = s;
   };

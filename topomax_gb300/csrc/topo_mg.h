@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "topo_common.cuh"
@@ -38,6 +39,12 @@ class Arena {
   size_t bytes_ = 0;
   bool failed_ = false;
 };
+
+// Serialises, across the threads of a process, what must not overlap another
+// thread's CUDA-graph recording: device memory release (cudaFree synchronises
+// the whole device, which would invalidate a recording in progress), context
+// set-up and the recordings themselves.
+std::recursive_mutex& device_lock();
 
 struct LevelSpec {
   bool p2 = false;  // P2 elasticity level (only level 0 of the state hierarchy)
@@ -143,7 +150,8 @@ class MG {
   // record the CG loop as a CUDA graph with a device-side WHILE node (default);
   // false runs the same kernels from a host loop
   bool use_graphs = true;
-  bool use_tail = true;  // run the smallest levels in the one-CTA shared-memory kernel
+  bool use_tail = true;
+  long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)  // run the smallest levels in the one-CTA shared-memory kernel
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;
   std::vector<double> level_ms;

@@ -3,11 +3,19 @@
 #include <cmath>
 #include <cstring>
 
+#include <mutex>
+
 #include "topo_mg.h"
 
 namespace topo {
 
+std::recursive_mutex& device_lock() {
+  static std::recursive_mutex m;
+  return m;
+}
+
 Arena::~Arena() {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());
   for (void* p : ptrs_) cudaFree(p);
 }
 

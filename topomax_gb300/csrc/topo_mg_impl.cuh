@@ -642,8 +642,12 @@ void MG<T>::build_tail(Arena& arena) {
     void* p = arena.alloc(sizeof(h));
     if (!p) return;
     cudaMemcpy(p, &h, sizeof(h), cudaMemcpyHostToDevice);
-    if (cudaFuncSetAttribute(k_tail_vcycle<T, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(size_t(off) * sizeof(T))) != cudaSuccess) {
+    // the limit is a property of the kernel, shared by every context in the
+    // process: always the budget, so that no context lowers another's
+    const int static_bytes = int(sizeof(TailLevel<T, NC>) * kTailMaxLevels + sizeof(T) * kCoarseMaxDofs * kCoarseMaxDofs);
+    const int limit = int(std::min<size_t>(kTailSmemBudget, size_t(227 * 1024 - static_bytes)));
+    if (size_t(off) * sizeof(T) > size_t(limit) ||
+        cudaFuncSetAttribute(k_tail_vcycle<T, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
@@ -1009,6 +1013,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
 // every graph call is checked and nothing is launched unless all succeeded.
 template <class T>
 int MG<T>::capture_pcg(bool warm) {
+  std::lock_guard<std::recursive_mutex> lock(device_lock());
   cudaStream_t s = cap_[0], sb = cap_[1];
   if (!s || !sb) return -5;
   Graph& G = graph_[warm ? 1 : 0];
@@ -1097,15 +1102,22 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
   if (use_graphs && !G.exec) {
     // the recording streams must not see work still queued on s
     if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
-    if (capture_pcg(warm) != 0) return -5;
+    if (capture_pcg(warm) != 0) {
+      // a recording can fail when another thread's work synchronises the device
+      // meanwhile (first use of a kernel, a free); this solve then runs the same
+      // kernels from the host and the next one records again
+      cudaGetLastError();
+      ++capture_failures;
+    }
   }
+  const bool graphs = use_graphs && G.exec;
   hdev_->tol2 = rtol * rtol;
   hdev_->maxit = maxit;
   cudaMemcpyAsync(bi, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   if (warm) cudaMemcpyAsync(xi, x, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(&dev_->tol2, &hdev_->tol2, sizeof(double), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(&dev_->maxit, &hdev_->maxit, sizeof(int), cudaMemcpyHostToDevice, s);
-  if (use_graphs) {
+  if (graphs) {
     cudaGraphLaunch(G.exec, s);
     launches += G.prologue_nodes;
   } else {
@@ -1125,7 +1137,7 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
   if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
   st.iterations = hdev_->it;
   st.relres = hdev_->relres;
-  if (use_graphs) launches += (long long)hdev_->it * G.body_nodes;
+  if (graphs) launches += (long long)hdev_->it * G.body_nodes;
   switch (hdev_->status) {
     case 0: return 0;
     case 5:

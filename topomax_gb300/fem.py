@@ -169,11 +169,8 @@ class _Context:
         self._lib = _capi.load_library()
 
     def __del__(self):
+        # topo_destroy frees with cudaFree, which waits for the device's pending work
         if getattr(self, "ptr", None):
-            try:
-                torch.cuda.synchronize()
-            except Exception:
-                pass
             self._lib.topo_destroy(self.ptr)
             self.ptr = None
 
@@ -211,6 +208,13 @@ class HelmholtzFilter:
                 raise _capi.TopoError(st.value, f"could not create the filter (status {st.value})")
             _ctx = _Context(ptr)
         self._ctx = _ctx
+
+    def mass_apply(self, values) -> torch.Tensor:
+        """M1 x: the consistent CG1 mass matrix times nodal values (FP64, lattice order)."""
+        x = as_cg1_tensor(values, self.function_space)
+        y = torch.empty_like(x)
+        self._ctx.check(self._ctx._lib.topo_mass_apply(self._ctx.ptr, _ptr(x), _ptr(y), _stream()))
+        return y
 
     def apply(self, input_function) -> Function:
         f = as_cg1_tensor(input_function, self.function_space)

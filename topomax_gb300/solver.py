@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _capi
-from .designs import ElasticityParameters, FluidParameters, parse_design
+from .designs import ElasticityParameters, FluidParameters, parse_design, parse_design_dict
 from .fem import (DEFAULT_RTOL, ElasticityProblem, Function, FunctionSpace, RectangleMesh, _device, _ptr,
                   _stream, as_cg1_tensor)
 from .utils import IterationData, SolverResult, Timer
@@ -39,16 +39,27 @@ def logit(x):
 class Solver(ABC):
     """EMD driver; subclasses supply the discretisation hooks (src/solver.py:80-128)."""
 
-    def __init__(self, N: int, design_file: str, data_path="output", skip_multiple=1, verbose=True,
+    def __init__(self, N: int, design_file, data_path="output", skip_multiple=1, verbose=True,
                  save=True):
+        """design_file: a design JSON path as in the reference, or the parsed JSON dict itself
+        (its optional top-level "name" names the output folder)."""
         self.full_N = N
         self.design_file = design_file
-        self.design_str = os.path.splitext(os.path.basename(design_file))[0]
+        if isinstance(design_file, dict):
+            design_file = dict(design_file)
+            self.design_str = str(design_file.pop("name", "design"))
+            self._design_dict = design_file
+        else:
+            self.design_str = os.path.splitext(os.path.basename(design_file))[0]
+            self._design_dict = None
         self.output_folder = f"{data_path}/{self.get_name()}/{self.design_str}/data"
         self.skip_multiple = skip_multiple
         self.verbose = verbose
         self.save = save
-        self.parameters, problem_parameters = parse_design(design_file)
+        if self._design_dict is not None:
+            self.parameters, problem_parameters = parse_design_dict(self._design_dict)
+        else:
+            self.parameters, problem_parameters = parse_design(design_file)
         self.width = self.parameters.width
         self.height = self.parameters.height
         self.N = int(self.full_N / min(self.width, self.height))
@@ -111,7 +122,7 @@ class Solver(ABC):
 class FEMSolver(Solver):
     """Structured-grid FEM design loop on the GPU (FEM_src/solver.py:15-89)."""
 
-    def __init__(self, N: int, design_file: str, data_path: str = "output", skip_multiple: int = 1, *,
+    def __init__(self, N: int, design_file, data_path: str = "output", skip_multiple: int = 1, *,
                  precision: str = "mixed", rtol: float = DEFAULT_RTOL, verbose: bool = True, save: bool = True,
                  max_iterations: int = 1000):
         self.precision = precision
