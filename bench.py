@@ -17,9 +17,13 @@ state solve + compliance).
   design resident in HBM, CUDA events per step, L2 flushed (256 MB write)
   before every step.
 * ``fp64``: the same loop with plain FP64 multigrid CG (the metric's
-  comparison), and the max relative compliance difference between the two.
-* ``e2e``: the same step through the reference-facing API with host (pinned)
-  arrays, as the reference's Solver.step/project/set_from_array drive it.
+  comparison) over the same design steps as the first timed mixed steps, and the
+  max relative compliance difference between the two.
+* ``e2e``: the same steps (same warm-up, same step sizes) through the
+  reference-facing API with host (pinned) arrays, as the reference's
+  Solver.step/project/set_from_array drive it.
+* ``c2_2000x1000``: the same loop on the 2000x1000 grid of the throughput
+  configuration (16,012,002 dofs), with its operator's bandwidth.
 * ``roofline``: the dominant kernel (the FP32 matrix-free P2 operator),
   algorithmic bytes 2*V2u*4 + V1*4 per launch over its CUDA-event duration
   measured in this run, against the measured HBM copy bandwidth.
@@ -58,6 +62,8 @@ def parse():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--fp64-steps", type=int, default=4)
     ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--c2-steps", type=int, default=2,
+                    help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
     ap.add_argument("--cpu-sample", default="160x80,320x160", help="oracle grids timed for the CPU baseline")
     return ap.parse_args()
 
@@ -253,13 +259,13 @@ def main():
         prob._ctx._lib.topo_launch_count(prob._ctx.ptr, ctypes.byref(n))
         return n.value
 
-    def device_loop(prob, steps, warmup, time_operator=False, profile=False):
+    def device_loop(prob, steps, warmup, time_operator=False, profile=False, space=None, start=None):
         """Design-resident loop; returns per-step ms (CUDA events), objectives, launches, operator ms.
 
         With profile=True the timed steps are bracketed by cudaProfilerStart/Stop, so that a
         profiler run with --profile-from-start off records exactly those launches."""
         lib = prob._ctx._lib
-        rho = F.Function(V, rho0.cuda())
+        rho = F.Function(space or V, (start if start is not None else rho0).cuda())
         psi = torch.log(rho.tensor / (1 - rho.tensor))
         objs = [prob.calculate_objective(rho)]
         times, op_ms = [], []
@@ -311,7 +317,7 @@ def main():
         volume = prob.domain_size[0] * prob.domain_size[1] * 0.5
         solver = _E2ESolver(prob, V, volume)
         times = []
-        for k in range(warmup + steps):
+        for k in range(warmup + steps):  # the same EMD step sizes as the device loop's steps
             flush.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -342,20 +348,38 @@ def main():
         total_ms = float(t.item())
     ms = total_ms / args.steps
     value = world * args.steps / (total_ms / 1000.0)
-    e2e_times = e2e_loop(prob, args.e2e_steps, 1)
+    e2e_times = e2e_loop(prob, args.e2e_steps, args.warmup)
     e2e_value = 1.0 / float(np.mean(e2e_times))
     stats = dict(prob.stats)
     del prob
     torch.cuda.empty_cache()
 
-    # --- plain FP64 comparison
+    # --- plain FP64 comparison: the same design steps as the first timed mixed steps
     prob64 = make("fp64")
-    times64, objs64, _, _ = device_loop(prob64, args.fp64_steps, 1)
+    times64, objs64, _, _ = device_loop(prob64, args.fp64_steps, args.warmup)
     ms64 = float(np.mean(times64))
+    ms_mixed_same = float(np.mean(times[:len(times64)]))
     del prob64
     torch.cuda.empty_cache()
     n = min(len(objs), len(objs64))
     comp_rel = max(abs(a - b) / abs(b) for a, b in zip(objs[:n], objs64[:n]))
+
+    # --- the 2000 x 1000 grid of the throughput configuration (16,012,002 P2 dofs)
+    c2 = None
+    if args.c2_steps > 0:
+        mesh2 = tg.RectangleMesh(2.0, 1.0, 2000, 1000)
+        V2 = tg.FunctionSpace(mesh2, "CG", 1)
+        g2 = torch.Generator().manual_seed(0)
+        rho02 = (torch.rand(V2.dim(), generator=g2, dtype=torch.float64) * 0.99 + 0.01)
+        prob2 = tg.ElasticityProblem(mesh2, V2, dom, par, precision="mixed", rtol=args.rtol)
+        prob2.set_penalization(PENALTY)
+        t2, _, _, op2 = device_loop(prob2, args.c2_steps, args.warmup, time_operator=True, space=V2, start=rho02)
+        alg2 = 2 * dofs(2000, 1000) * 4 + V2.dim() * 4
+        c2 = {"workload": "cantilever 2x1, 2000x1000 squares, vector P2, 16012002 dofs, rtol %g" % args.rtol,
+              "value": 1000.0 / float(np.mean(t2)), "ms_per_step": float(np.mean(t2)), "steps": len(t2),
+              "operator_launch_ms": float(np.mean(op2)), "operator_gbs": alg2 / (float(np.mean(op2)) * 1e-3) / 1e9}
+        del prob2
+        torch.cuda.empty_cache()
 
     # --- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
@@ -378,7 +402,7 @@ def main():
                                f"{dofs(args.nx, args.ny)} dofs, rtol {args.rtol}, replicas: {world}",
                    "l2": "flushed (256 MB write) before every timed step"},
         "fp64": {"value": 1000.0 / ms64 * world, "ms_per_step": ms64, "steps": len(times64)},
-        "mixed_over_fp64": ms64 / ms,
+        "mixed_over_fp64": ms64 / ms_mixed_same,
         "compliance_rel_diff_mixed_vs_fp64": comp_rel,
         "e2e": {"value": e2e_value * world, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                 "d2h_bytes_per_step": 2 * nbytes + 8},
@@ -388,6 +412,7 @@ def main():
                      "launch_ms": op},
         "cpu_baseline": {k: v for k, v in cpu.items() if k != "seconds_per_iteration_at_target"},
         "gpu_launches": int(nlaunch),
+        "c2_2000x1000": c2,
         "clocks": ck,
         "solver_iterations": stats,
     }
