@@ -14,6 +14,7 @@
 #include "topo_mg.h"
 #include "topo_p1.cuh"
 #include "topo_p2.cuh"
+#include "topo_p1march.cuh"
 #include "topo_setup.h"
 
 using namespace topo;
@@ -83,6 +84,43 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
         for (int l = 0; l < 32; ++l) {
           P2March<T>::advance(L[l]);
           P2March<T>::template load<1>(P, io, xi, L[l], j);
+        }
+        down(1);
+      }
+    }
+}
+
+// Runs the P1 column-march kernel on the CPU (lanes in lockstep, shuffles as copies).
+template <class T, int NC>
+void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
+  const int seg = p2_march_segment(P.nx, P.ny, 4);
+  const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
+  std::vector<P1Lane<T, NC>> L(32);
+  auto down = [&](int r0) {
+    for (int l = 0; l < 31; ++l)
+      if (!L[l].edge)
+        for (int r = r0; r <= 1; ++r)
+          for (int d = 0; d < NC; ++d) L[l].U[r][1][d] = L[l + 1].U[r][0][d];
+  };
+  for (int w = 0; w < nxw; ++w)
+    for (int js = 0; js < P.ny; js += seg) {
+      const int je = std::min(js + seg, P.ny);
+      for (int l = 0; l < 32; ++l) P1March<T, NC>::begin(L[l], w * P2M_OWN - 1 + l, l == 31);
+      int j = js > 0 ? js - 1 : 0;
+      for (int l = 0; l < 32; ++l) P1March<T, NC>::template load<0>(P, io, L[l], j);
+      down(0);
+      for (;;) {
+        for (int l = 0; l < 32; ++l) P1March<T, NC>::compute(P, L[l], j);
+        for (int l = 31; l >= 1; --l)
+          for (int r = 0; r < 2; ++r)
+            for (int d = 0; d < NC; ++d) L[l].A[r][0][d] += L[l - 1].A[r][1][d];
+        if (j >= js)
+          for (int l = 1; l < 32; ++l)
+            if (L[l].i <= P.nx) P1March<T, NC>::finish(P, io, L[l], j, j == P.ny - 1 ? 2 : 1);
+        if (++j >= je) break;
+        for (int l = 0; l < 32; ++l) {
+          P1March<T, NC>::advance(L[l]);
+          P1March<T, NC>::template load<1>(P, io, L[l], j);
         }
         down(1);
       }
@@ -248,7 +286,14 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
           else P1Smooth<double, K>::post2(a, b, Q, B);
         }
     };
-    if (stencil) {
+    if (stencil == 2) {  // the column march
+      P1Io<double> io;
+      std::memset(&io, 0, sizeof(io));
+      io.mode = mode;
+      io.u = B.x;
+      io.B = B;
+      p1_march_run<double, K>(P, io);
+    } else if (stencil) {
       // the assembled-stencil representation of the same level
       constexpr int SW = StencilLayout<K>::stride;
       std::vector<double> st(size_t(nx + 1) * (ny + 1) * SW);

@@ -217,12 +217,14 @@ def test_level_chain_shapes():
     assert c2["nx"] == 3 and c2["dir"][2] == 2
 
 
-@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil"])
+@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil", "p1x2-march",
+                                   "p1x1-march"])
 def test_fused_smoothing_steps_match_composition(level):
     """PRE / RES / FIRST / POST2 against the same steps composed from plain applies
-    (P1 levels also through their assembled 7-point stencil)."""
+    (P1 levels also through their assembled 7-point stencil and the column march)."""
     stencil = level.endswith("-stencil")
-    level = level.replace("-stencil", "")
+    march = level.endswith("-march")
+    level = level.replace("-stencil", "").replace("-march", "")
     nx, ny, hx, hy, p = 34, 10, 0.05, 0.05, 3.0
     lam, mu = lame(1.0, 0.3)
     rng = np.random.default_rng(21)
@@ -253,25 +255,29 @@ def test_fused_smoothing_steps_match_composition(level):
     cheb = np.array([0.7, 0.3, 0.9])
     bufs = dict(b=b.copy(), dinv=dinv.copy(), x=x.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
     # PRE
-    emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
+    emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
+               march=march)
     d0 = cheb[0] * dinv * b
     ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
     # RES
     bufs["x"] = x.copy()
-    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
+    emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
+               march=march)
     rr = b - A(x)
     assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
     # FIRST (coarse correction already added to x) then POST2
     xc = rng.standard_normal(NC * c["NX"] * c["NY"]) * _free_rows(c["dir"], c["NX"], c["NY"], NC)
     u = x + emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
     bufs["x"] = u.copy()
-    emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
+    emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
+               march=march)
     r0 = b - A(u)
     dd0 = cheb[0] * dinv * r0
     assert np.max(np.abs(bufs["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
     assert np.max(np.abs(bufs["x2"] - (u + dd0))) <= 1e-12 * np.max(np.abs(u))
-    emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil)
+    emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
+               march=march)
     r1 = r0 - A(dd0)
     ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))

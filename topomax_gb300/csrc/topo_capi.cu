@@ -71,6 +71,13 @@ __global__ void k_cell_rmass(int nx, int ny, Penal<double> pen, const double* __
   TOPO_GRID_STRIDE(c, nc) cell_rmass<T>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
 }
 
+// the FP32 operator's own r-weighted mass matrices (same arithmetic as its
+// on-the-fly evaluation, so reading them instead changes no result)
+__global__ void k_cell_rmass32(int nx, int ny, Penal<float> pen, const float* __restrict__ xi, float* __restrict__ out) {
+  const size_t nc = size_t(nx) * ny;
+  TOPO_GRID_STRIDE(c, nc) cell_rmass<float>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
+}
+
 __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
                                 int nxc, int nyc) {
   const size_t nt = size_t(2) * nxc * nyc;
@@ -566,14 +573,15 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
   k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64);
   if (C->precision == TOPO_PREC_MIXED) {
-    // optional (TOPO_RMASS32=1): the r-weighted mass matrices (12 values per
-    // cell, evaluated in FP64) read by the FP32 operator instead of seven r(xi)
-    // evaluations per triangle; the evaluation costs more per design iteration
-    // than the reads save, so the default evaluates on the fly
+    // the r-weighted mass matrices (12 values per cell) evaluated once per
+    // design by the FP32 operator's own code and read by it afterwards instead
+    // of seven r(xi) evaluations per triangle per apply (TOPO_RMASS32=0: on the fly)
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
     if (C->rm_op32) {
-      k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op32);
-      k_cell_rmass<float><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc32);
+      k_cell_rmass32<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, C->p2params<float>(0).pen, C->xi32,
+                                                             C->rm_op32);
+      k_cell_rmass32<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, C->p2params<float>(1).pen, C->xi32,
+                                                             C->rm_pc32);
       C->launches += 2;
     }
     C->smg32.set_p2(C->p2params<float>(0, C->rm_op32), C->p2params<float>(1, C->rm_pc32), C->xi32);
@@ -661,7 +669,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       const size_t ncell = size_t(C->nx) * C->ny;
       C->rm_op64 = C->arena.alloc_n<double>(12 * ncell);
       if (precision == TOPO_PREC_FP64) C->rm_pc64 = C->arena.alloc_n<double>(12 * ncell);
-      if (precision == TOPO_PREC_MIXED && env_flag("TOPO_RMASS32", false)) {
+      if (precision == TOPO_PREC_MIXED && env_flag("TOPO_RMASS32", true)) {
         C->rm_op32 = C->arena.alloc_n<float>(12 * ncell);
         C->rm_pc32 = C->arena.alloc_n<float>(12 * ncell);
       }

@@ -151,6 +151,7 @@ class MG {
   // false runs the same kernels from a host loop
   bool use_graphs = true;
   bool use_tail = true;
+  bool use_p1_march = true;  // large P1 levels: column march (false: node-centric kernels)
   long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)  // run the smallest levels in the one-CTA shared-memory kernel
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;

@@ -11,6 +11,7 @@
 
 #include "topo_mg.h"
 #include "topo_p1.cuh"
+#include "topo_p1march.cuh"
 #include "topo_p2.cuh"
 #include "topo_vec.cuh"
 
@@ -127,6 +128,48 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
         }
       }
     }
+  }
+}
+
+// The column-march kernel of the large P1 levels (see P1March).
+template <class T, int NC, int MODE>
+__global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1Io<T> io, int seg) {
+  io.mode = MODE;
+  const int lane = threadIdx.x & 31;
+  const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
+  if (js >= P.ny) return;  // whole warp
+  const int je = min(js + seg, P.ny);
+  P1Lane<T, NC> L;
+  P1March<T, NC>::begin(L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
+  const bool owner = lane > 0 && L.i <= P.nx;
+  int j = js > 0 ? js - 1 : 0;
+  auto down = [&](int r0) {
+#pragma unroll
+    for (int r = 0; r <= 1; ++r) {
+      if (r < r0) continue;
+#pragma unroll
+      for (int d = 0; d < NC; ++d) {
+        const T v = shfl_down1(L.U[r][0][d]);
+        if (!L.edge) L.U[r][1][d] = v;
+      }
+    }
+  };
+  P1March<T, NC>::template load<0>(P, io, L, j);
+  down(0);
+  for (;;) {
+    P1March<T, NC>::compute(P, L, j);
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int d = 0; d < NC; ++d) {
+        const T v = shfl_up1(L.A[r][1][d]);
+        if (lane > 0) L.A[r][0][d] += v;
+      }
+    if (owner && j >= js) P1March<T, NC>::finish(P, io, L, j, j == P.ny - 1 ? 2 : 1);
+    if (++j >= je) break;
+    P1March<T, NC>::advance(L);
+    P1March<T, NC>::template load<1>(P, io, L, j);
+    down(1);
   }
 }
 
@@ -436,6 +479,19 @@ inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io,
   }
 }
 
+template <class T, int NC>
+inline void launch_p1_march(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
+  int seg = 0;
+  const dim3 g = p2_march_grid(P.nx, P.ny, seg);
+  switch (io.mode) {
+    case kP2Apply: k_p1_march<T, NC, kP2Apply><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+    case kP2Pre: k_p1_march<T, NC, kP2Pre><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+    case kP2Res: k_p1_march<T, NC, kP2Res><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+    case kP2First: k_p1_march<T, NC, kP2First><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+    default: k_p1_march<T, NC, kP2Post2><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+  }
+}
+
 template <class T>
 inline void launch_p2_apply(const P2Params<T>& P, const T* xi, const T* x, T* y, cudaStream_t s) {
   P2Io<T> io;
@@ -670,15 +726,27 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   const dim3 g = row_grid(L.NX, L.NY);
   const Lev& v = lv_[l];
   if (L.NC == 2) {
-    if (v.st && stencils_ready_)
+    if (v.st && stencils_ready_) {
       k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st}, x, y);
-    else
-      k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(make_p1<T, 2>(L, refs_[l], v.kK, nullptr), x, y);
+    } else {
+      P1Io<T> io;
+      std::memset(&io, 0, sizeof(io));
+      io.mode = kP2Apply;
+      io.u = x;
+      io.y = y;
+      launch_p1_march<T, 2>(make_p1<T, 2>(L, refs_[l], v.kK, nullptr), io, s);
+    }
   } else {
-    if (v.st && stencils_ready_)
+    if (v.st && stencils_ready_) {
       k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st}, x, y);
-    else
-      k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(make_p1<T, 1>(L, refs_[l], v.kK, v.kM), x, y);
+    } else {
+      P1Io<T> io;
+      std::memset(&io, 0, sizeof(io));
+      io.mode = kP2Apply;
+      io.u = x;
+      io.y = y;
+      launch_p1_march<T, 1>(make_p1<T, 1>(L, refs_[l], v.kK, v.kM), io, s);
+    }
   }
 }
 
@@ -921,13 +989,37 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     k_p1_smooth<T, NC, kP2Post2, PP><<<gf, kRowThreads, 0, s>>>(P, B);
     launches += 3;
   };
+  // large levels without a stencil: the column march (element products per cell)
+  auto run_march = [&](auto nc_tag, const auto& P) {
+    constexpr int NC = decltype(nc_tag)::value;
+    P1Io<T> io;
+    std::memset(&io, 0, sizeof(io));
+    io.B = B;
+    io.u = x;
+    io.mode = kP2Pre;
+    launch_p1_march<T, NC>(P, io, s);
+    io.mode = kP2Res;
+    launch_p1_march<T, NC>(P, io, s);
+    k_restrict<T, NC><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launches += 3;
+    vcycle_level(l + 1, c.b, c.x, s);
+    k_prolong_add<T, NC><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
+    io.mode = kP2First;
+    launch_p1_march<T, NC>(P, io, s);
+    io.mode = kP2Post2;
+    launch_p1_march<T, NC>(P, io, s);
+    launches += 3;
+  };
   using I2 = std::integral_constant<int, 2>;
   using I1 = std::integral_constant<int, 1>;
+  const bool march = !v.st && use_p1_march;
   if (S.NC == 2) {
     if (v.st) run(I2{}, P1Stencil<T, 2>{S.nx, S.ny, S.dir, v.st});
+    else if (march) run_march(I2{}, make_p1<T, 2>(S, refs_[l], v.kK, nullptr));
     else run(I2{}, make_p1<T, 2>(S, refs_[l], v.kK, nullptr));
   } else {
     if (v.st) run(I1{}, P1Stencil<T, 1>{S.nx, S.ny, S.dir, v.st});
+    else if (march) run_march(I1{}, make_p1<T, 1>(S, refs_[l], v.kK, v.kM));
     else run(I1{}, make_p1<T, 1>(S, refs_[l], v.kK, v.kM));
   }
 }

@@ -1,0 +1,169 @@
+// Column-march kernel phases for the large P1 levels (the same scheme as the
+// P2 march, see P2March): a warp covers 32 consecutive cell columns
+// i = i0-1 .. i0+30 and marches upward through a segment of cell rows.  At
+// step j lane L works on cell (i0-1+L, j): it holds the operand at the cell's
+// 2x2 nodes (i+c, j+r) and the element results there.  Column 1 of a lane is
+// column 0 of the next lane (operand down by a shuffle, results up), row 1 of
+// a step is row 0 of the next (registers).  After a step the lane holds the
+// complete sum at its node (i, j) and finishes it (apply or a fused smoothing
+// step, the formulas of P1Smooth).  Per cell: two element products
+// y = kK Kref u (+ kM Mref u), against ~six incidences per node walked by the
+// node-centric kernel.
+#pragma once
+
+#include "topo_p1.cuh"
+#include "topo_p2.cuh"
+
+namespace topo {
+
+template <class T>
+struct P1Io {
+  int mode;         // P2Mode: kP2Apply, kP2Pre, kP2Res, kP2First, kP2Post2
+  const T* u;       // Apply / Res / First operand (x)
+  T* y;             // Apply output
+  SmoothBufs<T> B;  // smoothing modes
+};
+
+template <class T, int NC>
+struct P1Lane {
+  int i;            // cell column
+  bool edge;        // last lane of the warp: loads its column 1 itself
+  T U[2][2][NC];    // operand at nodes (i+c, j+r), zero at clamped nodes
+  T A[2][2][NC];    // element results at the same nodes
+};
+
+template <class T, int NC>
+struct P1March {
+  TOPO_HD static void operand(const P1Io<T>& io, size_t n, T (&v)[NC]) {
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      switch (io.mode) {
+        case kP2Pre: v[c] = io.B.cheb[0] * io.B.dinv[i] * io.B.b[i]; break;
+        case kP2Post2: v[c] = io.B.d[i]; break;
+        default: v[c] = io.u[i];
+      }
+    }
+  }
+
+  // operand at node (a,b); zero outside the lattice and at clamped nodes
+  TOPO_HD static void fetch(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, T (&v)[NC]) {
+    for (int c = 0; c < NC; ++c) v[c] = T(0);
+    if (a >= 0 && a <= P.nx && b >= 0 && b <= P.ny && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b)))
+      operand(io, size_t(b) * (P.nx + 1) + a, v);
+  }
+
+  template <int R0>
+  TOPO_HD static void load(const P1Params<T, NC>& P, const P1Io<T>& io, P1Lane<T, NC>& L, int j) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = R0; r <= 1; ++r) {
+      fetch(P, io, L.i, j + r, L.U[r][0]);
+      if (L.edge) fetch(P, io, L.i + 1, j + r, L.U[r][1]);
+    }
+  }
+
+  template <int O>
+  TOPO_HD static void tri(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int j) {
+    const size_t t = (size_t(j) * P.nx + L.i) * 2 + O;
+    const T kk = P.kK ? P.kK[t] : P.kK_c;
+    T km = T(0);
+    if constexpr (NC == 1) km = P.kM ? P.kM[t] : P.kM_c;
+    T u[3][NC];
+#define TOPO_LD(LV) \
+  for (int d = 0; d < NC; ++d) u[LV][d] = L.U[P1Off<O, LV>::b][P1Off<O, LV>::a][d];
+    TOPO_LD(0) TOPO_LD(1) TOPO_LD(2)
+#undef TOPO_LD
+#define TOPO_ST(LV)                                                                 \
+  for (int c = 0; c < NC; ++c) {                                                    \
+    T s = T(0);                                                                     \
+    for (int l = 0; l < 3; ++l)                                                     \
+      for (int d = 0; d < NC; ++d) s += P.K[O][LV * NC + c][l * NC + d] * u[l][d];  \
+    T y = kk * s;                                                                   \
+    if constexpr (NC == 1) {                                                        \
+      T m = T(0);                                                                   \
+      for (int l = 0; l < 3; ++l) m += P.Mm[O][LV][l] * u[l][0];                    \
+      y += km * m;                                                                  \
+    }                                                                               \
+    L.A[P1Off<O, LV>::b][P1Off<O, LV>::a][c] += y;                                  \
+  }
+    TOPO_ST(0) TOPO_ST(1) TOPO_ST(2)
+#undef TOPO_ST
+  }
+
+  TOPO_HD static void compute(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int j) {
+    if (L.i < 0 || L.i >= P.nx || j < 0 || j >= P.ny) return;
+    tri<0>(P, L, j);
+    tri<1>(P, L, j);
+  }
+
+  // finish node (a,b) with the complete sum t (clamped rows act as identity rows)
+  TOPO_HD static void finish_node(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, const T (&sum)[NC],
+                                  const T (&u)[NC]) {
+    const size_t n = size_t(b) * (P.nx + 1) + a;
+    const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
+    T un[NC], t[NC];
+    for (int c = 0; c < NC; ++c) {
+      un[c] = u[c];
+      t[c] = sum[c];
+    }
+    if (cl) {
+      operand(io, n, un);  // the loaded copy is zero at clamped nodes
+      for (int c = 0; c < NC; ++c) t[c] = un[c];
+    }
+    const SmoothBufs<T>& B = io.B;
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      switch (io.mode) {
+        case kP2Apply: io.y[i] = t[c]; break;
+        case kP2Pre: {
+          const T r1 = B.b[i] - t[c];
+          B.x[i] = un[c] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
+          break;
+        }
+        case kP2Res: B.r[i] = B.b[i] - t[c]; break;
+        case kP2First: {
+          const T r0 = B.b[i] - t[c];
+          const T d0 = B.cheb[0] * B.dinv[i] * r0;
+          B.r[i] = r0;
+          B.d[i] = d0;
+          B.x2[i] = un[c] + d0;
+          break;
+        }
+        default: {  // kP2Post2
+          const T r1 = B.r[i] - t[c];
+          B.x[i] = B.x2[i] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
+        }
+      }
+    }
+  }
+
+  // finish the lane's node of row 0 (and of row 1 on the last cell row)
+  TOPO_HD static void finish(const P1Params<T, NC>& P, const P1Io<T>& io, const P1Lane<T, NC>& L, int j, int nrows) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = 0; r < 2; ++r)
+      if (r < nrows && j + r <= P.ny) finish_node(P, io, L.i, j + r, L.A[r][0], L.U[r][0]);
+  }
+
+  // row 1 becomes row 0 of the next step
+  TOPO_HD static void advance(P1Lane<T, NC>& L) {
+    for (int c = 0; c < 2; ++c)
+      for (int d = 0; d < NC; ++d) {
+        L.U[0][c][d] = L.U[1][c][d];
+        L.A[0][c][d] = c == 0 ? L.A[1][c][d] : T(0);  // column 1 went to the next lane
+        L.A[1][c][d] = T(0);
+      }
+  }
+
+  TOPO_HD static void begin(P1Lane<T, NC>& L, int i, bool edge) {
+    L.i = i;
+    L.edge = edge;
+    for (int r = 0; r < 2; ++r)
+      for (int c = 0; c < 2; ++c)
+        for (int d = 0; d < NC; ++d) L.U[r][c][d] = L.A[r][c][d] = T(0);
+  }
+};
+
+}  // namespace topo

@@ -466,14 +466,14 @@ inline int p2_march_segment(int nx, int ny, int sms) {
 // ---------------------------------------------------------------------------
 
 // r-weighted mass matrices of every triangle, layout [o][k][cell] (P2Params::rmass)
-template <class T>
-TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const double* xi, const Penal<double>& pen, T* out) {
+template <class T, class TC>
+TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<TC>& pen, T* out) {
   const size_t nc = size_t(nx) * ny, c = size_t(j) * nx + i;
   const int VX = nx + 1;
   for (int o = 0; o < 2; ++o) {
-    double xe[3];
+    TC xe[3];
     for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
-    double M[6];
+    TC M[6];
     tri_rmass(xe, pen, M);
     for (int k = 0; k < 6; ++k) out[(size_t(o) * 6 + k) * nc + c] = T(M[k]);
   }
