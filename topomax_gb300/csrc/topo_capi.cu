@@ -199,9 +199,11 @@ struct topo_ctx {
   MG<float> smg32;
   MG<double> smg64;
   float* xi32 = nullptr;
+  double* xi64 = nullptr;  // FP64 mode: the design copied to a fixed buffer (graphs keep their parameters)
   // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
+  bool trace_solves = false;  // TOPO_TRACE_SOLVES=1: one line per refinement step and inner solve
   double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
   double* fst64_mass = nullptr;
   float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
@@ -313,6 +315,7 @@ bool env_flag(const char* name, bool dflt) {
 }
 
 int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
+  C->trace_solves = env_flag("TOPO_TRACE_SOLVES", false);
   if (!g || g->nx < 1 || g->ny < 1 || !(g->width > 0) || !(g->height > 0))
     return C->fail(TOPO_ERR_ARG, "invalid grid description");
   if (precision != TOPO_PREC_FP64 && precision != TOPO_PREC_MIXED)
@@ -455,6 +458,9 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     k_sub<double><<<g, kVecThreads, 0, s>>>(r, b, W.t, n);
     const double beta = std::sqrt(C->dot64(r, r, n, s));
     st.relres = beta / bn;
+    if (C->trace_solves)
+      std::fprintf(stderr, "[topo solve] fgmres cycle %d: |r|/|b| %.3e after %d inner iterations\n", cycle, beta / bn,
+                   st.iterations);
     if (!std::isfinite(beta)) return C->fail(TOPO_ERR_NAN, "non-finite residual");
     if (beta <= rtol * bn) return TOPO_OK;
     if (cycle > 0 && beta > 0.9 * prev) break;  // stagnation at the FP64 residual floor
@@ -474,6 +480,9 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       SolveStats is;
       const int rc = mg.pcg(r32, zj, false, inner, maxit, is, s);
       st.iterations += is.iterations;
+      if (C->trace_solves)
+        std::fprintf(stderr, "[topo solve]   inner %d: tol %.1e, %d iterations, FP32 relres %.3e, rc %d\n", j, inner,
+                     is.iterations, is.relres, rc);
       st.minres |= is.minres;
       if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
       if (rc == -5) return C->fail(TOPO_ERR_CUDA, "inner solve: CUDA graph recording or launch failed");
@@ -588,7 +597,8 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
     st = C->smg32.setup(s);
   } else {
     k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->rm_pc64);
-    C->smg64.set_p2(C->p2params<double>(0, C->rm_op64), C->p2params<double>(1, C->rm_pc64), xi);
+    cudaMemcpyAsync(C->xi64, xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    C->smg64.set_p2(C->p2params<double>(0, C->rm_op64), C->p2params<double>(1, C->rm_pc64), C->xi64);
     st = C->smg64.setup(s);
   }
   if (st == -5) return C->fail(TOPO_ERR_CUDA, "state set-up: CUDA error");
@@ -679,7 +689,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg32.use_graphs = graphs_enabled();
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
-    C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg32.set_coefficients(kK, kM);
         C->xi32 = C->arena.alloc_n<float>(C->nv);
         C->d32 = C->arena.alloc_n<float>(n);
@@ -689,8 +699,9 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg64.use_graphs = graphs_enabled();
         C->smg64.use_tail = env_flag("TOPO_TAIL", true);
         C->smg64.profile_levels = env_flag("TOPO_PROFILE", false);
-    C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
+        C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg64.set_coefficients(kK, kM);
+        C->xi64 = C->arena.alloc_n<double>(C->nv);
         C->sens_tri = C->arena.alloc_n<double>(size_t(3) * C->sspec[0].ntri());
       }
       if (C->arena.failed()) rc = C->fail(TOPO_ERR_CUDA, "out of device memory");
