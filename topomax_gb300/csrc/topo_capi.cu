@@ -204,6 +204,8 @@ struct topo_ctx {
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
   bool trace_solves = false;  // TOPO_TRACE_SOLVES=1: one line per refinement step and inner solve
+  // tightest relative tolerance of an FP32 inner solve (TOPO_INNER_FLOOR_STATE / _FILTER)
+  double inner_floor_state = 2e-3, inner_floor_filter = 1e-5;
   double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
   double* fst64_mass = nullptr;
   float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
@@ -316,6 +318,10 @@ bool env_flag(const char* name, bool dflt) {
 
 int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
   C->trace_solves = env_flag("TOPO_TRACE_SOLVES", false);
+  if (const char* e = std::getenv("TOPO_INNER_FLOOR_STATE"))
+    C->inner_floor_state = std::max(1e-8, std::min(0.5, std::atof(e)));
+  if (const char* e = std::getenv("TOPO_INNER_FLOOR_FILTER"))
+    C->inner_floor_filter = std::max(1e-8, std::min(0.5, std::atof(e)));
   if (!g || g->nx < 1 || g->ny < 1 || !(g->width > 0) || !(g->height > 0))
     return C->fail(TOPO_ERR_ARG, "invalid grid description");
   if (precision != TOPO_PREC_FP64 && precision != TOPO_PREC_MIXED)
@@ -428,7 +434,7 @@ int filter_stencils64(topo_ctx* C) {
 // has a nearly singular or slightly negative mode that FP32 cannot resolve.
 template <class Apply64>
 int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, double* x, bool warm, size_t n,
-              double rtol, Fgmres& W, int maxit, SolveStats& st, cudaStream_t s) {
+              double rtol, Fgmres& W, int maxit, double inner_floor, SolveStats& st, cudaStream_t s) {
   constexpr int m = Fgmres::m;
   const int g = C->grid(n);
   st = SolveStats{};
@@ -466,7 +472,10 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     if (cycle > 0 && beta > 0.9 * prev) break;  // stagnation at the FP64 residual floor
     prev = beta;
     k_scale<double><<<g, kVecThreads, 0, s>>>(r, 1.0 / beta, n);
-    const double inner = std::min(0.1, std::max(1e-5, 0.3 * rtol * bn / beta));
+    // an inner solve need not go much below what one refinement step can use:
+    // the FP32 operator itself differs from the FP64 one by ~1e-3 relative on
+    // high-contrast designs (rounding of K u with large, smooth u)
+    const double inner = std::min(0.1, std::max(inner_floor, 0.3 * rtol * bn / beta));
     double H[m + 1][m] = {};
     double cs[m], sn[m], gv[m + 1] = {};
     gv[0] = beta;
@@ -556,7 +565,7 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   int rc;
   if (C->precision == TOPO_PREC_MIXED) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
-    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, kFilterMaxIt, st, s);
+    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, kFilterMaxIt, C->inner_floor_filter, st, s);
   } else {
     rc = C->fmg64.pcg(b, xi, false, rtol, kFilterMaxIt, st, s);
     if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
@@ -809,7 +818,8 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     if (ctx->precision == TOPO_PREC_MIXED) {
       P2Params<double> P64 = ctx->p2params<double>(0, ctx->rm_op64);
       auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
-      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, kStateMaxIt, st, s);
+      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, kStateMaxIt, ctx->inner_floor_state,
+                     st, s);
     } else {
       rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, kStateMaxIt, st, s);
       if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");
