@@ -47,7 +47,7 @@ void dir_to(const Dir& r, int* d) {
 // each phase in turn and the shuffles become copies between lane states.
 template <class T>
 void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0) {
-  if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4);
+  if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   const bool operand = io.mode != kP2Diag;
   std::vector<P2Lane<T>> L(32);
@@ -72,18 +72,26 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
       const int je = std::min(js + seg, P.ny);
       for (int l = 0; l < 32; ++l) P2March<T>::begin(L[l], w * P2M_OWN - 1 + l, l == 31);
       int j = js > 0 ? js - 1 : 0;
-      for (int l = 0; l < 32; ++l) P2March<T>::template load<0>(P, io, xi, L[l], j);
+      for (int l = 0; l < 32; ++l) {
+        P2March<T>::template load<0>(P, io, xi, L[l], j);
+        P2March<T>::load_mass(P, L[l].i, j, L[l].M);
+      }
       down(0);
+      std::vector<P2Next<T>> N(32);
       for (;;) {
+        const bool more = j + 1 < je;
+        if (more)
+          for (int l = 0; l < 32; ++l) P2March<T>::prefetch(P, io, xi, L[l], j + 1, N[l]);
         for (int l = 0; l < 32; ++l) P2March<T>::compute(P, L[l], j, io.mode);
         up();
         if (j >= js)
           for (int l = 1; l < 32; ++l)
             if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, acc);
-        if (++j >= je) break;
+        if (!more) break;
+        ++j;
         for (int l = 0; l < 32; ++l) {
           P2March<T>::advance(L[l]);
-          P2March<T>::template load<1>(P, io, xi, L[l], j);
+          P2March<T>::take(L[l], N[l]);
         }
         down(1);
       }
@@ -93,7 +101,7 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
 // Runs the P1 column-march kernel on the CPU (lanes in lockstep, shuffles as copies).
 template <class T, int NC>
 void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
-  const int seg = p2_march_segment(P.nx, P.ny, 4);
+  const int seg = p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   std::vector<P1Lane<T, NC>> L(32);
   auto down = [&](int r0) {
@@ -107,9 +115,16 @@ void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
       const int je = std::min(js + seg, P.ny);
       for (int l = 0; l < 32; ++l) P1March<T, NC>::begin(L[l], w * P2M_OWN - 1 + l, l == 31);
       int j = js > 0 ? js - 1 : 0;
-      for (int l = 0; l < 32; ++l) P1March<T, NC>::template load<0>(P, io, L[l], j);
+      for (int l = 0; l < 32; ++l) {
+        P1March<T, NC>::template load<0>(P, io, L[l], j);
+        P1March<T, NC>::load_coef(P, L[l].i, j, L[l].kk, L[l].km);
+      }
       down(0);
+      std::vector<P1Next<T, NC>> N(32);
       for (;;) {
+        const bool more = j + 1 < je;
+        if (more)
+          for (int l = 0; l < 32; ++l) P1March<T, NC>::prefetch(P, io, L[l], j + 1, N[l]);
         for (int l = 0; l < 32; ++l) P1March<T, NC>::compute(P, L[l], j);
         for (int l = 31; l >= 1; --l)
           for (int r = 0; r < 2; ++r)
@@ -117,10 +132,11 @@ void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
         if (j >= js)
           for (int l = 1; l < 32; ++l)
             if (L[l].i <= P.nx) P1March<T, NC>::finish(P, io, L[l], j, j == P.ny - 1 ? 2 : 1);
-        if (++j >= je) break;
+        if (!more) break;
+        ++j;
         for (int l = 0; l < 32; ++l) {
           P1March<T, NC>::advance(L[l]);
-          P1March<T, NC>::template load<1>(P, io, L[l], j);
+          P1March<T, NC>::take(L[l], N[l]);
         }
         down(1);
       }

@@ -104,14 +104,19 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     const bool owner = lane > 0 && L.i <= P.nx;
     int j = js > 0 ? js - 1 : 0;
     P2March<T>::template load<0>(P, io, xi, L, j);
+    P2March<T>::load_mass(P, L.i, j, L.M);
     p2m_exchange_down<T, 0, OPERAND>(L);
+    P2Next<T> N;
     for (;;) {
+      const bool more = j + 1 < je;
+      if (more) P2March<T>::prefetch(P, io, xi, L, j + 1, N);  // in flight during this step's arithmetic
       P2March<T>::compute(P, L, j, MODE);
       p2m_exchange_up<T>(L, lane);
       if (owner && j >= js) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2, acc);
-      if (++j >= je) break;
+      if (!more) break;
+      ++j;
       P2March<T>::advance(L);
-      P2March<T>::template load<1>(P, io, xi, L, j);
+      P2March<T>::take(L, N);
       p2m_exchange_down<T, 1, OPERAND>(L);
     }
   }
@@ -155,8 +160,12 @@ __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1I
     }
   };
   P1March<T, NC>::template load<0>(P, io, L, j);
+  P1March<T, NC>::load_coef(P, L.i, j, L.kk, L.km);
   down(0);
+  P1Next<T, NC> N;
   for (;;) {
+    const bool more = j + 1 < je;
+    if (more) P1March<T, NC>::prefetch(P, io, L, j + 1, N);  // in flight during this step's arithmetic
     P1March<T, NC>::compute(P, L, j);
 #pragma unroll
     for (int r = 0; r < 2; ++r)
@@ -166,9 +175,10 @@ __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1I
         if (lane > 0) L.A[r][0][d] += v;
       }
     if (owner && j >= js) P1March<T, NC>::finish(P, io, L, j, j == P.ny - 1 ? 2 : 1);
-    if (++j >= je) break;
+    if (!more) break;
+    ++j;
     P1March<T, NC>::advance(L);
-    P1March<T, NC>::template load<1>(P, io, L, j);
+    P1March<T, NC>::take(L, N);
     down(1);
   }
 }
@@ -459,36 +469,91 @@ inline int device_sms() {
   return cached[dev];
 }
 
-inline dim3 p2_march_grid(int nx, int ny, int& seg) {
-  seg = p2_march_segment(nx, ny, device_sms());
+// resident blocks per SM of a march kernel at P2M_THREADS threads (its
+// registers decide: the grid is sized to one wave of them)
+template <class K>
+inline int march_blocks_per_sm(K kernel) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, P2M_THREADS, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    b = 0;
+  }
+  return b > 0 ? b : 1;
+}
+
+template <class T, int MODE>
+inline int p2_march_bps() {
+  static const int b = march_blocks_per_sm(k_p2_march<T, MODE>);
+  return b;
+}
+
+template <class T, int NC, int MODE>
+inline int p1_march_bps() {
+  static const int b = march_blocks_per_sm(k_p1_march<T, NC, MODE>);
+  return b;
+}
+
+inline dim3 march_grid(int nx, int ny, int blocks_per_sm, int& seg) {
+  seg = p2_march_segment(nx, ny, device_sms(), blocks_per_sm);
   const int nseg = (ny + seg - 1) / seg;
   return dim3((nx + 1 + P2M_OWN - 1) / P2M_OWN, (nseg + P2M_WARPS - 1) / P2M_WARPS);
 }
 
+// occupancy queries happen outside any stream capture
+template <class T>
+inline void prime_march_occupancy() {
+  (void)p2_march_bps<T, kP2Apply>();
+  (void)p2_march_bps<T, kP2Diag>();
+  (void)p2_march_bps<T, kP2Pre>();
+  (void)p2_march_bps<T, kP2Res>();
+  (void)p2_march_bps<T, kP2First>();
+  (void)p2_march_bps<T, kP2Post2>();
+  (void)p1_march_bps<T, 1, kP2Apply>();
+  (void)p1_march_bps<T, 1, kP2Pre>();
+  (void)p1_march_bps<T, 1, kP2Res>();
+  (void)p1_march_bps<T, 1, kP2First>();
+  (void)p1_march_bps<T, 1, kP2Post2>();
+  (void)p1_march_bps<T, 2, kP2Apply>();
+  (void)p1_march_bps<T, 2, kP2Pre>();
+  (void)p1_march_bps<T, 2, kP2Res>();
+  (void)p1_march_bps<T, 2, kP2First>();
+  (void)p1_march_bps<T, 2, kP2Post2>();
+}
+
+template <class T, int MODE>
+inline void launch_p2_mode(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
+  int seg = 0;
+  const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<T, MODE>(), seg);
+  k_p2_march<T, MODE><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg);
+}
+
 template <class T>
 inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
-  int seg = 0;
-  const dim3 g = p2_march_grid(P.nx, P.ny, seg);
   switch (io.mode) {
-    case kP2Apply: k_p2_march<T, kP2Apply><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
-    case kP2Diag: k_p2_march<T, kP2Diag><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
-    case kP2Pre: k_p2_march<T, kP2Pre><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
-    case kP2Res: k_p2_march<T, kP2Res><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
-    case kP2First: k_p2_march<T, kP2First><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
-    default: k_p2_march<T, kP2Post2><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg); break;
+    case kP2Apply: launch_p2_mode<T, kP2Apply>(P, xi, io, s); break;
+    case kP2Diag: launch_p2_mode<T, kP2Diag>(P, xi, io, s); break;
+    case kP2Pre: launch_p2_mode<T, kP2Pre>(P, xi, io, s); break;
+    case kP2Res: launch_p2_mode<T, kP2Res>(P, xi, io, s); break;
+    case kP2First: launch_p2_mode<T, kP2First>(P, xi, io, s); break;
+    default: launch_p2_mode<T, kP2Post2>(P, xi, io, s); break;
   }
+}
+
+template <class T, int NC, int MODE>
+inline void launch_p1_mode(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
+  int seg = 0;
+  const dim3 g = march_grid(P.nx, P.ny, p1_march_bps<T, NC, MODE>(), seg);
+  k_p1_march<T, NC, MODE><<<g, P2M_THREADS, 0, s>>>(P, io, seg);
 }
 
 template <class T, int NC>
 inline void launch_p1_march(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
-  int seg = 0;
-  const dim3 g = p2_march_grid(P.nx, P.ny, seg);
   switch (io.mode) {
-    case kP2Apply: k_p1_march<T, NC, kP2Apply><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
-    case kP2Pre: k_p1_march<T, NC, kP2Pre><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
-    case kP2Res: k_p1_march<T, NC, kP2Res><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
-    case kP2First: k_p1_march<T, NC, kP2First><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
-    default: k_p1_march<T, NC, kP2Post2><<<g, P2M_THREADS, 0, s>>>(P, io, seg); break;
+    case kP2Apply: launch_p1_mode<T, NC, kP2Apply>(P, io, s); break;
+    case kP2Pre: launch_p1_mode<T, NC, kP2Pre>(P, io, s); break;
+    case kP2Res: launch_p1_mode<T, NC, kP2Res>(P, io, s); break;
+    case kP2First: launch_p1_mode<T, NC, kP2First>(P, io, s); break;
+    default: launch_p1_mode<T, NC, kP2Post2>(P, io, s); break;
   }
 }
 
@@ -608,6 +673,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   mu_ = mu;
   red_ = red;
   sms_ = red->sms;
+  prime_march_occupancy<T>();
   lv_.assign(specs.size(), Lev{});
   for (size_t l = 0; l < specs.size(); ++l) {
     const size_t n = specs[l].ndof();
@@ -1061,9 +1127,12 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   const size_t n = specs_[0].ndof();
   const int g = vec_grid(n, sms_);
   T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  // both fused launches (operator and last post-smoothing) must fit the partial slots
   int seg = 0;
-  const dim3 mg = p2_march_grid(specs_[0].nx, specs_[0].ny, seg);
-  if (specs_[0].p2 && size_t(mg.x) * mg.y * 2 <= size_t(red_->blocks) * 16) {
+  const dim3 ga = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Apply>(), seg);
+  const dim3 gp = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Post2>(), seg);
+  const size_t mblocks = std::max(size_t(ga.x) * ga.y, size_t(gp.x) * gp.y);
+  if (specs_[0].p2 && mblocks * 2 <= size_t(red_->blocks) * 16) {
     // P2 level 0: p.q is reduced inside the operator launch, r.r / r.z and the
     // iteration's test inside the V-cycle's last post-smoothing launch
     P2Io<T> io;

@@ -30,6 +30,14 @@ struct P1Lane {
   bool edge;        // last lane of the warp: loads its column 1 itself
   T U[2][2][NC];    // operand at nodes (i+c, j+r), zero at clamped nodes
   T A[2][2][NC];    // element results at the same nodes
+  T kk[2], km[2];   // the cell's triangle coefficients
+};
+
+// The loads of the next step, issued before the current step's arithmetic.
+template <class T, int NC>
+struct P1Next {
+  T U[2][NC];       // operand row 1 of the next step (column 1 on the edge lane)
+  T kk[2], km[2];
 };
 
 template <class T, int NC>
@@ -63,12 +71,37 @@ struct P1March {
     }
   }
 
+  // coefficients of cell (i, j) (zero outside the mesh)
+  TOPO_HD static void load_coef(const P1Params<T, NC>& P, int i, int j, T (&kk)[2], T (&km)[2]) {
+    const bool in = i >= 0 && i < P.nx && j >= 0 && j < P.ny;
+    for (int o = 0; o < 2; ++o) {
+      const size_t t = in ? (size_t(j) * P.nx + i) * 2 + o : 0;
+      kk[o] = in ? (P.kK ? P.kK[t] : P.kK_c) : T(0);
+      km[o] = (in && NC == 1) ? (P.kM ? P.kM[t] : P.kM_c) : T(0);
+    }
+  }
+
+  TOPO_HD static void prefetch(const P1Params<T, NC>& P, const P1Io<T>& io, const P1Lane<T, NC>& L, int j,
+                               P1Next<T, NC>& N) {
+    fetch(P, io, L.i, j + 1, N.U[0]);
+    if (L.edge) fetch(P, io, L.i + 1, j + 1, N.U[1]);
+    load_coef(P, L.i, j, N.kk, N.km);
+  }
+
+  // after advance(): the prefetched loads become row 1 of the step
+  TOPO_HD static void take(P1Lane<T, NC>& L, const P1Next<T, NC>& N) {
+    for (int c = 0; c < 2; ++c)
+      for (int d = 0; d < NC; ++d) L.U[1][c][d] = N.U[c][d];
+    for (int o = 0; o < 2; ++o) {
+      L.kk[o] = N.kk[o];
+      L.km[o] = N.km[o];
+    }
+  }
+
   template <int O>
-  TOPO_HD static void tri(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int j) {
-    const size_t t = (size_t(j) * P.nx + L.i) * 2 + O;
-    const T kk = P.kK ? P.kK[t] : P.kK_c;
-    T km = T(0);
-    if constexpr (NC == 1) km = P.kM ? P.kM[t] : P.kM_c;
+  TOPO_HD static void tri(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int) {
+    const T kk = L.kk[O];
+    const T km = L.km[O];
     T u[3][NC];
 #define TOPO_LD(LV) \
   for (int d = 0; d < NC; ++d) u[LV][d] = L.U[P1Off<O, LV>::b][P1Off<O, LV>::a][d];
@@ -163,6 +196,7 @@ struct P1March {
     for (int r = 0; r < 2; ++r)
       for (int c = 0; c < 2; ++c)
         for (int d = 0; d < NC; ++d) L.U[r][c][d] = L.A[r][c][d] = T(0);
+    L.kk[0] = L.kk[1] = L.km[0] = L.km[1] = T(0);
   }
 };
 

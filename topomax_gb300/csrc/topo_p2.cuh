@@ -238,6 +238,16 @@ struct P2Lane {
   T U[3][3][2];   // operand at nodes (2i+c, 2j+r), zero at clamped nodes
   T X[2][2];      // density at vertices (i+c, j+r)
   T A[3][3][2];   // element results at the same nodes
+  T M[12];        // r-weighted mass matrices of the cell (when precomputed), [o][k]
+};
+
+// The loads of the next step, issued before the current step's arithmetic so
+// that their latency hides behind it.
+template <class T>
+struct P2Next {
+  T U[2][3][2];   // operand rows 1, 2 of the next step
+  T X[2];         // density row 1 of the next step
+  T M[12];        // mass matrices of the next cell
 };
 
 template <class T>
@@ -328,10 +338,8 @@ struct P2March {
       TOPO_LD(0) TOPO_LD(1) TOPO_LD(2) TOPO_LD(3) TOPO_LD(4) TOPO_LD(5)
 #undef TOPO_LD
       if (P.rmass) {
-        const size_t nc = size_t(P.nx) * P.ny, c = size_t(j) * P.nx + L.i;
-        const T* m = P.rmass + size_t(O) * 6 * nc + c;
         T M[6];
-        for (int k = 0; k < 6; ++k) M[k] = m[k * nc];
+        for (int k = 0; k < 6; ++k) M[k] = L.M[O * 6 + k];
         tri_apply_m<O>(ue, M, P, y);
       } else {
         tri_apply<O>(ue, xe, P, y);
@@ -342,6 +350,46 @@ struct P2March {
   L.A[P2Off<O, K>::b][P2Off<O, K>::a][1] += y[K][1];
     TOPO_ST(0) TOPO_ST(1) TOPO_ST(2) TOPO_ST(3) TOPO_ST(4) TOPO_ST(5)
 #undef TOPO_ST
+  }
+
+  // mass matrices of cell (i, j) (zero outside the mesh)
+  TOPO_HD static void load_mass(const P2Params<T>& P, int i, int j, T (&M)[12]) {
+    if (!P.rmass) return;
+    const bool in = i >= 0 && i < P.nx && j >= 0 && j < P.ny;
+    const size_t nc = size_t(P.nx) * P.ny, c = in ? size_t(j) * P.nx + i : 0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int k = 0; k < 12; ++k) M[k] = in ? P.rmass[size_t(k) * nc + c] : T(0);
+  }
+
+  // the loads of step j (operand rows 1, 2, density row 1, mass matrices)
+  TOPO_HD static void prefetch(const P2Params<T>& P, const P2Io<T>& io, const T* xi, const P2Lane<T>& L, int j,
+                               P2Next<T>& N) {
+    if (io.mode != kP2Diag) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+      for (int r = 1; r <= 2; ++r) {
+        const int b = 2 * j + r;
+        fetch(P, io, 2 * L.i, b, N.U[r - 1][0]);
+        fetch(P, io, 2 * L.i + 1, b, N.U[r - 1][1]);
+        if (L.edge) fetch(P, io, 2 * L.i + 2, b, N.U[r - 1][2]);
+      }
+    }
+    N.X[0] = density(P, xi, L.i, j + 1);
+    if (L.edge) N.X[1] = density(P, xi, L.i + 1, j + 1);
+    load_mass(P, L.i, j, N.M);
+  }
+
+  // after advance(): the prefetched loads become rows 1, 2 of the step
+  TOPO_HD static void take(P2Lane<T>& L, const P2Next<T>& N) {
+    for (int r = 1; r <= 2; ++r)
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 2; ++d) L.U[r][c][d] = N.U[r - 1][c][d];
+    L.X[1][0] = N.X[0];
+    L.X[1][1] = N.X[1];
+    for (int k = 0; k < 12; ++k) L.M[k] = N.M[k];
   }
 
   // element results of cell (L.i, j), both triangles
@@ -446,19 +494,30 @@ struct P2March {
       for (int c = 0; c < 3; ++c)
         for (int d = 0; d < 2; ++d) L.U[r][c][d] = L.A[r][c][d] = T(0);
     L.X[0][0] = L.X[0][1] = L.X[1][0] = L.X[1][1] = T(0);
+    for (int k = 0; k < 12; ++k) L.M[k] = T(0);
   }
 };
 
-// Cell rows per warp segment: enough segments to fill every SM with the 20
-// warps its registers allow, at least 4 rows so that the recomputed row below
-// a segment stays a bounded share.
-inline int p2_march_segment(int nx, int ny, int sms) {
-  const long nxw = (nx + 1 + P2M_OWN - 1) / P2M_OWN;
-  const long want = long(sms) * 20;
-  long seg = (long(ny) * nxw + want - 1) / want;
+// Cell rows per warp segment.  A block holds P2M_WARPS consecutive segments of
+// one warp column, so the grid is (warp columns) x ceil(segments / P2M_WARPS)
+// blocks.  The segment is the shortest whose grid still fits in ONE wave of
+// `blocks_per_sm` resident blocks on each of `sms` SMs (a second, partial wave
+// costs a whole segment's latency for a few blocks), and at least 4 rows so
+// that the recomputed row below a segment stays a bounded share.  A lattice
+// too wide for one wave gets whole-height segments.
+inline int p2_march_segment(int nx, int ny, int sms, int blocks_per_sm) {
+  if (ny <= 1) return 1;
+  const long gx = (nx + 1 + P2M_OWN - 1) / P2M_OWN;
+  const long cap = long(sms > 0 ? sms : 1) * (blocks_per_sm > 0 ? blocks_per_sm : 1);
+  const long gy = cap / gx;  // block rows of one wave
+  long seg = ny;
+  if (gy >= 1) {
+    const long nseg = gy * P2M_WARPS;  // ceil(ny / seg) <= nseg  =>  at most gy block rows
+    seg = (ny + nseg - 1) / nseg;
+  }
   if (seg < 4) seg = 4;
   if (seg > ny) seg = ny;
-  return int(seg < 1 ? 1 : seg);
+  return int(seg);
 }
 
 // ---------------------------------------------------------------------------
