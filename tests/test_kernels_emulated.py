@@ -64,6 +64,39 @@ def test_p2_apply_fp32_matches_oracle(case):
     assert np.max(np.abs(y - ref)) <= 2e-5 * np.max(np.abs(ref))
 
 
+def test_p2_fp32_operator_consistent_at_smooth_fields():
+    """The FP32 operator at a solved (smooth, large) displacement of a high-contrast
+    design: its arithmetic must stay far below the FP32 representation error of u
+    itself (the element products work on u - u_A; products of u itself lose
+    ~|K||u|/|Ku| ~ 1e5 in relative accuracy and reach the representation error)."""
+    nx, ny = 40, 20
+    d = make_design(tractions=[dict(side="Right", center=0.5, length=0.2, value=[0.0, -1.0])])
+    L = Lattice(2.0, 1.0, nx, ny)
+    o = FEMOracle(L, d)
+    o.set_penalization(3.0)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    dirv = emu.make_dir(nx, ny, L.hx, L.hy, ["Left"])
+    X, Y = np.meshgrid(L.xv, L.yv)
+    X, Y = X.ravel(), Y.ravel()
+    bars = np.zeros_like(X)  # a truss of solid bars in a void of density 1e-3
+    for (x0, y0, x1, y1) in [(0, 0.05, 2, 0.45), (0, 0.95, 2, 0.55), (0, 0.05, 0, 0.95), (0.5, 0.2, 1.0, 0.8),
+                             (0, 0.5, 2, 0.5)]:
+        t = np.clip(((X - x0) * (x1 - x0) + (Y - y0) * (y1 - y0)) / ((x1 - x0) ** 2 + (y1 - y0) ** 2), 0, 1)
+        dist = np.hypot(X - x0 - t * (x1 - x0), Y - y0 - t * (y1 - y0))
+        bars = np.maximum(bars, np.clip(1.5 - dist / 0.03, 0, 1))
+    xi = 1e-3 + (1 - 1e-3) * bars
+    u = o.state_solve(xi)
+    f = o.apply_state(xi, u)
+    u32 = u.astype(np.float32).astype(np.float64)
+    y64 = o.apply_state(xi, u32)
+    y32 = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, 3.0, dirv, xi, u32, prec=1)
+    fn = np.linalg.norm(f)
+    representation = np.linalg.norm(y64 - f) / fn   # ~2e-3
+    arithmetic = np.linalg.norm(y32 - y64) / fn     # ~6e-5 (~3e-3 without differences)
+    assert representation > 5e-4
+    assert arithmetic <= 3e-4 and arithmetic <= 0.1 * representation
+
+
 @pytest.mark.parametrize("case", CASES)
 def test_p2_diag_matches_oracle(case):
     W, H, nx, ny, sides, p = case

@@ -1,6 +1,7 @@
 // C ABI of the topomax GB300 design loop: problem context, load assembly,
 // iterative refinement, sensitivity and the entropic-mirror-descent update.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -37,11 +38,11 @@ struct NewtonState {
 struct Fgmres {
   static constexpr int m = 8;  // restart length
   double* V = nullptr;         // (m+1) x n Krylov basis (FP64)
-  float* Z = nullptr;          // m x n preconditioned directions (FP32 inner solutions)
+  double* Z = nullptr;         // m x n preconditioned directions (inner solutions, accumulated in FP64)
   double* t = nullptr;         // n
   void init(Arena& a, size_t n) {
     V = a.alloc_n<double>((m + 1) * n);
-    Z = a.alloc_n<float>(m * n);
+    Z = a.alloc_n<double>(m * n);
     t = a.alloc_n<double>(n);
   }
 };
@@ -205,7 +206,7 @@ struct topo_ctx {
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
   bool trace_solves = false;  // TOPO_TRACE_SOLVES=1: one line per refinement step and inner solve
   // tightest relative tolerance of an FP32 inner solve (TOPO_INNER_FLOOR_STATE / _FILTER)
-  double inner_floor_state = 2e-3, inner_floor_filter = 1e-5;
+  double inner_floor_state = 1e-4, inner_floor_filter = 1e-5;
   double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
   double* fst64_mass = nullptr;
   float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
@@ -380,6 +381,7 @@ int init_filter(topo_ctx* C, double eps) {
   int st;
   if (C->precision == TOPO_PREC_MIXED) {
     C->fmg32.use_graphs = graphs_enabled();
+    C->fmg32.fp64_solution = true;  // FGMRES directions keep the inner solutions in FP64
     C->fmg32.use_tail = env_flag("TOPO_TAIL", true);
     C->fmg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
@@ -460,8 +462,12 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
   for (int cycle = 0; cycle < kMaxOuter; ++cycle) {
     double* r = W.V;
     C->launches += 4;
-    apply64(x, W.t, s);
-    k_sub<double><<<g, kVecThreads, 0, s>>>(r, b, W.t, n);
+    if (cycle == 0 && !warm) {
+      cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s);  // x = 0
+    } else {
+      apply64(x, W.t, s);
+      k_sub<double><<<g, kVecThreads, 0, s>>>(r, b, W.t, n);
+    }
     const double beta = std::sqrt(C->dot64(r, r, n, s));
     st.relres = beta / bn;
     if (C->trace_solves)
@@ -473,8 +479,8 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     prev = beta;
     k_scale<double><<<g, kVecThreads, 0, s>>>(r, 1.0 / beta, n);
     // an inner solve need not go much below what one refinement step can use:
-    // the FP32 operator itself differs from the FP64 one by ~1e-3 relative on
-    // high-contrast designs (rounding of K u with large, smooth u)
+    // the FP32 operator's arithmetic differs from the FP64 operator's by
+    // ~1e-5..1e-4 relative at smooth fields of high-contrast designs
     const double inner = std::min(0.1, std::max(inner_floor, 0.3 * rtol * bn / beta));
     double H[m + 1][m] = {};
     double cs[m], sn[m], gv[m + 1] = {};
@@ -484,10 +490,10 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       st.outer += 1;
       C->launches += 6;
       double* vj = W.V + size_t(j) * n;
-      float* zj = W.Z + size_t(j) * n;
+      double* zj = W.Z + size_t(j) * n;
       k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, vj, 1.0, n);
       SolveStats is;
-      const int rc = mg.pcg(r32, zj, false, inner, maxit, is, s);
+      const int rc = mg.pcg_x64(r32, zj, false, inner, maxit, is, s);
       st.iterations += is.iterations;
       if (C->trace_solves)
         std::fprintf(stderr, "[topo solve]   inner %d: tol %.1e, %d iterations, FP32 relres %.3e, rc %d\n", j, inner,
@@ -495,9 +501,8 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       st.minres |= is.minres;
       if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
       if (rc == -5) return C->fail(TOPO_ERR_CUDA, "inner solve: CUDA graph recording or launch failed");
-      k_convert<double, float><<<g, kVecThreads, 0, s>>>(W.t, zj, 1.0, n);
       double* w = W.V + size_t(j + 1) * n;
-      apply64(W.t, w, s);
+      apply64(zj, w, s);
       // classical Gram-Schmidt; a second pass only when the first one cancelled
       // more than half of w (Kahan's "twice is enough" test)
       double h[m + 1] = {};
@@ -549,7 +554,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     }
     MultiCoef cf{};
     for (int i = 0; i < k; ++i) cf.c[i] = y[i];
-#define TOPO_AM(K) k_add_multi<float, double, K><<<g, kVecThreads, 0, s>>>(x, W.Z, n, cf, n)
+#define TOPO_AM(K) k_add_multi<double, double, K><<<g, kVecThreads, 0, s>>>(x, W.Z, n, cf, n)
     TOPO_DISPATCH_COUNT(k, TOPO_AM)
 #undef TOPO_AM
   }
@@ -696,6 +701,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
         C->smg32.use_graphs = graphs_enabled();
+        C->smg32.fp64_solution = true;
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
@@ -809,8 +815,14 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
     if (!xi || !u || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid state-solve arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = state_setup(ctx, xi, s);
     if (rc) return rc;
+    if (ctx->trace_solves) {
+      cudaStreamSynchronize(s);
+      std::fprintf(stderr, "[topo solve] state set-up %.3f ms\n",
+                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
     ctx->xi_last = xi;
     const size_t n = 2 * ctx->nn2;
     const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
@@ -827,6 +839,12 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
       else if (rc) rc = ctx->fail(TOPO_ERR_NOT_CONVERGED, "state CG did not converge (relres %.3g)", st.relres);
     }
     if (iters) *iters = st.iterations;
+    if (ctx->trace_solves) {
+      cudaStreamSynchronize(s);
+      std::fprintf(stderr, "[topo solve] state solve %.3f ms (set-up included), %d inner iterations, %d outer steps\n",
+                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                   st.iterations, st.outer);
+    }
     if (rc) return rc;
     return ctx->cuda_check("state solve");
   });

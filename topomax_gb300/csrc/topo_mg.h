@@ -134,13 +134,22 @@ class MG {
   // Solves A x = b to ||r|| <= rtol ||b|| (x used as initial guess when x_nonzero).
   // Returns 0, -2 (iteration cap) or -4 (non-finite).
   int pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s);
+  // As pcg, with the solution accumulated and returned in FP64 (requires
+  // fp64_solution): x64 is the initial guess when x_nonzero (rounded to T) and
+  // receives the result.  Returns -5 when the object was set up without it.
+  int pcg_x64(const T* b, double* x64, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s);
   int minres(const T* b, T* x, double rtol, int maxit, SolveStats& st, cudaStream_t s);
   const LevelSpec& spec(int l) const { return specs_[l]; }
   int levels() const { return int(specs_.size()); }
   double lmax(int l) const { return lv_[l].lmax; }
   // device scratch vectors of level 0 (n dofs), free for callers between solves
   T* scratch0(int k) { return pcg_[k]; }
-  static constexpr int kScratch = 9;
+  static constexpr int kScratch = 10;
+  // Accumulate the CG solution in FP64 (x += alpha p with the exact product).
+  // With T = float the solution's own FP32 rounding limits its residual: on a
+  // high-contrast design |A fl32(u) - f| / |f| is ~1e-2 at the exact u, while
+  // the FP32 operator arithmetic alone is consistent to ~1e-4.  Set before init().
+  bool fp64_solution = false;
 
   int cheb_degree = 2;  // the fused smoothing kernels implement degree 2
   double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
@@ -150,9 +159,9 @@ class MG {
   // record the CG loop as a CUDA graph with a device-side WHILE node (default);
   // false runs the same kernels from a host loop
   bool use_graphs = true;
-  bool use_tail = true;
+  bool use_tail = true;      // run the smallest levels in the one-CTA shared-memory kernel
   bool use_p1_march = true;  // large P1 levels: column march (false: node-centric kernels)
-  long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)  // run the smallest levels in the one-CTA shared-memory kernel
+  long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;
   std::vector<double> level_ms;
@@ -180,7 +189,9 @@ class MG {
   int capture_pcg(bool warm);
   void pcg_prologue(bool warm, cudaStream_t s);
   void pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond);
-  int graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s);
+  // x (precision T) or x64 (FP64 solution mode) is the initial guess / result
+  int graph_pcg(const T* b, T* x, double* x64, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s);
+  void pcg_xr(int g, cudaStream_t s);  // x += alpha p, r -= alpha q
   double dot(const T* a, const T* b, size_t n, cudaStream_t s);  // synchronising
   void diag_of(int l, T* d, cudaStream_t s);
   double estimate_lmax(int l, cudaStream_t s);
@@ -219,6 +230,7 @@ class MG {
   int fuse_use_cond_ = 0;
 
   T* pcg_[kScratch] = {};
+  double* xacc_ = nullptr;  // FP64 solution of the CG loop (fp64_solution)
   Reducer* red_ = nullptr;
   int sms_ = 148;
 };

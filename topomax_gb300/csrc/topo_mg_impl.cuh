@@ -603,8 +603,9 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 // ---------------------------------------------------------------------------
 // x += alpha p ; r -= alpha q with alpha = rz / pq read from device memory
 // (evaluated once per block: an FP64 division per thread is not free here)
-template <class T>
-__global__ void k_pcg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+// x in T or FP64 (TX = double: the product of two FP32 numbers is exact in FP64)
+template <class T, class TX>
+__global__ void k_pcg_xr(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
                          const PcgDev* __restrict__ dv, size_t n) {
   __shared__ T alpha_s;
   __shared__ bool ok_s;
@@ -617,7 +618,7 @@ __global__ void k_pcg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restri
   if (!ok_s) return;
   const T alpha = alpha_s;
   TOPO_GRID_STRIDE(i, n) {
-    x[i] += alpha * p[i];
+    x[i] += TX(alpha) * TX(p[i]);
     r[i] -= alpha * q[i];
   }
 }
@@ -697,6 +698,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   }
   const size_t n0 = specs[0].ndof();
   for (int k = 0; k < kScratch; ++k) pcg_[k] = arena.alloc_n<T>(n0);
+  if (fp64_solution) xacc_ = arena.alloc_n<double>(n0);
   const int nc = int(specs.back().ndof());
   cinv_ = arena.alloc_n<T>(size_t(nc) * nc);
   cstat_ = arena.alloc_n<int>(1);
@@ -1110,16 +1112,28 @@ void MG<T>::pcg_prologue(bool warm, cudaStream_t s) {
   if (warm) {
     apply(0, xi, q, s, true);
     k_sub<T><<<g, kVecThreads, 0, s>>>(r, bi, q, n);
+    // the FP64 solution starts exactly at the guess the residual belongs to
+    if (xacc_) k_convert<double, T><<<g, kVecThreads, 0, s>>>(xacc_, xi, 1.0, n);
   } else {
     k_fill<T><<<g, kVecThreads, 0, s>>>(xi, T(0), n);
+    if (xacc_) k_fill<double><<<g, kVecThreads, 0, s>>>(xacc_, 0.0, n);
     cudaMemcpyAsync(r, bi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   }
+  if (xacc_) launches += 1;
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(bi, bi, n, red_->partials, red_->counter, &dev_->bb);
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(r, r, n, red_->partials, red_->counter, &dev_->rr);
   vcycle(r, z, s);
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(r, z, n, red_->partials, red_->counter, &dev_->rz);
   cudaMemcpyAsync(p, z, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   launches += 5;
+}
+
+template <class T>
+void MG<T>::pcg_xr(int g, cudaStream_t s) {
+  const size_t n = specs_[0].ndof();
+  T *r = pcg_[0], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  if (xacc_) k_pcg_xr<T, double><<<g, kVecThreads, 0, s>>>(xacc_, r, p, q, dev_, n);
+  else k_pcg_xr<T, T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
 }
 
 template <class T>
@@ -1145,7 +1159,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
     io.counter = red_->counter;
     io.pcg = dev_;
     launch_p2_tile<T>(p2_op_, xi_, io, s);
-    k_pcg_xr<T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
+    pcg_xr(g, s);
     fuse_rz_ = true;
     fuse_cond_ = (unsigned long long)h;
     fuse_use_cond_ = use_cond;
@@ -1157,7 +1171,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   }
   apply(0, p, q, s, true);
   k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(p, q, n, red_->partials, red_->counter, &dev_->pq);
-  k_pcg_xr<T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
+  pcg_xr(g, s);
   vcycle(r, z, s);
   k_dot2<T><<<red_->blocks, kVecThreads, 0, s>>>(r, r, r, z, n, red_->partials, red_->counter, &dev_->rr);
   k_pcg_check<<<1, 1, 0, s>>>(dev_, h, use_cond);
@@ -1247,7 +1261,8 @@ int MG<T>::capture_pcg(bool warm) {
 // rtol^2 and the iteration cap are written to the device scalars the start
 // kernel reads, and the result and the scalars come back after one sync.
 template <class T>
-int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s) {
+int MG<T>::graph_pcg(const T* b, T* x, double* x64, bool warm, double rtol, int maxit, SolveStats& st,
+                     cudaStream_t s) {
   const size_t n = specs_[0].ndof();
   T* bi = pcg_[5];
   T* xi = pcg_[6];
@@ -1275,7 +1290,10 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
   hdev_->tol2 = rtol * rtol;
   hdev_->maxit = maxit;
   cudaMemcpyAsync(bi, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
-  if (warm) cudaMemcpyAsync(xi, x, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  if (warm) {
+    if (x64) k_convert<T, double><<<vec_grid(n, sms_), kVecThreads, 0, s>>>(xi, x64, 1.0, n);
+    else cudaMemcpyAsync(xi, x, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  }
   cudaMemcpyAsync(&dev_->tol2, &hdev_->tol2, sizeof(double), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(&dev_->maxit, &hdev_->maxit, sizeof(int), cudaMemcpyHostToDevice, s);
   if (graphs) {
@@ -1293,7 +1311,8 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
       pcg_body(s, 0, 0);
     }
   }
-  cudaMemcpyAsync(x, xi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  if (x64) cudaMemcpyAsync(x64, xacc_, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  else cudaMemcpyAsync(x, xi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(hdev_, dev_, sizeof(PcgDev), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
   st.iterations = hdev_->it;
@@ -1302,7 +1321,8 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
   switch (hdev_->status) {
     case 0: return 0;
     case 5:
-      k_fill<T><<<vec_grid(n, sms_), kVecThreads, 0, s>>>(x, T(0), n);
+      if (x64) k_fill<double><<<vec_grid(n, sms_), kVecThreads, 0, s>>>(x64, 0.0, n);
+      else k_fill<T><<<vec_grid(n, sms_), kVecThreads, 0, s>>>(x, T(0), n);
       return 0;
     case 4: return -4;
     case 3: return -3;  // breakdown: caller falls back
@@ -1313,11 +1333,35 @@ int MG<T>::graph_pcg(const T* b, T* x, bool warm, double rtol, int maxit, SolveS
 template <class T>
 int MG<T>::pcg(const T* b, T* x, bool x_nonzero, double rtol, int maxit, SolveStats& st, cudaStream_t s) {
   st = SolveStats{};
-  int rc = graph_pcg(b, x, x_nonzero, rtol, maxit, st, s);
+  int rc = graph_pcg(b, x, nullptr, x_nonzero, rtol, maxit, st, s);
   if (rc == -3) {
     // p.Ap <= 0: the operator is indefinite here; continue with MINRES from x
     SolveStats ms;
     rc = minres(b, x, rtol, std::max(1, maxit - st.iterations), ms, s);
+    st.iterations += ms.iterations;
+    st.relres = ms.relres;
+    st.minres = 1;
+  }
+  return rc;
+}
+
+template <class T>
+int MG<T>::pcg_x64(const T* b, double* x64, bool x_nonzero, double rtol, int maxit, SolveStats& st,
+                   cudaStream_t s) {
+  st = SolveStats{};
+  if (!xacc_) return -5;
+  int rc = graph_pcg(b, nullptr, x64, x_nonzero, rtol, maxit, st, s);
+  if (rc == -3) {
+    // MINRES continues in T from the iterate rounded to T (pcg_[9]: neither
+    // MINRES's work vectors nor the callers' scratch0(4))
+    const size_t n = specs_[0].ndof();
+    const int g = vec_grid(n, sms_);
+    T* xt = pcg_[9];
+    k_convert<T, double><<<g, kVecThreads, 0, s>>>(xt, x64, 1.0, n);
+    SolveStats ms;
+    rc = minres(b, xt, rtol, std::max(1, maxit - st.iterations), ms, s);
+    k_convert<double, T><<<g, kVecThreads, 0, s>>>(x64, xt, 1.0, n);
+    launches += 2;
     st.iterations += ms.iterations;
     st.relres = ms.relres;
     st.minres = 1;
