@@ -159,3 +159,15 @@ def smooth(mode, p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, N
                      dp(xi) if xi is not None else None, dp(kK) if kK is not None else None, ptrs, dp(cheb),
                      NXc, NYc, ip(dirc), dp(xc) if xc is not None else None, dp(bc) if bc is not None else None,
                      2 if march else int(stencil))
+
+
+def coarse_cheb(nx, ny, hx, hy, eps2, b, deg=0):
+    """Chebyshev coarse solve of eps2 K + M from x = 0; returns (x, lo, hi, planned degree)."""
+    E = lib()
+    E.emu_coarse_cheb.argtypes = [C_I, C_I, C_D, C_D, C_D, C_I, P_D, P_D, P_D]
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    info = np.zeros(3)
+    rc = E.emu_coarse_cheb(nx, ny, hx, hy, eps2, deg, dp(b), dp(x), dp(info))
+    assert rc == 0
+    return x, info[0], info[1], int(info[2])

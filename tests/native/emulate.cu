@@ -446,4 +446,66 @@ int emu_vertex_weights(int nx, int ny, double hx, double hy, double* w) {
   return 0;
 }
 
+// Coarse Chebyshev solve of the scalar level eps2 K + M (assembled stencil, no
+// clamping) from x = 0: the node phases of k_coarse_cheb run sequentially.
+// info: [lo, hi, degree] of the plan for the level's coefficient ratio eps2.
+int emu_coarse_cheb(int nx, int ny, double hx, double hy, double eps2, int deg_force, const double* b, double* x,
+                    double* info) {
+  const ElemRefs R = make_elem_refs(hx, hy, 0.0, 0.0);
+  const int NX = nx + 1, NY = ny + 1, nn = NX * NY;
+  P1Params<double, 1> P;
+  std::memset(&P, 0, sizeof(P));
+  P.nx = nx;
+  P.ny = ny;
+  std::memset(&P.dir, 0, sizeof(P.dir));  // no clamped nodes
+  P.dir.x_hi_from = NX;
+  P.dir.y_hi_from = NY;
+  for (int o = 0; o < 2; ++o)
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) {
+        P.K[o][a][c] = R.K1[o][a][c];
+        P.Mm[o][a][c] = R.M1[o][a][c];
+      }
+  P.kK_c = eps2;
+  P.kM_c = 1.0;
+  constexpr int SW = StencilLayout<1>::stride;
+  std::vector<double> st(size_t(nn) * SW), dinv(nn);
+  for (int bb = 0; bb < NY; ++bb)
+    for (int a = 0; a < NX; ++a) p1_stencil_node<double, 1>(a, bb, P, st.data() + (size_t(bb) * NX + a) * SW);
+  for (int n = 0; n < nn; ++n) {  // diagonal = row sum - couplings (difference form)
+    double d = st[size_t(n) * SW];
+    for (int k = 1; k < 7; ++k) d -= st[size_t(n) * SW + k];
+    dinv[n] = 1.0 / d;
+  }
+  double lo, hi;
+  int deg = coarse_cheb_plan(R, eps2, eps2, 1e-2, lo, hi);
+  info[0] = lo;
+  info[1] = hi;
+  info[2] = deg;
+  if (deg_force > 0) deg = deg_force;
+  if (deg > kCoarseChebMax) return 1;
+  CoarseCheb<double> C;
+  std::memset(&C, 0, sizeof(C));
+  double c0, c1[kCoarseChebMax], c2[kCoarseChebMax];
+  coarse_cheb_coefficients(lo, hi, deg, c0, c1, c2);
+  C.deg = deg;
+  C.c0 = c0;
+  for (int k = 0; k + 1 < deg; ++k) {
+    C.c1[k] = c1[k];
+    C.c2[k] = c2[k];
+  }
+  const P1Stencil<double, 1> S{nx, ny, P.dir, st.data()};
+  std::vector<double> r(nn), xv(nn), d0(nn), d1(nn);
+  for (int n = 0; n < nn; ++n) CoarseChebNode<double, 1>::init(size_t(n), C, b, dinv.data(), r.data(), xv.data(), d0.data());
+  double* dc = d0.data();
+  double* dn = d1.data();
+  for (int k = 0; k + 1 < deg; ++k) {
+    for (int n = 0; n < nn; ++n)
+      CoarseChebNode<double, 1>::step(n % NX, n / NX, k, S, C, dinv.data(), dc, r.data(), xv.data(), dn);
+    std::swap(dc, dn);
+  }
+  for (int n = 0; n < nn; ++n) CoarseChebNode<double, 1>::finish(size_t(n), dc, xv.data(), x);
+  return 0;
+}
+
 }  // extern "C"

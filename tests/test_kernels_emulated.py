@@ -322,3 +322,44 @@ def test_fused_smoothing_steps_match_composition(level):
         assert np.max(np.abs(bufs2["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
         assert np.max(np.abs(bufs2["x2"] - (u + dd0))) <= 1e-12 * np.max(np.abs(u))
         assert np.array_equal(bufs2["x"], x)
+
+
+@pytest.mark.parametrize("nx,ny,radius", [(16, 8, 0.05), (24, 12, 0.05), (12, 6, 0.2)])
+def test_coarse_chebyshev_solve(nx, ny, radius):
+    """Truncated filter hierarchy: the planned interval holds the spectrum of
+    Dinv A (A = eps^2 K + M), the node phases equal the textbook recurrence on the
+    oracle's assembled matrix, the solve is a symmetric operator, and it reduces
+    the error (A-norm) by the planned factor."""
+    W, H = 2.0, 1.0
+    d = make_design(width=W, height=H, filter_radius=radius)
+    L = Lattice(W, H, nx, ny)
+    o = FEMOracle(L, d)
+    eps2 = (radius / (2.0 * np.sqrt(3.0))) ** 2
+    A = (eps2 * o.K1 + o.M1).toarray()
+    Dg = np.diag(A)
+    rng = np.random.default_rng(4)
+    b1, b2 = rng.standard_normal(L.n_vertices), rng.standard_normal(L.n_vertices)
+    x1, lo, hi, deg = emu.coarse_cheb(nx, ny, L.hx, L.hy, eps2, b1)
+    ev = np.linalg.eigvals(A / Dg[:, None]).real
+    assert lo <= ev.min() and ev.max() <= hi
+    assert 1 <= deg <= 16
+    # textbook Chebyshev iteration (Saad, Alg. 12.1) from x = 0
+    theta, delta = 0.5 * (hi + lo), 0.5 * (hi - lo)
+    sigma = theta / delta
+    rho = 1.0 / sigma
+    r = b1.copy()
+    dd = r / Dg / theta
+    x = np.zeros_like(b1)
+    for _ in range(deg - 1):
+        x += dd
+        r -= A @ dd
+        rn = 1.0 / (2.0 * sigma - rho)
+        dd = rn * rho * dd + 2.0 * rn / delta * r / Dg
+        rho = rn
+    x += dd
+    assert np.max(np.abs(x1 - x)) <= 1e-12 * np.max(np.abs(x))
+    x2, *_ = emu.coarse_cheb(nx, ny, L.hx, L.hy, eps2, b2)
+    assert abs(x1 @ b2 - x2 @ b1) <= 1e-12 * abs(x1 @ b1)
+    e = np.linalg.solve(A, b1)
+    err = np.sqrt((x1 - e) @ A @ (x1 - e) / (e @ A @ e))
+    assert err <= 1e-2

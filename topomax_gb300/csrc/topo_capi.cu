@@ -52,20 +52,6 @@ __device__ __forceinline__ double expit_d(double x) { return 1.0 / (1.0 + exp(-x
 // ---------------------------------------------------------------------------
 // design-level kernels
 // ---------------------------------------------------------------------------
-__global__ void k_kappa_p2(int nx, int ny, Penal<double> pen, const double* __restrict__ xi,
-                           double* __restrict__ kK) {
-  const size_t nt = size_t(2) * nx * ny;
-  const int VX = nx + 1;
-  TOPO_GRID_STRIDE(t, nt) {
-    const int o = int(t & 1);
-    const size_t cell = t >> 1;
-    const int i = int(cell % nx), j = int(cell / nx);
-    double xe[3];
-    for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
-    kK[t] = tri_kappa(xe, pen);
-  }
-}
-
 template <class T>
 __global__ void k_cell_rmass(int nx, int ny, Penal<double> pen, const double* __restrict__ xi, T* __restrict__ out) {
   const size_t nc = size_t(nx) * ny;
@@ -77,6 +63,13 @@ __global__ void k_cell_rmass(int nx, int ny, Penal<double> pen, const double* __
 __global__ void k_cell_rmass32(int nx, int ny, Penal<float> pen, const float* __restrict__ xi, float* __restrict__ out) {
   const size_t nc = size_t(nx) * ny;
   TOPO_GRID_STRIDE(c, nc) cell_rmass<float>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
+}
+
+// kappa of state level 1 and the FP64 operator's mass matrices, one pass
+__global__ void k_cell_rmass_kappa(int nx, int ny, Penal<double> pen, const double* __restrict__ xi,
+                                   double* __restrict__ rm, double* __restrict__ kK) {
+  const size_t nc = size_t(nx) * ny;
+  TOPO_GRID_STRIDE(c, nc) cell_rmass_kappa<double>(int(c % nx), int(c / nx), nx, ny, xi, pen, rm, kK);
 }
 
 __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
@@ -205,6 +198,7 @@ struct topo_ctx {
   double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
   bool trace_solves = false;  // TOPO_TRACE_SOLVES=1: one line per refinement step and inner solve
+  bool verify_residual = false;  // TOPO_VERIFY_RESIDUAL=1: confirm FGMRES convergence with a true residual
   // tightest relative tolerance of an FP32 inner solve (TOPO_INNER_FLOOR_STATE / _FILTER)
   double inner_floor_state = 1e-4, inner_floor_filter = 1e-5;
   double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
@@ -319,6 +313,7 @@ bool env_flag(const char* name, bool dflt) {
 
 int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
   C->trace_solves = env_flag("TOPO_TRACE_SOLVES", false);
+  C->verify_residual = env_flag("TOPO_VERIFY_RESIDUAL", false);
   if (const char* e = std::getenv("TOPO_INNER_FLOOR_STATE"))
     C->inner_floor_state = std::max(1e-8, std::min(0.5, std::atof(e)));
   if (const char* e = std::getenv("TOPO_INNER_FLOOR_FILTER"))
@@ -400,6 +395,12 @@ int init_filter(topo_ctx* C, double eps) {
     st = C->fmg64.setup(s);
   }
   if (st) return C->fail(st == -5 ? TOPO_ERR_CUDA : TOPO_ERR_NOT_CONVERGED, "filter multigrid set-up failed (%d)", st);
+  if (C->trace_solves) {
+    const int lc = C->precision == TOPO_PREC_MIXED ? C->fmg32.coarse_cheb_level() : C->fmg64.coarse_cheb_level();
+    const int dg = C->precision == TOPO_PREC_MIXED ? C->fmg32.coarse_cheb_deg : C->fmg64.coarse_cheb_deg;
+    std::fprintf(stderr, "[topo setup] filter hierarchy: %zu levels, coarse Chebyshev at level %d (degree %d)\n",
+                 C->fspec.size(), lc, dg);
+  }
   if (int rc = filter_stencils64(C)) return rc;
   return C->cuda_check("filter set-up");
 }
@@ -478,10 +479,6 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     if (cycle > 0 && beta > 0.9 * prev) break;  // stagnation at the FP64 residual floor
     prev = beta;
     k_scale<double><<<g, kVecThreads, 0, s>>>(r, 1.0 / beta, n);
-    // an inner solve need not go much below what one refinement step can use:
-    // the FP32 operator's arithmetic differs from the FP64 operator's by
-    // ~1e-5..1e-4 relative at smooth fields of high-contrast designs
-    const double inner = std::min(0.1, std::max(inner_floor, 0.3 * rtol * bn / beta));
     double H[m + 1][m] = {};
     double cs[m], sn[m], gv[m + 1] = {};
     gv[0] = beta;
@@ -492,6 +489,11 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       double* vj = W.V + size_t(j) * n;
       double* zj = W.Z + size_t(j) * n;
       k_convert<float, double><<<g, kVecThreads, 0, s>>>(r32, vj, 1.0, n);
+      // the inner solve aims at what is left of the target (|gv[j]| is the
+      // current residual), but need not go much below what one refinement step
+      // can use: the FP32 operator's arithmetic differs from the FP64
+      // operator's by ~1e-5..1e-4 relative at smooth fields of high-contrast designs
+      const double inner = std::min(0.1, std::max(inner_floor, 0.3 * rtol * bn / std::fabs(gv[j])));
       SolveStats is;
       const int rc = mg.pcg_x64(r32, zj, false, inner, maxit, is, s);
       st.iterations += is.iterations;
@@ -557,6 +559,16 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
 #define TOPO_AM(K) k_add_multi<double, double, K><<<g, kVecThreads, 0, s>>>(x, W.Z, n, cf, n)
     TOPO_DISPATCH_COUNT(k, TOPO_AM)
 #undef TOPO_AM
+    // the least-squares residual is the FP64 residual of the updated x up to the
+    // Arnoldi relation's rounding (~1e-11 relative here): accept it without
+    // another operator apply unless asked to verify (TOPO_VERIFY_RESIDUAL=1)
+    if (k > 0 && std::fabs(gv[k]) <= 0.5 * rtol * bn && !C->verify_residual) {
+      st.relres = std::fabs(gv[k]) / bn;
+      if (C->trace_solves)
+        std::fprintf(stderr, "[topo solve] fgmres converged: estimated |r|/|b| %.3e after %d inner iterations\n",
+                     st.relres, st.iterations);
+      return TOPO_OK;
+    }
   }
   apply64(x, W.t, s);
   k_sub<double><<<g, kVecThreads, 0, s>>>(W.V, b, W.t, n);
@@ -585,16 +597,21 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
 int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   const int L = int(C->sspec.size());
   Penal<double> pen = make_penal<double>(C->p, C->pmin, 1);
-  k_kappa_p2<<<C->grid(C->sspec[1].ntri()), kVecThreads, 0, s>>>(C->nx, C->ny, pen, xi, C->skK[1]);
-  C->launches += 2 + (L - 2);
+  const size_t ncell = size_t(C->nx) * C->ny;
+  const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
+  k_cell_rmass_kappa<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64, C->skK[1]);
+  C->launches += 1 + (L - 2);
   for (int l = 2; l < L; ++l) {
     const LevelSpec &F = C->sspec[l - 1], &Cc = C->sspec[l];
     k_coarsen_kappa<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->skK[l - 1], F.nx, F.ny, C->skK[l], Cc.nx, Cc.ny);
   }
   int st;
-  const size_t ncell = size_t(C->nx) * C->ny;
-  const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
-  k_cell_rmass<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64);
+  if (C->trace_solves) {
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStreamSynchronize(s);
+    std::fprintf(stderr, "[topo setup] kappa, FP64 mass (wait)  %.3f ms\n",
+                 std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
   if (C->precision == TOPO_PREC_MIXED) {
     // the r-weighted mass matrices (12 values per cell) evaluated once per
     // design by the FP32 operator's own code and read by it afterwards instead
@@ -702,6 +719,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       if (precision == TOPO_PREC_MIXED) {
         C->smg32.use_graphs = graphs_enabled();
         C->smg32.fp64_solution = true;
+        C->smg32.trace_setup = C->trace_solves;
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);

@@ -69,6 +69,11 @@ struct ElemRefs {
 };
 ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu);
 double p1_elasticity_bound(const ElemRefs& R);
+void p1_helmholtz_bounds(const ElemRefs& R, double t, double& lo, double& hi);
+// Interval [lo, hi] holding the spectrum of Dinv A for P1 levels assembled from
+// t K_e + M_e with t in [tmin, tmax], and the Chebyshev degree reaching a
+// residual reduction tol on it.
+int coarse_cheb_plan(const ElemRefs& R, double tmin, double tmax, double tol, double& lo, double& hi);
 
 // Reduction scratch shared by one stream.
 struct Reducer {
@@ -154,16 +159,24 @@ class MG {
   int cheb_degree = 2;  // the fused smoothing kernels implement degree 2
   double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
   int power_iters = 10;
+  int power_iters_warm = 4;  // level 0 of a P2 hierarchy, started from the previous set-up's vector
   // kernels launched by this object since construction (graph nodes counted per execution)
   long long launches = 0;
   // record the CG loop as a CUDA graph with a device-side WHILE node (default);
   // false runs the same kernels from a host loop
   bool use_graphs = true;
   bool use_tail = true;      // run the smallest levels in the one-CTA shared-memory kernel
+  // stop the V-cycle at the first P1 level whose Jacobi-scaled operator is well
+  // conditioned enough for a short Chebyshev solve (scalar mass+stiffness levels)
+  bool use_coarse_cheb = true;
+  int coarse_cheb_max_degree = 16;
+  int coarse_cheb_level() const { return cheb_coarse_; }
+  int coarse_cheb_deg = 0;
   bool use_p1_march = true;  // large P1 levels: column march (false: node-centric kernels)
   long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;
+  bool trace_setup = false;  // print synchronised set-up phase times to stderr
   std::vector<double> level_ms;
   std::vector<long long> level_calls;
   void flush_level_profile();
@@ -218,6 +231,14 @@ class MG {
   bool graph_valid_ = false;
   void build_tail(Arena& arena);
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events_;
+  // truncated hierarchy: the V-cycle stops at level cheb_coarse_ and solves it
+  // with a fixed-degree Chebyshev iteration in one CTA (CoarseChebDesc, device)
+  int cheb_coarse_ = -1;
+  void* cc_desc_ = nullptr;
+  size_t cc_smem_ = 0;
+  void select_coarse_cheb();
+  void* cc_buf_ = nullptr;
+  bool cc_selected_ = false;
   int tail_ = -1;              // first level run by the one-CTA shared-memory tail kernel
   void* tail_desc_ = nullptr;  // TailDesc<T, NC> (device)
   size_t tail_smem_ = 0;
@@ -231,6 +252,8 @@ class MG {
 
   T* pcg_[kScratch] = {};
   double* xacc_ = nullptr;  // FP64 solution of the CG loop (fp64_solution)
+  T* pw_ = nullptr;         // level-0 power-iteration vector (P2 hierarchies)
+  bool pw_ready_ = false;
   Reducer* red_ = nullptr;
   int sms_ = 148;
 };

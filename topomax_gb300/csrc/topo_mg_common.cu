@@ -151,8 +151,8 @@ ElemRefs make_elem_refs(double hx, double hy, double lmbda, double mu) {
   return R;
 }
 
-// Largest eigenvalue of the symmetric n x n matrix A (cyclic Jacobi rotations).
-static double sym_eig_max(std::vector<double> A, int n) {
+// Eigenvalue range of the symmetric n x n matrix A (cyclic Jacobi rotations).
+static void sym_eig_range(std::vector<double> A, int n, double& lo, double& hi) {
   for (int sweep = 0; sweep < 60; ++sweep) {
     double off = 0.0;
     for (int p = 0; p < n; ++p)
@@ -177,9 +177,17 @@ static double sym_eig_max(std::vector<double> A, int n) {
         }
       }
   }
-  double m = A[0];
-  for (int k = 1; k < n; ++k) m = std::max(m, A[k * n + k]);
-  return m;
+  lo = hi = A[0];
+  for (int k = 1; k < n; ++k) {
+    lo = std::min(lo, A[k * n + k]);
+    hi = std::max(hi, A[k * n + k]);
+  }
+}
+
+static double sym_eig_max(const std::vector<double>& A, int n) {
+  double lo, hi;
+  sym_eig_range(A, n, lo, hi);
+  return hi;
 }
 
 // max over orientations of lambda_max(D_e^-1 K_e) for the unit-coefficient P1
@@ -195,6 +203,45 @@ double p1_elasticity_bound(const ElemRefs& R) {
     m = std::max(m, sym_eig_max(A, 6));
   }
   return m;
+}
+
+// Range of the element eigenvalues of D_e^-1 (t K_e + M_e) over both triangle
+// orientations (P1, Jacobi-scaled): bounds the spectrum of Dinv A of any
+// operator assembled from such elements with coefficient ratio t.
+void p1_helmholtz_bounds(const ElemRefs& R, double t, double& lo, double& hi) {
+  lo = 1e300;
+  hi = 0.0;
+  for (int o = 0; o < 2; ++o) {
+    double E[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) E[i][j] = t * R.K1[o][i][j] + R.M1[o][i][j];
+    std::vector<double> A(9);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) A[i * 3 + j] = E[i][j] / std::sqrt(E[i][i] * E[j][j]);
+    double l, h;
+    sym_eig_range(A, 3, l, h);
+    lo = std::min(lo, l);
+    hi = std::max(hi, h);
+  }
+}
+
+int coarse_cheb_plan(const ElemRefs& R, double tmin, double tmax, double tol, double& lo, double& hi) {
+  lo = 1e300;
+  hi = 0.0;
+  // the element bounds at ratios spread over [tmin, tmax], with margins
+  for (int k = 0; k <= 8; ++k) {
+    const double t = tmin > 0 ? tmin * std::pow(tmax / tmin, k / 8.0) : tmin + (tmax - tmin) * k / 8.0;
+    double a, b;
+    p1_helmholtz_bounds(R, t, a, b);
+    lo = std::min(lo, a);
+    hi = std::max(hi, b);
+  }
+  lo = std::min(0.9 * lo, 1.0);  // clamped rows are identity rows (eigenvalue 1)
+  hi = std::max(1.05 * hi, 1.0);
+  const double kap = hi / lo, q = (std::sqrt(kap) - 1.0) / (std::sqrt(kap) + 1.0);
+  if (!(q > 0.0)) return 1;
+  const int d = int(std::ceil(std::log(0.5 * tol) / std::log(q)));
+  return d < 1 ? 1 : d;
 }
 
 void Reducer::init(Arena& a, int nsms) {

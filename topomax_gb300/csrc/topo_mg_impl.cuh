@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -238,18 +239,19 @@ __global__ void k_power_start(T* x, size_t n) {
 }
 
 // Dense inverse of the coarsest operator (n <= kCoarseMaxDofs), assembled from
-// the FP64 coefficient masters, Gauss-Jordan in shared memory (SPD, no pivoting).
+// the FP64 coefficient masters, Gauss-Jordan (SPD, no pivoting) by ONE warp:
+// lane j owns column j in shared memory, so a step needs no block barrier and
+// one reciprocal of the pivot.
 template <class T, int NC>
-__global__ void k_coarse_inverse(int nx, int ny, Dir dir, ElemRefs R, const double* __restrict__ kK,
-                                 const double* __restrict__ kM, T* __restrict__ inv, int* status) {
+__global__ void __launch_bounds__(32) k_coarse_inverse(int nx, int ny, Dir dir, ElemRefs R,
+                                                       const double* __restrict__ kK, const double* __restrict__ kM,
+                                                       T* __restrict__ inv, int* status) {
   __shared__ double A[kCoarseMaxDofs * kCoarseMaxDofs];
-  __shared__ double f[kCoarseMaxDofs];
-  __shared__ int bad;
   const int NX = nx + 1, NY = ny + 1, n = NX * NY * NC;
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x) A[i] = 0.0;
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  const int j = threadIdx.x;
+  for (int i = j; i < n * n; i += 32) A[i] = 0.0;
+  __syncwarp();
+  if (j == 0) {
     for (int cj = 0; cj < ny; ++cj)
       for (int ci = 0; ci < nx; ++ci)
         for (int o = 0; o < 2; ++o) {
@@ -271,38 +273,45 @@ __global__ void k_coarse_inverse(int nx, int ny, Dir dir, ElemRefs R, const doub
           }
         }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+  __syncwarp();
+  for (int i = j; i < n * n; i += 32) {
     const int r = i / n, c = i % n;
     const int nr = r / NC, nc = c / NC;
     const bool cr = is_clamped(dir, nr % NX, nr / NX), cc = is_clamped(dir, nc % NX, nc / NX);
     if (cr || cc) A[i] = (r == c) ? 1.0 : 0.0;
   }
-  __syncthreads();
+  __syncwarp();
+  int bad = 0;
   for (int k = 0; k < n; ++k) {
     const double p = A[k * n + k];
-    if (!(p > 0.0) || !isfinite(p)) {
-      if (threadIdx.x == 0) bad = 1;
+    if (!(p > 0.0) || !isfinite(p)) {  // the same value in every lane: a uniform exit
+      bad = 1;
       break;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = A[i * n + k];
-    __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x) A[k * n + j] = (j == k) ? 1.0 / p : A[k * n + j] / p;
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-      const int i = idx / n, j = idx % n;
-      if (i == k) continue;
-      if (j == k) A[idx] = -f[i] / p;
-      else A[idx] -= f[i] * A[k * n + j];
+    const double ip = 1.0 / p;
+    double f[kCoarseMaxDofs];  // column k before this step
+#pragma unroll
+    for (int i = 0; i < kCoarseMaxDofs; ++i) f[i] = i < n ? A[i * n + k] : 0.0;
+    __syncwarp();
+    if (j < n) {
+      if (j == k) {
+#pragma unroll
+        for (int i = 0; i < kCoarseMaxDofs; ++i)
+          if (i < n) A[i * n + k] = (i == k) ? ip : -f[i] * ip;
+      } else {
+        const double c = A[k * n + j] * ip;
+#pragma unroll
+        for (int i = 0; i < kCoarseMaxDofs; ++i)
+          if (i < n) A[i * n + j] = (i == k) ? c : A[i * n + j] - f[i] * c;
+      }
     }
-    __syncthreads();
+    __syncwarp();
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+  for (int i = j; i < n * n; i += 32) {
     const int r = i / n, c = i % n;
     inv[i] = T(0.5 * (A[r * n + c] + A[c * n + r]));
   }
-  if (threadIdx.x == 0) *status = bad;
+  if (j == 0) *status = bad;
 }
 
 template <class T>
@@ -451,6 +460,85 @@ __global__ void __launch_bounds__(kTailThreads)
     mark();
   }
   if (trace) trace[kTailTraceSlots - 1] += 1;
+}
+
+template <class T, int NC>
+struct CoarseChebDesc {
+  P1Stencil<T, NC> S;  // the level's stencil (global memory; staged into shared)
+  const T* dinv;
+  int NX, nn;
+  CoarseCheb<T> C;
+};
+
+// The whole Chebyshev solve of a truncated hierarchy's last level in one CTA
+// (scalar levels, at most coarse_cheb_npt<T>() nodes per thread).  A
+// thread keeps its nodes' stencil rows, inverse diagonal, residual and
+// iterate in registers; only the direction, which the neighbours read, goes
+// through shared memory (two buffers, one barrier per step).  A neighbour
+// outside the lattice has a zero coupling, so its index is only clamped into
+// the array.  A step is ~30 instructions per node (the arithmetic of
+// CoarseChebNode::step in the stencil's difference form).
+// nodes per thread: what the registers of a 1024-thread block hold without spilling
+template <class T>
+constexpr int coarse_cheb_npt() {
+  return sizeof(T) == 4 ? 3 : 2;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kTailThreads)
+    k_coarse_cheb(const CoarseChebDesc<T, 1>* __restrict__ D, const T* __restrict__ b, T* __restrict__ x_out) {
+  constexpr int NP = coarse_cheb_npt<T>(), SW = StencilLayout<1>::stride;
+  extern __shared__ __align__(16) unsigned char cc_raw[];
+  T* d0 = reinterpret_cast<T*>(cc_raw);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int nn = D->nn, NX = D->NX;
+  T* d1 = d0 + nn;
+  const CoarseCheb<T>& C = D->C;  // read in place (uniform loads)
+  const T* __restrict__ sg = D->S.s;
+  T st[NP][7], dv[NP], r[NP], x[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const int n = tid + q * nt;
+    const bool on = n < nn;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) st[q][k] = on ? sg[size_t(n) * SW + k] : T(0);
+    dv[q] = on ? D->dinv[n] : T(0);
+    r[q] = on ? b[n] : T(0);
+    x[q] = T(0);
+    if (on) d0[n] = C.c0 * dv[q] * r[q];
+  }
+  __syncthreads();
+  T* dc = d0;
+  T* dn = d1;
+  const int deg = C.deg;
+  for (int k = 0; k + 1 < deg; ++k) {
+    const T c1 = C.c1[k], c2 = C.c2[k];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const int n = tid + q * nt;
+      if (n < nn) {
+        const T dn0 = dc[n];
+        T t = st[q][0] * dn0;
+#pragma unroll
+        for (int e = 1; e < 7; ++e) {
+          const int m = min(max(n + st_da(e) + st_db(e) * NX, 0), nn - 1);
+          t += st[q][e] * (dc[m] - dn0);
+        }
+        x[q] += dn0;
+        r[q] -= t;
+        dn[n] = c1 * dn0 + c2 * dv[q] * r[q];
+      }
+    }
+    __syncthreads();
+    T* tmp = dc;
+    dc = dn;
+    dn = tmp;
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const int n = tid + q * nt;
+    if (n < nn) x_out[n] = x[q] + dc[n];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -699,6 +787,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   const size_t n0 = specs[0].ndof();
   for (int k = 0; k < kScratch; ++k) pcg_[k] = arena.alloc_n<T>(n0);
   if (fp64_solution) xacc_ = arena.alloc_n<double>(n0);
+  if (specs[0].p2) pw_ = arena.alloc_n<T>(n0);  // power-iteration vector kept between set-ups
   const int nc = int(specs.back().ndof());
   cinv_ = arena.alloc_n<T>(size_t(nc) * nc);
   cstat_ = arena.alloc_n<int>(1);
@@ -709,6 +798,73 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
     if (!c) cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
   graph_valid_ = false;
   build_tail(arena);
+  cc_buf_ = arena.alloc(sizeof(CoarseChebDesc<T, 1>));
+}
+
+// Picks the truncation level (see CoarseCheb): the finest level l >= 1 with a
+// scalar assembled stencil that fits one CTA's shared memory and whose Dinv A
+// spectrum -- bounded element by element from the coefficient ratios kK/kM
+// of the level's triangles -- needs at most coarse_cheb_max_degree steps for
+// a residual reduction of 1e-2.  Levels past it are no longer visited.
+template <class T>
+void MG<T>::select_coarse_cheb() {
+  const int prev = cheb_coarse_;
+  cheb_coarse_ = -1;
+  cc_desc_ = nullptr;
+  coarse_cheb_deg = 0;
+  const int L = levels();
+  for (int l = 1; use_coarse_cheb && cc_buf_ && l < L; ++l) {
+    const LevelSpec& S = specs_[l];
+    if (S.p2 || S.NC != 1 || !lv_[l].st || !kK64_[l] || !kM64_[l]) continue;
+    const size_t smem = 2 * S.nn() * sizeof(T);  // the two direction buffers
+    if (S.nn() > size_t(kTailThreads) * coarse_cheb_npt<T>() || smem > kTailSmemBudget) continue;
+    const size_t nt = S.ntri();
+    std::vector<double> kk(nt), km(nt);
+    if (cudaMemcpy(kk.data(), kK64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(km.data(), kM64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    double tmin = 1e300, tmax = 0.0;
+    bool ok = nt > 0;
+    for (size_t t = 0; t < nt && ok; ++t) {
+      if (!(km[t] > 0.0) || !(kk[t] >= 0.0) || !std::isfinite(kk[t] / km[t])) ok = false;
+      else {
+        tmin = std::min(tmin, kk[t] / km[t]);
+        tmax = std::max(tmax, kk[t] / km[t]);
+      }
+    }
+    if (!ok) continue;
+    double lo, hi;
+    const int deg = coarse_cheb_plan(refs_[l], tmin, tmax, 1e-2, lo, hi);
+    if (deg > coarse_cheb_max_degree || deg > kCoarseChebMax) continue;
+    CoarseChebDesc<T, 1> h;
+    std::memset(&h, 0, sizeof(h));
+    h.S = P1Stencil<T, 1>{S.nx, S.ny, S.dir, lv_[l].st};
+    h.dinv = lv_[l].dinv;
+    h.NX = S.NX;
+    h.nn = int(S.nn());
+    double c0, c1[kCoarseChebMax], c2[kCoarseChebMax];
+    coarse_cheb_coefficients(lo, hi, deg, c0, c1, c2);
+    h.C.deg = deg;
+    h.C.c0 = T(c0);
+    for (int k = 0; k + 1 < deg; ++k) {
+      h.C.c1[k] = T(c1[k]);
+      h.C.c2[k] = T(c2[k]);
+    }
+    const int limit = int(kTailSmemBudget);
+    if (cudaMemcpy(cc_buf_, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaFuncSetAttribute(k_coarse_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    cheb_coarse_ = l;
+    cc_desc_ = cc_buf_;
+    cc_smem_ = smem;
+    coarse_cheb_deg = deg;
+    break;
+  }
+  if (cheb_coarse_ != prev) graph_valid_ = false;
 }
 
 // Chooses the tail levels (smallest levels whose shared vectors fit the
@@ -849,38 +1005,60 @@ double MG<T>::dot(const T* a, const T* b, size_t n, cudaStream_t s) {
   return red_->host[0];
 }
 
+// Power iteration for lambda_max(D^-1 A) on level l (Rayleigh quotient
+// x'Ax / x'Dx).  On the state hierarchy's level 0 the iterate is kept between
+// set-ups: consecutive designs differ little, so a warm start needs fewer
+// steps.  Normalisation happens on the device; one host read at the end.
 template <class T>
 double MG<T>::estimate_lmax(int l, cudaStream_t s) {
   const size_t n = specs_[l].ndof();
   const int g = vec_grid(n, sms_);
   Lev& v = lv_[l];
-  T* x = v.r;
+  const bool keep = (l == 0 && pw_);
+  T* x = keep ? pw_ : v.r;
   T* y = v.d;
-  k_power_start<T><<<g, kVecThreads, 0, s>>>(x, n);
-  for (int it = 0; it < power_iters; ++it) {
+  const bool warm = keep && pw_ready_;
+  const int iters = warm ? power_iters_warm : power_iters;
+  if (!warm) {
+    k_power_start<T><<<g, kVecThreads, 0, s>>>(x, n);
+    launches += 1;
+  }
+  for (int it = 0; it < iters; ++it) {
     apply(l, x, y, s);
     k_mul<T><<<g, kVecThreads, 0, s>>>(x, v.dinv, y, n);
     launches += 1;
-    if (it % 4 == 3) {  // rescale to stay in range
-      const double nrm = std::sqrt(dot(x, x, n, s));
-      if (!(nrm > 0) || !std::isfinite(nrm)) return 4.0;
-      k_scale<T><<<g, kVecThreads, 0, s>>>(x, T(1.0 / nrm), n);
-      launches += 1;
+    if (it % 4 == 3 || it + 1 == iters) {  // rescale to unit length (on the device)
+      k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(x, x, n, red_->partials, red_->counter, red_->out);
+      k_scale_unit<T><<<g, kVecThreads, 0, s>>>(x, red_->out, n);
+      launches += 2;
     }
   }
   apply(l, x, y, s);
-  const double num = dot(x, y, n, s);
   k_mul<T><<<g, kVecThreads, 0, s>>>(v.t, v.diag, x, n);
+  k_dot2<T><<<red_->blocks, kVecThreads, 0, s>>>(x, y, x, v.t, n, red_->partials, red_->counter, red_->out);
   launches += 2;
-  const double den = dot(x, v.t, n, s);
+  cudaMemcpyAsync(red_->host, red_->out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double num = red_->host[0], den = red_->host[1];
   double lam = (den > 0) ? num / den : 4.0;
-  if (!std::isfinite(lam) || lam <= 0) lam = 4.0;
+  const bool ok = std::isfinite(lam) && lam > 0;
+  if (!ok) lam = 4.0;
+  if (keep) pw_ready_ = ok;  // a failed estimate restarts from the fixed start vector
   return lam;
 }
 
 template <class T>
 int MG<T>::setup(cudaStream_t s) {
   const int L = levels();
+  auto t_last = std::chrono::steady_clock::now();
+  auto mark = [&](const char* what) {  // trace_setup: synchronised phase times
+    if (!trace_setup) return;
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[topo setup] %-22s %.3f ms\n", what, std::chrono::duration<double, std::milli>(now - t_last).count());
+    t_last = now;
+  };
+  mark("(queued before)");
   for (int l = 0; l < L; ++l) {
     const LevelSpec& S = specs_[l];
     Lev& v = lv_[l];
@@ -898,13 +1076,18 @@ int MG<T>::setup(cudaStream_t s) {
     }
   }
   stencils_ready_ = true;
+  mark("coefficients, stencils");
   for (int l = 0; l < L; ++l) {
     const size_t n = specs_[l].ndof();
     const int g = vec_grid(n, sms_);
     diag_of(l, lv_[l].diag, s);
-    k_convert<T, T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, lv_[l].diag, 1.0, n);
-    k_recip<T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, n);
-    launches += 2;
+    k_inverse<T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, lv_[l].diag, n);
+    launches += 1;
+  }
+  mark("diagonals");
+  if (!cc_selected_) {  // the coefficient ratios of a hierarchy with a mass term do not change
+    select_coarse_cheb();
+    cc_selected_ = true;
   }
   std::vector<double> cc(8 * L, 0.0);
   for (int l = 0; l + 1 < L; ++l) {
@@ -930,18 +1113,20 @@ int MG<T>::setup(cudaStream_t s) {
   }
   // stored in the levels' precision: the kernels use them without conversion
   // (an FP64 load and convert per node costs FP64-pipe time on this GPU)
+  mark("eigenvalue bounds");
   cheb_host_.assign(cc.begin(), cc.end());
   cudaMemcpyAsync(cheb_, cheb_host_.data(), cheb_host_.size() * sizeof(T), cudaMemcpyHostToDevice, s);
   const LevelSpec& C = specs_[L - 1];
   if (C.NC == 2)
-    k_coarse_inverse<T, 2><<<1, 256, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
+    k_coarse_inverse<T, 2><<<1, 32, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
   else
-    k_coarse_inverse<T, 1><<<1, 256, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], kM64_[L - 1], cinv_,
+    k_coarse_inverse<T, 1><<<1, 32, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], kM64_[L - 1], cinv_,
                                              cstat_);
   launches += 1;
   int st = 0;
   cudaMemcpyAsync(&st, cstat_, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamSynchronize(s);
+  mark("coarse inverse");
   if (e != cudaSuccess) return -5;
   return st ? -2 : 0;
 }
@@ -998,6 +1183,11 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   Lev& v = lv_[l];
   const int L = levels();
   const LevelSpec& S = specs_[l];
+  if (l == cheb_coarse_ && cc_desc_) {
+    k_coarse_cheb<T><<<1, kTailThreads, cc_smem_, s>>>(static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
+    ++launches;
+    return;
+  }
   if (l == tail_ && tail_desc_ && use_tail) {
     if (S.NC == 2)
       k_tail_vcycle<T, 2><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);

@@ -10,6 +10,8 @@
 // as zero).
 #pragma once
 
+#include <cmath>
+
 #include "topo_common.cuh"
 
 namespace topo {
@@ -436,6 +438,71 @@ struct P1Smooth {
       const T r1 = B.r[i] - t[c];
       B.x[i] = B.x2[i] + c1 * B.d[i] + c2 * B.dinv[i] * r1;
     }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Chebyshev iteration as the coarse solver of a truncated hierarchy
+// ---------------------------------------------------------------------------
+// Where a level's operator is well conditioned in the Jacobi metric (the
+// filter's eps^2 K + M once the mesh width passes eps: mass-dominated), the
+// V-cycle stops there and solves it with a fixed-degree Chebyshev iteration
+// from x = 0 (Saad, Iterative Methods for Sparse Linear Systems, Alg. 12.1):
+//   d_0 = c0 Dinv b ;  x_(k+1) = x_k + d_k ;  r_(k+1) = r_k - A d_k ;
+//   d_(k+1) = c1_k d_k + c2_k Dinv r_(k+1)
+// The result is p(Dinv A) Dinv b for a fixed polynomial p: a symmetric positive
+// definite preconditioner when [lo, hi] holds the spectrum of Dinv A.
+constexpr int kCoarseChebMax = 16;
+
+template <class T>
+struct CoarseCheb {
+  int deg;                  // polynomial degree (deg - 1 operator applications)
+  T c0;                     // 1 / theta
+  T c1[kCoarseChebMax], c2[kCoarseChebMax];
+};
+
+// host: the coefficients for the interval [lo, hi]
+inline void coarse_cheb_coefficients(double lo, double hi, int deg, double& c0, double* c1, double* c2) {
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  c0 = 1.0 / theta;
+  double rho = 1.0 / sigma;
+  for (int k = 1; k < deg; ++k) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    c1[k - 1] = rn * rho;
+    c2[k - 1] = 2.0 * rn / delta;
+    rho = rn;
+  }
+}
+
+template <class T, int NC>
+struct CoarseChebNode {
+  // r = b, x = 0, d = c0 Dinv b
+  TOPO_HD static void init(size_t n, const CoarseCheb<T>& C, const T* b, const T* dinv, T* r, T* x, T* d) {
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      r[i] = b[i];
+      x[i] = T(0);
+      d[i] = C.c0 * dinv[i] * b[i];
+    }
+  }
+  // step k: x += d ; r -= A d ; dn = c1_k d + c2_k Dinv r   (reads d around the node)
+  template <class PP>
+  TOPO_HD static void step(int a, int b, int k, const PP& P, const CoarseCheb<T>& C, const T* dinv, const T* d, T* r,
+                           T* x, T* dn) {
+    const size_t n = size_t(b) * (P.nx + 1) + a;
+    T t[NC];
+    if (!p1_node_eval<T, NC>(a, b, P, FetchArray<T, NC>{d}, t))
+      for (int c = 0; c < NC; ++c) t[c] = d[NC * n + c];
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      x[i] += d[i];
+      const T rn = r[i] - t[c];
+      r[i] = rn;
+      dn[i] = C.c1[k] * d[i] + C.c2[k] * dinv[i] * rn;
+    }
+  }
+  TOPO_HD static void finish(size_t n, const T* d, const T* x, T* out) {
+    for (int c = 0; c < NC; ++c) out[NC * n + c] = x[NC * n + c] + d[NC * n + c];
   }
 };
 

@@ -552,6 +552,40 @@ TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<
   }
 }
 
+// Both per-design FP64 coefficient sets of a cell in one pass over the
+// quadrature points: the r-weighted mass matrices of the operator (r as given)
+// and kappa_T of the P1 levels (r clamped at pmin, the preconditioner's
+// coefficient).  Same arithmetic, term by term, as cell_rmass and tri_kappa.
+template <class T>
+TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const Penal<T>& pen, T* rm, T* kK) {
+  const size_t nc = size_t(nx) * ny, c = size_t(j) * nx + i;
+  const int VX = nx + 1;
+  for (int o = 0; o < 2; ++o) {
+    T xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
+    T M[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    T kap = T(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int q = 0; q < Rule7::n; ++q) {
+      const T l0 = T(Rule7::lam(q, 0)), l1 = T(Rule7::lam(q, 1)), l2 = T(Rule7::lam(q, 2));
+      const T x = l0 * xe[0] + l1 * xe[1] + l2 * xe[2];
+      const T r = pen.r(x);
+      const T wr = T(Rule7::w(q)) * r;
+      M[0] += wr * (l0 * l0);
+      M[1] += wr * (l1 * l1);
+      M[2] += wr * (l2 * l2);
+      M[3] += wr * (l0 * l1);
+      M[4] += wr * (l0 * l2);
+      M[5] += wr * (l1 * l2);
+      kap += T(Rule7::w(q)) * (r >= pen.pmin ? r : pen.pmin);
+    }
+    for (int k = 0; k < 6; ++k) rm[(size_t(o) * 6 + k) * nc + c] = M[k];
+    kK[c * 2 + o] = kap;
+  }
+}
+
 // kappa_T = (1/|T|) int_T r(xi) with the 7-point rule: the Galerkin P1
 // coefficient of the P2 operator (P1 strains are constant per triangle).
 template <class T>

@@ -65,6 +65,24 @@ __global__ void k_recip(T* __restrict__ x, size_t n) {
   TOPO_GRID_STRIDE(i, n) x[i] = T(1) / x[i];
 }
 
+template <class T>
+__global__ void k_inverse(T* __restrict__ y, const T* __restrict__ x, size_t n) {
+  TOPO_GRID_STRIDE(i, n) y[i] = T(1) / x[i];
+}
+
+// x /= sqrt(*nrm2) (nrm2 = x.x on the device; left unchanged when not positive)
+template <class T>
+__global__ void k_scale_unit(T* __restrict__ x, const double* __restrict__ nrm2, size_t n) {
+  __shared__ T a_s;
+  if (threadIdx.x == 0) {
+    const double q = *nrm2;
+    a_s = (q > 0.0 && isfinite(q)) ? T(1.0 / sqrt(q)) : T(1);
+  }
+  __syncthreads();
+  const T a = a_s;
+  TOPO_GRID_STRIDE(i, n) x[i] *= a;
+}
+
 // Chebyshev smoother pieces (preconditioner Dinv).  The coefficients live in
 // device memory (coef[0] = 1/theta, coef[2k-1], coef[2k] = step-k weights) so a
 // captured graph stays valid when a new set-up changes the eigenvalue bounds.
