@@ -22,6 +22,21 @@
 #define TOPO_HD inline
 #endif
 
+// Programmatic dependent launch.  Kernels of the solve chain start with
+// TOPO_PDL_ENTRY(): they wait for their predecessor's results (a no-op when
+// launched without the programmatic attribute), then allow their own
+// successor to be scheduled; the successor launches once every block of this
+// grid has passed that point and overlaps its launch with this grid's drain.
+#if defined(__CUDA_ARCH__)
+#define TOPO_PDL_ENTRY()                                 \
+  do {                                                   \
+    asm volatile("griddepcontrol.wait;" ::: "memory");   \
+    asm volatile("griddepcontrol.launch_dependents;" :::); \
+  } while (0)
+#else
+#define TOPO_PDL_ENTRY() ((void)0)
+#endif
+
 namespace topo {
 
 constexpr int kMaxDirPoints = 32;

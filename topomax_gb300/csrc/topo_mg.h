@@ -223,7 +223,8 @@ class MG {
   std::vector<T> cheb_host_;
   PcgDev* dev_ = nullptr;   // device scalars of the graph solve
   PcgDev* hdev_ = nullptr;  // pinned mirror
-  cudaStream_t cap_[2] = {nullptr, nullptr};  // owned streams: graph recording only
+  cudaStream_t cap_[2] = {nullptr, nullptr};  // owned streams: graph recording, concurrent set-up
+  cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};  // set-up fork/join
   struct Graph {
     cudaGraphExec_t exec = nullptr;
     long long prologue_nodes = 0, body_nodes = 0;

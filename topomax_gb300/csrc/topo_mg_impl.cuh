@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
+#include <utility>
 
 #include "topo_mg.h"
 #include "topo_p1.cuh"
@@ -93,6 +94,7 @@ __device__ inline void pcg_check_dev(PcgDev* dv, cudaGraphConditionalHandle h, i
 template <class T, int MODE>
 __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
+  TOPO_PDL_ENTRY();
   io.mode = MODE;  // compile-time mode: the per-node switches fold
   constexpr bool OPERAND = MODE != kP2Diag;
   const int lane = threadIdx.x & 31;
@@ -140,6 +142,7 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
 // The column-march kernel of the large P1 levels (see P1March).
 template <class T, int NC, int MODE>
 __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1Io<T> io, int seg) {
+  TOPO_PDL_ENTRY();
   io.mode = MODE;
   const int lane = threadIdx.x & 31;
   const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
@@ -186,6 +189,7 @@ __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1I
 
 template <class T, int NC, int MODE, class PP>
 __global__ void __launch_bounds__(kRowThreads_) k_p1_smooth(PP P, SmoothBufs<T> B) {
+  TOPO_PDL_ENTRY();
   const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
   if (a > P.nx) return;
   if (MODE == kP2Pre) P1Smooth<T, NC>::pre(a, b, P, B);
@@ -196,12 +200,14 @@ __global__ void __launch_bounds__(kRowThreads_) k_p1_smooth(PP P, SmoothBufs<T> 
 
 template <class T, int NC>
 __global__ void __launch_bounds__(kRowThreads_) k_prolong_add(Transfer X, const T* __restrict__ xc, T* __restrict__ xf) {
+  TOPO_PDL_ENTRY();
   const int a = blockIdx.x * kRowThreads_ + threadIdx.x, b = blockIdx.y;
   if (a < X.NXf) TransferKern<T, NC>::node_prolong_add(a, b, X, xc, xf);
 }
 
 template <class T, int NC, class PP>
 __global__ void __launch_bounds__(kRowThreads) k_p1_apply(PP P, const T* __restrict__ u, T* __restrict__ y) {
+  TOPO_PDL_ENTRY();
   const int a = blockIdx.x * kRowThreads + threadIdx.x, b = blockIdx.y;
   if (a <= P.nx) p1_node_apply<T, NC>(a, b, P, u, y);
 }
@@ -221,6 +227,7 @@ __global__ void __launch_bounds__(kRowThreads) k_p1_stencil(P1Params<T, NC> P, T
 template <class T, int NC>
 __global__ void __launch_bounds__(kRowThreads) k_restrict(Transfer X, const T* __restrict__ rf, T* __restrict__ bc,
                                                           const T* __restrict__ tf) {
+  TOPO_PDL_ENTRY();
   const int I = blockIdx.x * kRowThreads + threadIdx.x, J = blockIdx.y;
   if (I < X.NXc) TransferKern<T, NC>::node_restrict(I, J, X, rf, bc, tf);
 }
@@ -316,6 +323,7 @@ __global__ void __launch_bounds__(32) k_coarse_inverse(int nx, int ny, Dir dir, 
 
 template <class T>
 __global__ void k_dense_matvec(const T* __restrict__ Ainv, const T* __restrict__ b, T* __restrict__ x, int n) {
+  TOPO_PDL_ENTRY();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     T s = T(0);
     for (int j = 0; j < n; ++j) s += Ainv[size_t(i) * n + j] * b[j];
@@ -354,6 +362,7 @@ struct TailDesc {
 template <class T, int NC>
 __global__ void __launch_bounds__(kTailThreads)
     k_tail_vcycle(const TailDesc<T, NC>* __restrict__ D, const T* __restrict__ b_in, T* __restrict__ x_out) {
+  TOPO_PDL_ENTRY();
   __shared__ TailLevel<T, NC> lv[kTailMaxLevels];
   __shared__ T cinv[kCoarseMaxDofs * kCoarseMaxDofs];
   extern __shared__ __align__(16) unsigned char tail_raw[];
@@ -487,6 +496,7 @@ constexpr int coarse_cheb_npt() {
 template <class T>
 __global__ void __launch_bounds__(kTailThreads)
     k_coarse_cheb(const CoarseChebDesc<T, 1>* __restrict__ D, const T* __restrict__ b, T* __restrict__ x_out) {
+  TOPO_PDL_ENTRY();
   constexpr int NP = coarse_cheb_npt<T>(), SW = StencilLayout<1>::stride;
   extern __shared__ __align__(16) unsigned char cc_raw[];
   T* d0 = reinterpret_cast<T*>(cc_raw);
@@ -557,6 +567,33 @@ inline int device_sms() {
   return cached[dev];
 }
 
+// Kernels of the solve chain are launched with programmatic stream
+// serialization (they begin with TOPO_PDL_ENTRY): a launch overlaps the
+// predecessor's drain instead of following its completion.  TOPO_PDL=0
+// launches them plainly.
+inline bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("TOPO_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <class... KP, class... A>
+inline void launch_pdl(void (*k)(KP...), dim3 g, dim3 b, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 // resident blocks per SM of a march kernel at P2M_THREADS threads (its
 // registers decide: the grid is sized to one wave of them)
 template <class K>
@@ -612,7 +649,7 @@ template <class T, int MODE>
 inline void launch_p2_mode(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
   int seg = 0;
   const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<T, MODE>(), seg);
-  k_p2_march<T, MODE><<<g, P2M_THREADS, 0, s>>>(P, xi, io, seg);
+  launch_pdl(k_p2_march<T, MODE>, g, P2M_THREADS, 0, s, P, xi, io, seg);
 }
 
 template <class T>
@@ -631,7 +668,7 @@ template <class T, int NC, int MODE>
 inline void launch_p1_mode(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
   int seg = 0;
   const dim3 g = march_grid(P.nx, P.ny, p1_march_bps<T, NC, MODE>(), seg);
-  k_p1_march<T, NC, MODE><<<g, P2M_THREADS, 0, s>>>(P, io, seg);
+  launch_pdl(k_p1_march<T, NC, MODE>, g, P2M_THREADS, 0, s, P, io, seg);
 }
 
 template <class T, int NC>
@@ -695,6 +732,7 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 template <class T, class TX>
 __global__ void k_pcg_xr(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
                          const PcgDev* __restrict__ dv, size_t n) {
+  TOPO_PDL_ENTRY();
   __shared__ T alpha_s;
   __shared__ bool ok_s;
   if (threadIdx.x == 0) {
@@ -714,6 +752,7 @@ __global__ void k_pcg_xr(TX* __restrict__ x, T* __restrict__ r, const T* __restr
 // p = z + beta p
 template <class T>
 __global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, const PcgDev* __restrict__ dv, size_t n) {
+  TOPO_PDL_ENTRY();
   __shared__ T beta_s;
   if (threadIdx.x == 0) beta_s = T(dv->beta);
   __syncthreads();
@@ -724,6 +763,7 @@ __global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, const PcgDev
 // after the prologue: decide whether the loop runs at all.  On entry dv->tol2
 // holds rtol^2 and dv->maxit the iteration cap (both written by the host).
 static __global__ void k_pcg_start(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
+  TOPO_PDL_ENTRY();
   const double bb = dv->bb, rr = dv->rr;
   dv->tol2 = dv->tol2 * bb;
   dv->it = 0;
@@ -738,6 +778,7 @@ static __global__ void k_pcg_start(PcgDev* dv, cudaGraphConditionalHandle h, int
 
 // end of one iteration: convergence / cap / breakdown test and beta
 static __global__ void k_pcg_check(PcgDev* dv, cudaGraphConditionalHandle h, int use_cond) {
+  TOPO_PDL_ENTRY();
   pcg_check_dev(dv, h, use_cond);
 }
 
@@ -750,6 +791,8 @@ MG<T>::~MG() {
     if (g.exec) cudaGraphExecDestroy(g.exec);
   for (auto c : cap_)
     if (c) cudaStreamDestroy(c);
+  for (auto e : ev_)
+    if (e) cudaEventDestroy(e);
   if (hdev_) cudaFreeHost(hdev_);
 }
 
@@ -796,6 +839,8 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   if (!hdev_) cudaMallocHost(&hdev_, sizeof(PcgDev));
   for (auto& c : cap_)
     if (!c) cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
+  for (auto& e : ev_)
+    if (!e) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   graph_valid_ = false;
   build_tail(arena);
   cc_buf_ = arena.alloc(sizeof(CoarseChebDesc<T, 1>));
@@ -951,7 +996,7 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   const Lev& v = lv_[l];
   if (L.NC == 2) {
     if (v.st && stencils_ready_) {
-      k_p1_apply<T, 2><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st}, x, y);
+      launch_pdl(k_p1_apply<T, 2, P1Stencil<T, 2>>, g, kRowThreads, 0, s, P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st}, x, y);
     } else {
       P1Io<T> io;
       std::memset(&io, 0, sizeof(io));
@@ -962,7 +1007,7 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
     }
   } else {
     if (v.st && stencils_ready_) {
-      k_p1_apply<T, 1><<<g, kRowThreads, 0, s>>>(P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st}, x, y);
+      launch_pdl(k_p1_apply<T, 1, P1Stencil<T, 1>>, g, kRowThreads, 0, s, P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st}, x, y);
     } else {
       P1Io<T> io;
       std::memset(&io, 0, sizeof(io));
@@ -1059,38 +1104,50 @@ int MG<T>::setup(cudaStream_t s) {
     t_last = now;
   };
   mark("(queued before)");
-  for (int l = 0; l < L; ++l) {
+  // Three independent chains once the coefficient masters (written on s) are
+  // ready: level 0's diagonal and eigenvalue estimate on s (the only user of
+  // the shared reduction scratch); the P1 levels' coefficients, stencils and
+  // diagonals on one owned stream; the coarsest inverse (one warp, long
+  // latency) on the other.  s waits for both before it reads levels >= 1.
+  cudaStream_t side = cap_[1], side2 = cap_[0];
+  cudaEventRecord(ev_[0], s);
+  cudaStreamWaitEvent(side, ev_[0], 0);
+  cudaStreamWaitEvent(side2, ev_[0], 0);
+  auto prep = [&](int l, cudaStream_t q) {
     const LevelSpec& S = specs_[l];
     Lev& v = lv_[l];
     if (!S.p2) {
       const int g = vec_grid(S.ntri(), sms_);
-      k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kK, kK64_[l], 1.0, S.ntri());
-      if (v.kM) k_convert<T, double><<<g, kVecThreads, 0, s>>>(v.kM, kM64_[l], 1.0, S.ntri());
+      k_convert<T, double><<<g, kVecThreads, 0, q>>>(v.kK, kK64_[l], 1.0, S.ntri());
+      if (v.kM) k_convert<T, double><<<g, kVecThreads, 0, q>>>(v.kM, kM64_[l], 1.0, S.ntri());
       launches += v.kM ? 2 : 1;
       if (v.st) {
         const dim3 gr = row_grid(S.NX, S.NY);
-        if (S.NC == 2) k_p1_stencil<T, 2><<<gr, kRowThreads, 0, s>>>(make_p1<T, 2>(S, refs_[l], v.kK, nullptr), v.st);
-        else k_p1_stencil<T, 1><<<gr, kRowThreads, 0, s>>>(make_p1<T, 1>(S, refs_[l], v.kK, v.kM), v.st);
+        if (S.NC == 2) k_p1_stencil<T, 2><<<gr, kRowThreads, 0, q>>>(make_p1<T, 2>(S, refs_[l], v.kK, nullptr), v.st);
+        else k_p1_stencil<T, 1><<<gr, kRowThreads, 0, q>>>(make_p1<T, 1>(S, refs_[l], v.kK, v.kM), v.st);
         launches += 1;
       }
     }
-  }
-  stencils_ready_ = true;
-  mark("coefficients, stencils");
-  for (int l = 0; l < L; ++l) {
-    const size_t n = specs_[l].ndof();
-    const int g = vec_grid(n, sms_);
-    diag_of(l, lv_[l].diag, s);
-    k_inverse<T><<<g, kVecThreads, 0, s>>>(lv_[l].dinv, lv_[l].diag, n);
+    stencils_ready_ = true;  // the operator of level l is chosen at launch time
+    const size_t n = S.ndof();
+    diag_of(l, v.diag, q);
+    k_inverse<T><<<vec_grid(n, sms_), kVecThreads, 0, q>>>(v.dinv, v.diag, n);
     launches += 1;
-  }
-  mark("diagonals");
-  if (!cc_selected_) {  // the coefficient ratios of a hierarchy with a mass term do not change
-    select_coarse_cheb();
-    cc_selected_ = true;
-  }
+  };
+  const LevelSpec& C = specs_[L - 1];
+  if (C.NC == 2)
+    k_coarse_inverse<T, 2><<<1, 32, 0, side2>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
+  else
+    k_coarse_inverse<T, 1><<<1, 32, 0, side2>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], kM64_[L - 1], cinv_,
+                                                cstat_);
+  launches += 1;
+  cudaEventRecord(ev_[2], side2);
+  for (int l = 1; l < L; ++l) prep(l, side);
+  cudaEventRecord(ev_[1], side);
+  prep(0, s);
+  mark("level 0 diagonal");
   std::vector<double> cc(8 * L, 0.0);
-  for (int l = 0; l + 1 < L; ++l) {
+  auto bounds = [&](int l) {
     const LevelSpec& S = specs_[l];
     if (!S.p2 && S.NC == 2) {
       lv_[l].lmax = p1_elasticity_bound(refs_[l]);
@@ -1110,19 +1167,22 @@ int MG<T>::setup(cudaStream_t s) {
       c[2 * k] = 2.0 * rho_new / delta;
       rho_old = rho_new;
     }
+  };
+  if (L > 1) bounds(0);
+  mark("level 0 eigenvalue bound");
+  cudaStreamWaitEvent(s, ev_[1], 0);
+  if (!cc_selected_) {  // the coefficient ratios of a hierarchy with a mass term do not change
+    cudaStreamSynchronize(s);
+    select_coarse_cheb();
+    cc_selected_ = true;
   }
+  for (int l = 1; l + 1 < L; ++l) bounds(l);
+  mark("levels >= 1 (side stream)");
   // stored in the levels' precision: the kernels use them without conversion
   // (an FP64 load and convert per node costs FP64-pipe time on this GPU)
-  mark("eigenvalue bounds");
   cheb_host_.assign(cc.begin(), cc.end());
   cudaMemcpyAsync(cheb_, cheb_host_.data(), cheb_host_.size() * sizeof(T), cudaMemcpyHostToDevice, s);
-  const LevelSpec& C = specs_[L - 1];
-  if (C.NC == 2)
-    k_coarse_inverse<T, 2><<<1, 32, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], nullptr, cinv_, cstat_);
-  else
-    k_coarse_inverse<T, 1><<<1, 32, 0, s>>>(C.nx, C.ny, C.dir, refs_[L - 1], kK64_[L - 1], kM64_[L - 1], cinv_,
-                                             cstat_);
-  launches += 1;
+  cudaStreamWaitEvent(s, ev_[2], 0);
   int st = 0;
   cudaMemcpyAsync(&st, cstat_, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamSynchronize(s);
@@ -1184,20 +1244,20 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   const int L = levels();
   const LevelSpec& S = specs_[l];
   if (l == cheb_coarse_ && cc_desc_) {
-    k_coarse_cheb<T><<<1, kTailThreads, cc_smem_, s>>>(static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
+    launch_pdl(k_coarse_cheb<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
     ++launches;
     return;
   }
   if (l == tail_ && tail_desc_ && use_tail) {
     if (S.NC == 2)
-      k_tail_vcycle<T, 2><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);
+      launch_pdl(k_tail_vcycle<T, 2>, 1, kTailThreads, tail_smem_, s, static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);
     else
-      k_tail_vcycle<T, 1><<<1, kTailThreads, tail_smem_, s>>>(static_cast<const TailDesc<T, 1>*>(tail_desc_), b, x);
+      launch_pdl(k_tail_vcycle<T, 1>, 1, kTailThreads, tail_smem_, s, static_cast<const TailDesc<T, 1>*>(tail_desc_), b, x);
     ++launches;
     return;
   }
   if (l == L - 1) {
-    k_dense_matvec<T><<<1, 256, 0, s>>>(cinv_, b, x, int(S.ndof()));
+    launch_pdl(k_dense_matvec<T>, 1, 256, 0, s, static_cast<const T*>(cinv_), b, x, int(S.ndof()));
     ++launches;
     return;
   }
@@ -1214,7 +1274,7 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Res;
     launch_p2_tile<T>(p2_, xi_, io, s);
-    k_restrict<T, 2><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launch_pdl(k_restrict<T, 2>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
     io.mode = kP2First;  // adds the prolonged coarse correction to its operand on the fly
@@ -1237,14 +1297,14 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   auto run = [&](auto nc_tag, const auto& P) {
     constexpr int NC = decltype(nc_tag)::value;
     using PP = std::decay_t<decltype(P)>;
-    k_p1_smooth<T, NC, kP2Pre, PP><<<gf, kRowThreads, 0, s>>>(P, B);
-    k_p1_smooth<T, NC, kP2Res, PP><<<gf, kRowThreads, 0, s>>>(P, B);
-    k_restrict<T, NC><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launch_pdl(k_p1_smooth<T, NC, kP2Pre, PP>, gf, kRowThreads, 0, s, P, B);
+    launch_pdl(k_p1_smooth<T, NC, kP2Res, PP>, gf, kRowThreads, 0, s, P, B);
+    launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    k_prolong_add<T, NC><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
-    k_p1_smooth<T, NC, kP2First, PP><<<gf, kRowThreads, 0, s>>>(P, B);
-    k_p1_smooth<T, NC, kP2Post2, PP><<<gf, kRowThreads, 0, s>>>(P, B);
+    launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x);
+    launch_pdl(k_p1_smooth<T, NC, kP2First, PP>, gf, kRowThreads, 0, s, P, B);
+    launch_pdl(k_p1_smooth<T, NC, kP2Post2, PP>, gf, kRowThreads, 0, s, P, B);
     launches += 3;
   };
   // large levels without a stencil: the column march (element products per cell)
@@ -1258,10 +1318,10 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     launch_p1_march<T, NC>(P, io, s);
     io.mode = kP2Res;
     launch_p1_march<T, NC>(P, io, s);
-    k_restrict<T, NC><<<gc, kRowThreads, 0, s>>>(X, v.r, c.b, nullptr);
+    launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    k_prolong_add<T, NC><<<gf, kRowThreads, 0, s>>>(X, c.x, x);
+    launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x);
     io.mode = kP2First;
     launch_p1_march<T, NC>(P, io, s);
     io.mode = kP2Post2;
@@ -1322,8 +1382,9 @@ template <class T>
 void MG<T>::pcg_xr(int g, cudaStream_t s) {
   const size_t n = specs_[0].ndof();
   T *r = pcg_[0], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
-  if (xacc_) k_pcg_xr<T, double><<<g, kVecThreads, 0, s>>>(xacc_, r, p, q, dev_, n);
-  else k_pcg_xr<T, T><<<g, kVecThreads, 0, s>>>(xi, r, p, q, dev_, n);
+  const PcgDev* dv = dev_;
+  if (xacc_) launch_pdl(k_pcg_xr<T, double>, g, kVecThreads, 0, s, xacc_, r, static_cast<const T*>(p), static_cast<const T*>(q), dv, n);
+  else launch_pdl(k_pcg_xr<T, T>, g, kVecThreads, 0, s, xi, r, static_cast<const T*>(p), static_cast<const T*>(q), dv, n);
 }
 
 template <class T>
@@ -1355,17 +1416,19 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
     fuse_use_cond_ = use_cond;
     vcycle(r, z, s);
     fuse_rz_ = false;
-    k_pcg_p<T><<<g, kVecThreads, 0, s>>>(p, z, dev_, n);
+    launch_pdl(k_pcg_p<T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), static_cast<const PcgDev*>(dev_), n);
     launches += 3;
     return;
   }
   apply(0, p, q, s, true);
-  k_dot<T, T><<<red_->blocks, kVecThreads, 0, s>>>(p, q, n, red_->partials, red_->counter, &dev_->pq);
+  launch_pdl(k_dot<T, T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(p), static_cast<const T*>(q), n,
+             red_->partials, red_->counter, &dev_->pq);
   pcg_xr(g, s);
   vcycle(r, z, s);
-  k_dot2<T><<<red_->blocks, kVecThreads, 0, s>>>(r, r, r, z, n, red_->partials, red_->counter, &dev_->rr);
-  k_pcg_check<<<1, 1, 0, s>>>(dev_, h, use_cond);
-  k_pcg_p<T><<<g, kVecThreads, 0, s>>>(p, z, dev_, n);
+  launch_pdl(k_dot2<T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(r), static_cast<const T*>(r),
+             static_cast<const T*>(r), static_cast<const T*>(z), n, red_->partials, red_->counter, &dev_->rr);
+  launch_pdl(k_pcg_check, 1, 1, 0, s, dev_, h, use_cond);
+  launch_pdl(k_pcg_p<T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), static_cast<const PcgDev*>(dev_), n);
   launches += 5;
 }
 

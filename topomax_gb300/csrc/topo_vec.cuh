@@ -21,58 +21,58 @@ inline int vec_grid(size_t n, int sms) {
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (n); i += size_t(gridDim.x) * blockDim.x)
 
 template <class T>
-__global__ void k_fill(T* x, T v, size_t n) { TOPO_GRID_STRIDE(i, n) x[i] = v; }
+__global__ void k_fill(T* x, T v, size_t n) { TOPO_PDL_ENTRY(); TOPO_GRID_STRIDE(i, n) x[i] = v; }
 
 template <class TD, class TS>
-__global__ void k_convert(TD* __restrict__ d, const TS* __restrict__ s, double scale, size_t n) {
+__global__ void k_convert(TD* __restrict__ d, const TS* __restrict__ s, double scale, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) d[i] = TD(double(s[i]) * scale);
 }
 
 // y += a x
 template <class T>
-__global__ void k_axpy(T* __restrict__ y, T a, const T* __restrict__ x, size_t n) {
+__global__ void k_axpy(T* __restrict__ y, T a, const T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) y[i] += a * x[i];
 }
 
 // p = z + b p
 template <class T>
-__global__ void k_xpby(T* __restrict__ p, const T* __restrict__ z, T b, size_t n) {
+__global__ void k_xpby(T* __restrict__ p, const T* __restrict__ z, T b, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) p[i] = z[i] + b * p[i];
 }
 
 // r = b - y
 template <class T>
-__global__ void k_sub(T* __restrict__ r, const T* __restrict__ b, const T* __restrict__ y, size_t n) {
+__global__ void k_sub(T* __restrict__ r, const T* __restrict__ b, const T* __restrict__ y, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) r[i] = b[i] - y[i];
 }
 
 // u += s * d  (d in lower precision)
 template <class TU, class TD>
-__global__ void k_add_scaled(TU* __restrict__ u, double s, const TD* __restrict__ d, size_t n) {
+__global__ void k_add_scaled(TU* __restrict__ u, double s, const TD* __restrict__ d, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) u[i] += TU(s * double(d[i]));
 }
 
 template <class T>
-__global__ void k_mul(T* __restrict__ y, const T* __restrict__ a, const T* __restrict__ x, size_t n) {
+__global__ void k_mul(T* __restrict__ y, const T* __restrict__ a, const T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) y[i] = a[i] * x[i];
 }
 
 template <class T>
-__global__ void k_scale(T* __restrict__ x, T a, size_t n) { TOPO_GRID_STRIDE(i, n) x[i] *= a; }
+__global__ void k_scale(T* __restrict__ x, T a, size_t n) { TOPO_PDL_ENTRY(); TOPO_GRID_STRIDE(i, n) x[i] *= a; }
 
 template <class T>
-__global__ void k_recip(T* __restrict__ x, size_t n) {
+__global__ void k_recip(T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) x[i] = T(1) / x[i];
 }
 
 template <class T>
-__global__ void k_inverse(T* __restrict__ y, const T* __restrict__ x, size_t n) {
+__global__ void k_inverse(T* __restrict__ y, const T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) y[i] = T(1) / x[i];
 }
 
 // x /= sqrt(*nrm2) (nrm2 = x.x on the device; left unchanged when not positive)
 template <class T>
-__global__ void k_scale_unit(T* __restrict__ x, const double* __restrict__ nrm2, size_t n) {
+__global__ void k_scale_unit(T* __restrict__ x, const double* __restrict__ nrm2, size_t n) { TOPO_PDL_ENTRY();
   __shared__ T a_s;
   if (threadIdx.x == 0) {
     const double q = *nrm2;
@@ -91,7 +91,7 @@ __global__ void k_scale_unit(T* __restrict__ x, const double* __restrict__ nrm2,
 template <class T>
 __global__ void k_cheb_first(const T* __restrict__ b, const T* __restrict__ t, T* __restrict__ r,
                              const T* __restrict__ dinv, T* __restrict__ d, T* __restrict__ x,
-                             const double* __restrict__ coef, size_t n) {
+                             const double* __restrict__ coef, size_t n) { TOPO_PDL_ENTRY();
   const T c0 = T(coef[0]);
   TOPO_GRID_STRIDE(i, n) {
     const T ri = t ? b[i] - t[i] : b[i];
@@ -104,7 +104,7 @@ __global__ void k_cheb_first(const T* __restrict__ b, const T* __restrict__ t, T
 // later steps: r -= t ; d = c1 d + c2 Dinv r ; x += d
 template <class T>
 __global__ void k_cheb_next(T* __restrict__ r, const T* __restrict__ t, const T* __restrict__ dinv,
-                            T* __restrict__ d, T* __restrict__ x, const double* __restrict__ coef, size_t n) {
+                            T* __restrict__ d, T* __restrict__ x, const double* __restrict__ coef, size_t n) { TOPO_PDL_ENTRY();
   const T c1 = T(coef[0]), c2 = T(coef[1]);
   TOPO_GRID_STRIDE(i, n) {
     const T ri = r[i] - t[i];
@@ -175,7 +175,7 @@ __device__ bool finish_reduction(const R (&v)[NV], double* partials, unsigned* c
 // out[0] = sum a_i b_i (or sum a_i^2 when b == nullptr)
 template <class TA, class TB>
 __global__ void k_dot(const TA* __restrict__ a, const TB* __restrict__ b, size_t n, double* partials,
-                      unsigned* counter, double* out) {
+                      unsigned* counter, double* out) { TOPO_PDL_ENTRY();
   // per-thread partial in the input precision (a handful of terms), then FP64
   using Acc = typename std::conditional<sizeof(TA) == 4 && sizeof(TB) == 4, float, double>::type;
   Acc acc = Acc(0);
@@ -189,7 +189,7 @@ __global__ void k_dot(const TA* __restrict__ a, const TB* __restrict__ b, size_t
 template <class T>
 __global__ void k_dot2(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
                        const T* __restrict__ d, size_t n, double* partials, unsigned* counter,
-                       double* out) {
+                       double* out) { TOPO_PDL_ENTRY();
   // per-thread partials in the input precision (a handful of terms), then FP64
   T p0 = T(0), p1 = T(0);
   TOPO_GRID_STRIDE(i, n) {
@@ -213,7 +213,7 @@ struct MultiCoef {
 
 template <class TV, class TW, int C>
 __global__ void k_multidot(const TV* __restrict__ V, size_t stride, const TW* __restrict__ w, size_t n,
-                           double* partials, unsigned* counter, double* out) {
+                           double* partials, unsigned* counter, double* out) { TOPO_PDL_ENTRY();
   double v[C + 1];
 #pragma unroll
   for (int k = 0; k <= C; ++k) v[k] = 0.0;
@@ -230,7 +230,7 @@ __global__ void k_multidot(const TV* __restrict__ V, size_t stride, const TW* __
 
 // w -= sum_k c_k V_k
 template <class TV, class TW, int C>
-__global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t stride, MultiCoef c, size_t n) {
+__global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t stride, MultiCoef c, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) {
     double s = double(w[i]);
 #pragma unroll
@@ -241,7 +241,7 @@ __global__ void k_sub_multi(TW* __restrict__ w, const TV* __restrict__ V, size_t
 
 // x += sum_k c_k Z_k
 template <class TZ, class TX, int C>
-__global__ void k_add_multi(TX* __restrict__ x, const TZ* __restrict__ Z, size_t stride, MultiCoef c, size_t n) {
+__global__ void k_add_multi(TX* __restrict__ x, const TZ* __restrict__ Z, size_t stride, MultiCoef c, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) {
     double s = double(x[i]);
 #pragma unroll
