@@ -118,7 +118,8 @@ int topo_filter_solve(topo_ctx* ctx, const double* b, double* xi, double rtol, i
 
 /* u = K(xi)^-1 f: replaces ElasticityProblem.forward / SmartMumpsSolver.solve
  * (FEM_src/elasisity_problem.py:168-169, FEM_src/pde_solver.py:106-133).
- * flags: TOPO_SOLVE_WARM uses u as the initial guess. */
+ * flags: TOPO_SOLVE_WARM uses u as the initial guess.  u must be 16-byte aligned
+ * (TOPO_ERR_ARG otherwise): the kernels access a node's two components at once. */
 int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, int flags, int* iters,
                      topo_stream_t stream);
 
@@ -151,7 +152,7 @@ int topo_emd_finish(topo_ctx* ctx, const double* psi, const double* psi_prev, do
 int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t stream);
 
 /* y = K(xi) u in FP64 with clamped rows/columns as identity (test hook: the operator of
- * FEM_src/elasisity_problem.py:104-132 after bc.apply). */
+ * FEM_src/elasisity_problem.py:104-132 after bc.apply).  u and y 16-byte aligned. */
 int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y, topo_stream_t stream);
 
 /* Measurement hook (no counterpart in the reference): *ms = duration of ONE launch of the

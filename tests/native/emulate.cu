@@ -46,7 +46,8 @@ void dir_to(const Dir& r, int* d) {
 // Runs the column-march P2 kernel on the CPU: the 32 lanes of a warp execute
 // each phase in turn and the shuffles become copies between lane states.
 template <class T>
-void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0) {
+void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
+  P2March<T>::prepare(io);
   if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   const bool operand = io.mode != kP2Diag;
@@ -82,11 +83,15 @@ void p2_run_io(const P2Params<T>& P, const T* xi, const P2Io<T>& io, int seg = 0
         const bool more = j + 1 < je;
         if (more)
           for (int l = 0; l < 32; ++l) P2March<T>::prefetch(P, io, xi, L[l], j + 1, N[l]);
+        std::vector<typename P2March<T>::Fin> F(32);
+        if (j >= js)
+          for (int l = 1; l < 32; ++l)
+            if (L[l].i <= P.nx) P2March<T>::fin_load(P, io, L[l], j, F[l]);
         for (int l = 0; l < 32; ++l) P2March<T>::compute(P, L[l], j, io.mode);
         up();
         if (j >= js)
           for (int l = 1; l < 32; ++l)
-            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, acc);
+            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, F[l], acc);
         if (!more) break;
         ++j;
         for (int l = 0; l < 32; ++l) {

@@ -4,6 +4,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -637,6 +638,11 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   return TOPO_OK;
 }
 
+// P2-lattice arrays are read and written two components at a time (16-byte
+// accesses in FP64): their base must be 16-byte aligned (cudaMalloc and torch
+// allocations are; a view at an odd element offset is not)
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 template <class F>
 int guarded(topo_ctx* C, F&& f) {
   if (!C) return TOPO_ERR_ARG;
@@ -832,6 +838,7 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
     if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
     if (!xi || !u || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid state-solve arguments");
+    if (!aligned16(u)) return ctx->fail(TOPO_ERR_ARG, "displacement array must be 16-byte aligned");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const auto t0 = std::chrono::steady_clock::now();
     int rc = state_setup(ctx, xi, s);
@@ -1018,6 +1025,7 @@ int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y
     if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
     if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
     if (!xi || !u || !y) return ctx->fail(TOPO_ERR_ARG, "invalid apply arguments");
+    if (!aligned16(u) || !aligned16(y)) return ctx->fail(TOPO_ERR_ARG, "displacement arrays must be 16-byte aligned");
     p2_apply_f64(ctx->p2params<double>(), xi, u, y, reinterpret_cast<cudaStream_t>(stream));
     return ctx->cuda_check("apply");
   });

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
   TOPO_PDL_ENTRY();
   io.mode = MODE;  // compile-time mode: the per-node switches fold
+  P2March<T>::prepare(io);
   constexpr bool OPERAND = MODE != kP2Diag;
   const int lane = threadIdx.x & 31;
   const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
@@ -113,9 +114,12 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     for (;;) {
       const bool more = j + 1 < je;
       if (more) P2March<T>::prefetch(P, io, xi, L, j + 1, N);  // in flight during this step's arithmetic
+      const bool fin = owner && j >= js;
+      typename P2March<T>::Fin F;
+      if (MODE != kP2Apply && MODE != kP2Diag && fin) P2March<T>::fin_load(P, io, L, j, F);
       P2March<T>::compute(P, L, j, MODE);
       p2m_exchange_up<T>(L, lane);
-      if (owner && j >= js) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2, acc);
+      if (fin) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2, F, acc);
       if (!more) break;
       ++j;
       P2March<T>::advance(L);

@@ -18,6 +18,37 @@
 
 namespace topo {
 
+// The two displacement components of a node (and the smoothing vectors' pair
+// at a node) are adjacent: one 8-byte (FP32) or 16-byte (FP64) access.
+template <class T>
+TOPO_HD void ld2(const T* p, T (&v)[2]) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(T) == 4) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+    const double2 t = *reinterpret_cast<const double2*>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+  }
+#else
+  v[0] = p[0];
+  v[1] = p[1];
+#endif
+}
+
+template <class T>
+TOPO_HD void st2(T* p, T a, T b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(T) == 4) *reinterpret_cast<float2*>(p) = make_float2(a, b);
+  else *reinterpret_cast<double2*>(p) = make_double2(a, b);
+#else
+  p[0] = a;
+  p[1] = b;
+#endif
+}
+
 template <class T>
 struct P2Params {
   int nx, ny;     // cells
@@ -25,8 +56,9 @@ struct P2Params {
   T lamT, mu2T;   // lambda*|T|, 2*mu*|T|
   Penal<T> pen;
   Dir dir;        // on the (2nx+1)x(2ny+1) node lattice
-  // optional precomputed r-weighted mass matrices, layout [o][k][cell] with
-  // cell = j*nx + i and k over [00,11,22,01,02,12] (null: evaluate r(xi) on the fly)
+  // optional precomputed r-weighted mass matrices, 12 consecutive values per
+  // cell (cell = j*nx + i): [o][k], k over [00,11,22,01,02,12] (null: evaluate
+  // r(xi) on the fly).  48 B (FP32) / 96 B (FP64) per cell: 16-byte vector loads.
   const T* rmass;
 };
 
@@ -229,6 +261,7 @@ struct P2Io {
   PcgDev* pcg;         // CG scalars
   unsigned long long cond;  // graph conditional handle of the CG loop
   int use_cond;
+  T cf[3];             // B.cheb[0..2], copied in by P2March::prepare (registers, not re-read)
 };
 
 template <class T>
@@ -252,22 +285,29 @@ struct P2Next {
 
 template <class T>
 struct P2March {
+  // once per launch, before any phase: the smoothing coefficients by value
+  TOPO_HD static void prepare(P2Io<T>& io) {
+    const bool smooth = io.mode == kP2Pre || io.mode == kP2First || io.mode == kP2Post2;
+    for (int k = 0; k < 3; ++k) io.cf[k] = (smooth && io.B.cheb) ? io.B.cheb[k] : T(0);
+  }
+
   // operand of the apply at node n for the launch's mode
   TOPO_HD static void operand(const P2Io<T>& io, size_t n, T (&v)[2]) {
     switch (io.mode) {
       case kP2Pre: {
-        const T c0 = io.B.cheb[0];
-        v[0] = c0 * io.B.dinv[2 * n] * io.B.b[2 * n];
-        v[1] = c0 * io.B.dinv[2 * n + 1] * io.B.b[2 * n + 1];
+        const T c0 = io.cf[0];
+        T dv[2], bv[2];
+        ld2(io.B.dinv + 2 * n, dv);
+        ld2(io.B.b + 2 * n, bv);
+        v[0] = c0 * dv[0] * bv[0];
+        v[1] = c0 * dv[1] * bv[1];
         break;
       }
       case kP2Post2:
-        v[0] = io.B.d[2 * n];
-        v[1] = io.B.d[2 * n + 1];
+        ld2(io.B.d + 2 * n, v);
         break;
       default:
-        v[0] = io.u[2 * n];
-        v[1] = io.u[2 * n + 1];
+        ld2(io.u + 2 * n, v);
     }
   }
 
@@ -277,10 +317,17 @@ struct P2March {
     const int NXc = P.nx + 1;
     const int pa = a & 1, pb = b & 1, I0 = a >> 1, J0 = b >> 1;
     const size_t m0 = size_t(J0) * NXc + I0;
-    const size_t m1 = size_t(J0 + pb) * NXc + I0 + pa;
-    for (int c = 0; c < 2; ++c) {
-      const T x00 = xc[2 * m0 + c];
-      v[c] += (pa | pb) ? T(0.5) * (x00 + xc[2 * m1 + c]) : x00;
+    T x0[2];
+    ld2(xc + 2 * m0, x0);
+    if (pa | pb) {
+      const size_t m1 = size_t(J0 + pb) * NXc + I0 + pa;
+      T x1[2];
+      ld2(xc + 2 * m1, x1);
+      v[0] += T(0.5) * (x0[0] + x1[0]);
+      v[1] += T(0.5) * (x0[1] + x1[1]);
+    } else {
+      v[0] += x0[0];
+      v[1] += x0[1];
     }
   }
 
@@ -370,11 +417,34 @@ struct P2March {
   TOPO_HD static void load_mass(const P2Params<T>& P, int i, int j, T (&M)[12]) {
     if (!P.rmass) return;
     const bool in = i >= 0 && i < P.nx && j >= 0 && j < P.ny;
-    const size_t nc = size_t(P.nx) * P.ny, c = in ? size_t(j) * P.nx + i : 0;
+    if (!in) {
+      for (int k = 0; k < 12; ++k) M[k] = T(0);
+      return;
+    }
+    const T* src = P.rmass + (size_t(j) * P.nx + i) * 12;
 #if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 4) {
+      const float4* q = reinterpret_cast<const float4*>(src);
 #pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float4 t = q[k];
+        M[4 * k] = t.x;
+        M[4 * k + 1] = t.y;
+        M[4 * k + 2] = t.z;
+        M[4 * k + 3] = t.w;
+      }
+    } else {
+      const double2* q = reinterpret_cast<const double2*>(src);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double2 t = q[k];
+        M[2 * k] = t.x;
+        M[2 * k + 1] = t.y;
+      }
+    }
+#else
+    for (int k = 0; k < 12; ++k) M[k] = src[k];
 #endif
-    for (int k = 0; k < 12; ++k) M[k] = in ? P.rmass[size_t(k) * nc + c] : T(0);
   }
 
   // the loads of step j (operand rows 1, 2, density row 1, mass matrices)
@@ -414,14 +484,65 @@ struct P2March {
   }
 
   // finish node (a,b) with the complete sum r (clamped rows act as identity rows)
+  // The finish phase's per-node vectors of step j (rows 0, 1 of the lane's
+  // nodes), loaded before the step's arithmetic so that it hides their latency:
+  //   Pre, First: b, Dinv   Res: b   Post2: w, Dinv (+ b for the fused r.r, r.z)
+  struct Fin {
+    T v[4][3][2];
+  };
+  TOPO_HD static void fin_load(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, Fin& F) {
+    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+    const SmoothBufs<T>& B = io.B;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int q = 0; q < 4; ++q) {
+      const int a = 2 * L.i + (q & 1), b = 2 * j + (q >> 1);
+      if (a < 0 || a >= NX || b >= NY) continue;
+      const size_t i = 2 * (size_t(b) * NX + a);
+      switch (io.mode) {
+        case kP2Pre:
+        case kP2First:
+          ld2(B.b + i, F.v[q][0]);
+          ld2(B.dinv + i, F.v[q][1]);
+          break;
+        case kP2Res: ld2(B.b + i, F.v[q][0]); break;
+        case kP2Post2:
+          ld2(B.x2 + i, F.v[q][0]);
+          ld2(B.dinv + i, F.v[q][1]);
+          if (io.fuse == kFuseRZ) ld2(B.b + i, F.v[q][2]);
+          break;
+        default: break;
+      }
+    }
+  }
+  // the same vectors for one node (row 2 of the last cell row)
+  TOPO_HD static void fin_load_node(const P2Io<T>& io, size_t i, T (&v)[3][2]) {
+    const SmoothBufs<T>& B = io.B;
+    switch (io.mode) {
+      case kP2Pre:
+      case kP2First:
+        ld2(B.b + i, v[0]);
+        ld2(B.dinv + i, v[1]);
+        break;
+      case kP2Res: ld2(B.b + i, v[0]); break;
+      case kP2Post2:
+        ld2(B.x2 + i, v[0]);
+        ld2(B.dinv + i, v[1]);
+        if (io.fuse == kFuseRZ) ld2(B.b + i, v[2]);
+        break;
+      default: break;
+    }
+  }
+
+  // v: the node's finish vectors (Fin)
   TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, const T (&sum)[2],
-                                  const T (&u)[2], T (&acc)[2]) {
+                                  const T (&u)[2], const T (&v)[3][2], T (&acc)[2]) {
     const int NX = 2 * P.nx + 1;
-    const size_t n = size_t(b) * NX + a;
+    const size_t n = size_t(b) * NX + a, i = 2 * n;
     const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
     if (io.mode == kP2Diag) {
-      io.y[2 * n] = cl ? T(1) : sum[0];
-      io.y[2 * n + 1] = cl ? T(1) : sum[1];
+      st2(io.y + i, cl ? T(1) : sum[0], cl ? T(1) : sum[1]);
       return;
     }
     T un[2] = {u[0], u[1]}, r[2] = {sum[0], sum[1]};
@@ -431,36 +552,50 @@ struct P2March {
       r[1] = un[1];
     }
     const SmoothBufs<T>& B = io.B;
-    for (int c = 0; c < 2; ++c) {
-      const size_t i = 2 * n + c;
-      switch (io.mode) {
-        case kP2Apply:
-          io.y[i] = r[c];
-          if (io.fuse == kFusePQ) acc[0] += un[c] * r[c];
-          break;
-        case kP2Pre: {
-          const T rr = B.b[i] - r[c];
-          B.x[i] = un[c] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * rr;
-          break;
+    const T c0 = io.cf[0], c1 = io.cf[1], c2 = io.cf[2];
+    switch (io.mode) {
+      case kP2Apply:
+        st2(io.y + i, r[0], r[1]);
+        if (io.fuse == kFusePQ) {
+          acc[0] += un[0] * r[0];
+          acc[0] += un[1] * r[1];
         }
-        case kP2Res: B.r[i] = B.b[i] - r[c]; break;
-        case kP2First: {
-          const T r0 = B.b[i] - r[c];
-          const T d0 = B.cheb[0] * B.dinv[i] * r0;
-          B.r[i] = r0;
-          B.d[i] = d0;
-          B.x2[i] = un[c] + d0;
-          break;
-        }
-        default: {  // kP2Post2
-          const T r1 = B.r[i] - r[c];
-          const T z = B.x2[i] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
-          B.x[i] = z;
-          if (io.fuse == kFuseRZ) {
-            const T bi = B.b[i];
-            acc[0] += bi * bi;
-            acc[1] += bi * z;
-          }
+        break;
+      case kP2Pre: {
+        const T(&bv)[2] = v[0];
+        const T(&dv)[2] = v[1];
+        const T r0 = bv[0] - r[0], r1 = bv[1] - r[1];
+        st2(B.x + i, un[0] + c1 * un[0] + c2 * dv[0] * r0, un[1] + c1 * un[1] + c2 * dv[1] * r1);
+        break;
+      }
+      case kP2Res: {
+        const T(&bv)[2] = v[0];
+        st2(B.r + i, bv[0] - r[0], bv[1] - r[1]);
+        break;
+      }
+      case kP2First: {
+        // d0 = c0 Dinv r0 and w = x + d0 + c2 Dinv r0 (into x2): the second
+        // step then needs only w, Dinv and A d0 (x = w + c1 d0 - c2 Dinv A d0)
+        const T(&bv)[2] = v[0];
+        const T(&dv)[2] = v[1];
+        const T r0 = bv[0] - r[0], r1 = bv[1] - r[1];
+        const T d0 = c0 * dv[0] * r0, d1 = c0 * dv[1] * r1;
+        st2(B.d + i, d0, d1);
+        st2(B.x2 + i, un[0] + d0 + c2 * dv[0] * r0, un[1] + d1 + c2 * dv[1] * r1);
+        break;
+      }
+      default: {  // kP2Post2
+        const T(&wv)[2] = v[0];
+        const T(&dv)[2] = v[1];
+        const T z0 = wv[0] + c1 * un[0] - c2 * dv[0] * r[0];
+        const T z1 = wv[1] + c1 * un[1] - c2 * dv[1] * r[1];
+        st2(B.x + i, z0, z1);
+        if (io.fuse == kFuseRZ) {
+          const T(&bv)[2] = v[2];
+          acc[0] += bv[0] * bv[0];
+          acc[1] += bv[0] * z0;
+          acc[0] += bv[1] * bv[1];
+          acc[1] += bv[1] * z1;
         }
       }
     }
@@ -470,7 +605,7 @@ struct P2March {
   // acc: the lane's partial sums of the fused reductions, in the operator's
   // precision (a few dozen terms; blocks combine them in FP64)
   TOPO_HD static void finish(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, int nrows,
-                             T (&acc)[2]) {
+                             const Fin& F, T (&acc)[2]) {
     const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
@@ -480,8 +615,17 @@ struct P2March {
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-      for (int c = 0; c < 2; ++c)
-        if (2 * L.i + c < NX) finish_node(P, io, 2 * L.i + c, 2 * j + r, L.A[r][c], L.U[r][c], acc);
+      for (int c = 0; c < 2; ++c) {
+        const int a = 2 * L.i + c, b = 2 * j + r;
+        if (a >= NX) continue;
+        if (r < 2) {
+          finish_node(P, io, a, b, L.A[r][c], L.U[r][c], F.v[2 * r + c], acc);
+        } else {  // row 2: only on the last cell row
+          T v[3][2] = {};
+          fin_load_node(io, 2 * (size_t(b) * NX + a), v);
+          finish_node(P, io, a, b, L.A[r][c], L.U[r][c], v, acc);
+        }
+      }
     }
   }
 
@@ -541,14 +685,14 @@ inline int p2_march_segment(int nx, int ny, int sms, int blocks_per_sm) {
 // r-weighted mass matrices of every triangle, layout [o][k][cell] (P2Params::rmass)
 template <class T, class TC>
 TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<TC>& pen, T* out) {
-  const size_t nc = size_t(nx) * ny, c = size_t(j) * nx + i;
+  const size_t c = size_t(j) * nx + i;
   const int VX = nx + 1;
   for (int o = 0; o < 2; ++o) {
     TC xe[3];
     for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
     TC M[6];
     tri_rmass(xe, pen, M);
-    for (int k = 0; k < 6; ++k) out[(size_t(o) * 6 + k) * nc + c] = T(M[k]);
+    for (int k = 0; k < 6; ++k) out[c * 12 + o * 6 + k] = T(M[k]);
   }
 }
 
@@ -558,7 +702,7 @@ TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<
 // coefficient).  Same arithmetic, term by term, as cell_rmass and tri_kappa.
 template <class T>
 TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const Penal<T>& pen, T* rm, T* kK) {
-  const size_t nc = size_t(nx) * ny, c = size_t(j) * nx + i;
+  const size_t c = size_t(j) * nx + i;
   const int VX = nx + 1;
   for (int o = 0; o < 2; ++o) {
     T xe[3];
@@ -581,7 +725,7 @@ TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const P
       M[5] += wr * (l1 * l2);
       kap += T(Rule7::w(q)) * (r >= pen.pmin ? r : pen.pmin);
     }
-    for (int k = 0; k < 6; ++k) rm[(size_t(o) * 6 + k) * nc + c] = M[k];
+    for (int k = 0; k < 6; ++k) rm[c * 12 + o * 6 + k] = M[k];
     kK[c * 2 + o] = kap;
   }
 }
