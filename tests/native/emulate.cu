@@ -105,7 +105,8 @@ void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
 
 // Runs the P1 column-march kernel on the CPU (lanes in lockstep, shuffles as copies).
 template <class T, int NC>
-void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
+void p1_march_run(const P1Params<T, NC>& P, P1Io<T> io) {
+  P1March<T, NC>::prepare(io);
   const int seg = p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   std::vector<P1Lane<T, NC>> L(32);
@@ -130,13 +131,17 @@ void p1_march_run(const P1Params<T, NC>& P, const P1Io<T>& io) {
         const bool more = j + 1 < je;
         if (more)
           for (int l = 0; l < 32; ++l) P1March<T, NC>::prefetch(P, io, L[l], j + 1, N[l]);
+        std::vector<typename P1March<T, NC>::Fin> F(32);
+        if (j >= js && io.mode != kP2Apply)
+          for (int l = 1; l < 32; ++l)
+            if (L[l].i <= P.nx) P1March<T, NC>::fin_load(P, io, L[l].i, j, F[l]);
         for (int l = 0; l < 32; ++l) P1March<T, NC>::compute(P, L[l], j);
         for (int l = 31; l >= 1; --l)
           for (int r = 0; r < 2; ++r)
             for (int d = 0; d < NC; ++d) L[l].A[r][0][d] += L[l - 1].A[r][1][d];
         if (j >= js)
           for (int l = 1; l < 32; ++l)
-            if (L[l].i <= P.nx) P1March<T, NC>::finish(P, io, L[l], j, j == P.ny - 1 ? 2 : 1);
+            if (L[l].i <= P.nx) P1March<T, NC>::finish(P, io, L[l], j, j == P.ny - 1 ? 2 : 1, F[l]);
         if (!more) break;
         ++j;
         for (int l = 0; l < 32; ++l) {

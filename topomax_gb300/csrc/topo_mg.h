@@ -90,6 +90,7 @@ struct Reducer {
 struct PcgDev {
   double bb, rz, pq, beta, tol2, relres;
   double rr, rz_new;  // adjacent: one two-value reduction writes both
+  double alpha;       // the iteration's step as applied to r (rounded to the CG's precision; 0 on breakdown)
   int it, maxit, status, pad;  // status: 0 converged, 1 running, 2 iteration cap, 3 breakdown, 4 non-finite, 5 zero rhs
 };
 
@@ -193,6 +194,7 @@ class MG {
     T* kK = nullptr;
     T* kM = nullptr;
     T* st = nullptr;  // assembled stencil (levels up to stencil_max_nodes(NC) nodes)
+    T* inner = nullptr;  // the shared interior stencil row (uniform levels; see P1Stencil::inner)
     double lmax = 1.0;
     bool bound = false;  // lmax is a guaranteed upper bound (no safety factor)
   };
@@ -204,7 +206,8 @@ class MG {
   void pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond);
   // x (precision T) or x64 (FP64 solution mode) is the initial guess / result
   int graph_pcg(const T* b, T* x, double* x64, bool warm, double rtol, int maxit, SolveStats& st, cudaStream_t s);
-  void pcg_xr(int g, cudaStream_t s);  // x += alpha p, r -= alpha q
+  void pcg_xr(int g, cudaStream_t s);  // r -= alpha q (alpha recorded for pcg_p)
+  void pcg_p(int g, cudaStream_t s);   // x += alpha p, p = z + beta p
   double dot(const T* a, const T* b, size_t n, cudaStream_t s);  // synchronising
   void diag_of(int l, T* d, cudaStream_t s);
   double estimate_lmax(int l, cudaStream_t s);
@@ -238,7 +241,9 @@ class MG {
   void* cc_desc_ = nullptr;
   size_t cc_smem_ = 0;
   void select_coarse_cheb();
+  void detect_uniform_levels();  // sets Lev::inner where every interior row is the same
   void* cc_buf_ = nullptr;
+  T* inner_buf_ = nullptr;  // per level: one stencil row (detect_uniform_levels)
   bool cc_selected_ = false;
   int tail_ = -1;              // first level run by the one-CTA shared-memory tail kernel
   void* tail_desc_ = nullptr;  // TailDesc<T, NC> (device)

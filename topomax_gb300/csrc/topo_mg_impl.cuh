@@ -148,6 +148,7 @@ template <class T, int NC, int MODE>
 __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1Io<T> io, int seg) {
   TOPO_PDL_ENTRY();
   io.mode = MODE;
+  P1March<T, NC>::prepare(io);
   const int lane = threadIdx.x & 31;
   const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
   if (js >= P.ny) return;  // whole warp
@@ -174,6 +175,9 @@ __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1I
   for (;;) {
     const bool more = j + 1 < je;
     if (more) P1March<T, NC>::prefetch(P, io, L, j + 1, N);  // in flight during this step's arithmetic
+    const bool fin = owner && j >= js;
+    typename P1March<T, NC>::Fin F;
+    if (MODE != kP2Apply && fin) P1March<T, NC>::fin_load(P, io, L.i, j, F);
     P1March<T, NC>::compute(P, L, j);
 #pragma unroll
     for (int r = 0; r < 2; ++r)
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(P2M_THREADS) k_p1_march(P1Params<T, NC> P, P1I
         const T v = shfl_up1(L.A[r][1][d]);
         if (lane > 0) L.A[r][0][d] += v;
       }
-    if (owner && j >= js) P1March<T, NC>::finish(P, io, L, j, j == P.ny - 1 ? 2 : 1);
+    if (fin) P1March<T, NC>::finish(P, io, L, j, j == P.ny - 1 ? 2 : 1, F);
     if (!more) break;
     ++j;
     P1March<T, NC>::advance(L);
@@ -733,9 +737,10 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 // x += alpha p ; r -= alpha q with alpha = rz / pq read from device memory
 // (evaluated once per block: an FP64 division per thread is not free here)
 // x in T or FP64 (TX = double: the product of two FP32 numbers is exact in FP64)
-template <class T, class TX>
-__global__ void k_pcg_xr(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
-                         const PcgDev* __restrict__ dv, size_t n) {
+// r -= alpha q with alpha = rz / pq; block 0 records the alpha it applied
+// (the solution update happens in k_pcg_p, which reads p anyway)
+template <class T>
+__global__ void k_pcg_r(T* __restrict__ r, const T* __restrict__ q, PcgDev* __restrict__ dv, size_t n) {
   TOPO_PDL_ENTRY();
   __shared__ T alpha_s;
   __shared__ bool ok_s;
@@ -743,25 +748,32 @@ __global__ void k_pcg_xr(TX* __restrict__ x, T* __restrict__ r, const T* __restr
     const double pq = dv->pq;
     ok_s = (pq > 0.0) && isfinite(pq);
     alpha_s = ok_s ? T(dv->rz / pq) : T(0);
+    if (blockIdx.x == 0) dv->alpha = double(alpha_s);
   }
   __syncthreads();
   if (!ok_s) return;
   const T alpha = alpha_s;
-  TOPO_GRID_STRIDE(i, n) {
-    x[i] += TX(alpha) * TX(p[i]);
-    r[i] -= alpha * q[i];
-  }
+  TOPO_GRID_STRIDE(i, n) r[i] -= alpha * q[i];
 }
 
-// p = z + beta p
-template <class T>
-__global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, const PcgDev* __restrict__ dv, size_t n) {
+// x += alpha p (x in T or FP64: the product of two FP32 numbers is exact in
+// FP64), then p = z + beta p
+template <class T, class TX>
+__global__ void k_pcg_p(T* __restrict__ p, const T* __restrict__ z, TX* __restrict__ x, const PcgDev* __restrict__ dv,
+                        size_t n) {
   TOPO_PDL_ENTRY();
-  __shared__ T beta_s;
-  if (threadIdx.x == 0) beta_s = T(dv->beta);
+  __shared__ T beta_s, alpha_s;
+  if (threadIdx.x == 0) {
+    beta_s = T(dv->beta);
+    alpha_s = T(dv->alpha);
+  }
   __syncthreads();
-  const T beta = beta_s;
-  TOPO_GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
+  const T beta = beta_s, alpha = alpha_s;
+  TOPO_GRID_STRIDE(i, n) {
+    const T pi = p[i];
+    x[i] += TX(alpha) * TX(pi);
+    p[i] = z[i] + beta * pi;
+  }
 }
 
 // after the prologue: decide whether the loop runs at all.  On entry dv->tol2
@@ -848,6 +860,42 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   graph_valid_ = false;
   build_tail(arena);
   cc_buf_ = arena.alloc(sizeof(CoarseChebDesc<T, 1>));
+  inner_buf_ = arena.alloc_n<T>(specs.size() * StencilLayout<1>::stride);
+}
+
+// Levels with a mass term (the filter), no clamped nodes and the same stencil
+// row at every interior node (constant coefficients on the uniform lattice,
+// checked on the rows themselves) read that row once instead of per node.
+template <class T>
+void MG<T>::detect_uniform_levels() {
+  const int L = levels();
+  for (int l = 0; l < L; ++l) {
+    const LevelSpec& S = specs_[l];
+    Lev& v = lv_[l];
+    v.inner = nullptr;
+    if (S.p2 || S.NC != 1 || !v.st || !kM64_[l] || !inner_buf_) continue;
+    const Dir& d = S.dir;
+    if (d.x_lo || d.y_lo || d.npts || d.x_hi_from < S.NX || d.y_hi_from < S.NY || S.NX < 3 || S.NY < 3) continue;
+    constexpr int SW = StencilLayout<1>::stride;
+    std::vector<T> st(S.nn() * SW);
+    if (cudaMemcpy(st.data(), v.st, st.size() * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    const T* ref = st.data() + (size_t(1) * S.NX + 1) * SW;
+    bool same = true;
+    for (int b = 1; same && b + 1 < S.NY; ++b)
+      for (int a = 1; same && a + 1 < S.NX; ++a)
+        same = std::memcmp(st.data() + (size_t(b) * S.NX + a) * SW, ref, SW * sizeof(T)) == 0;
+    if (!same) continue;
+    T* dst = inner_buf_ + size_t(l) * SW;
+    if (cudaMemcpy(dst, ref, SW * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    v.inner = dst;
+  }
+  graph_valid_ = false;
 }
 
 // Picks the truncation level (see CoarseCheb): the finest level l >= 1 with a
@@ -1000,7 +1048,7 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   const Lev& v = lv_[l];
   if (L.NC == 2) {
     if (v.st && stencils_ready_) {
-      launch_pdl(k_p1_apply<T, 2, P1Stencil<T, 2>>, g, kRowThreads, 0, s, P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st}, x, y);
+      launch_pdl(k_p1_apply<T, 2, P1Stencil<T, 2>>, g, kRowThreads, 0, s, P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st, v.inner}, x, y);
     } else {
       P1Io<T> io;
       std::memset(&io, 0, sizeof(io));
@@ -1011,7 +1059,7 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
     }
   } else {
     if (v.st && stencils_ready_) {
-      launch_pdl(k_p1_apply<T, 1, P1Stencil<T, 1>>, g, kRowThreads, 0, s, P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st}, x, y);
+      launch_pdl(k_p1_apply<T, 1, P1Stencil<T, 1>>, g, kRowThreads, 0, s, P1Stencil<T, 1>{L.nx, L.ny, L.dir, v.st, v.inner}, x, y);
     } else {
       P1Io<T> io;
       std::memset(&io, 0, sizeof(io));
@@ -1175,9 +1223,10 @@ int MG<T>::setup(cudaStream_t s) {
   if (L > 1) bounds(0);
   mark("level 0 eigenvalue bound");
   cudaStreamWaitEvent(s, ev_[1], 0);
-  if (!cc_selected_) {  // the coefficient ratios of a hierarchy with a mass term do not change
+  if (!cc_selected_) {  // the coefficients of a hierarchy with a mass term do not change
     cudaStreamSynchronize(s);
     select_coarse_cheb();
+    detect_uniform_levels();
     cc_selected_ = true;
   }
   for (int l = 1; l + 1 < L; ++l) bounds(l);
@@ -1336,11 +1385,11 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   using I1 = std::integral_constant<int, 1>;
   const bool march = !v.st && use_p1_march;
   if (S.NC == 2) {
-    if (v.st) run(I2{}, P1Stencil<T, 2>{S.nx, S.ny, S.dir, v.st});
+    if (v.st) run(I2{}, P1Stencil<T, 2>{S.nx, S.ny, S.dir, v.st, v.inner});
     else if (march) run_march(I2{}, make_p1<T, 2>(S, refs_[l], v.kK, nullptr));
     else run(I2{}, make_p1<T, 2>(S, refs_[l], v.kK, nullptr));
   } else {
-    if (v.st) run(I1{}, P1Stencil<T, 1>{S.nx, S.ny, S.dir, v.st});
+    if (v.st) run(I1{}, P1Stencil<T, 1>{S.nx, S.ny, S.dir, v.st, v.inner});
     else if (march) run_march(I1{}, make_p1<T, 1>(S, refs_[l], v.kK, v.kM));
     else run(I1{}, make_p1<T, 1>(S, refs_[l], v.kK, v.kM));
   }
@@ -1385,17 +1434,24 @@ void MG<T>::pcg_prologue(bool warm, cudaStream_t s) {
 template <class T>
 void MG<T>::pcg_xr(int g, cudaStream_t s) {
   const size_t n = specs_[0].ndof();
-  T *r = pcg_[0], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  T *r = pcg_[0], *q = pcg_[3];
+  launch_pdl(k_pcg_r<T>, g, kVecThreads, 0, s, r, static_cast<const T*>(q), dev_, n);
+}
+
+template <class T>
+void MG<T>::pcg_p(int g, cudaStream_t s) {
+  const size_t n = specs_[0].ndof();
+  T *z = pcg_[1], *p = pcg_[2], *xi = pcg_[6];
   const PcgDev* dv = dev_;
-  if (xacc_) launch_pdl(k_pcg_xr<T, double>, g, kVecThreads, 0, s, xacc_, r, static_cast<const T*>(p), static_cast<const T*>(q), dv, n);
-  else launch_pdl(k_pcg_xr<T, T>, g, kVecThreads, 0, s, xi, r, static_cast<const T*>(p), static_cast<const T*>(q), dv, n);
+  if (xacc_) launch_pdl(k_pcg_p<T, double>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), xacc_, dv, n);
+  else launch_pdl(k_pcg_p<T, T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), xi, dv, n);
 }
 
 template <class T>
 void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
   const size_t n = specs_[0].ndof();
   const int g = vec_grid(n, sms_);
-  T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3], *xi = pcg_[6];
+  T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3];
   // both fused launches (operator and last post-smoothing) must fit the partial slots
   int seg = 0;
   const dim3 ga = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Apply>(), seg);
@@ -1420,7 +1476,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
     fuse_use_cond_ = use_cond;
     vcycle(r, z, s);
     fuse_rz_ = false;
-    launch_pdl(k_pcg_p<T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), static_cast<const PcgDev*>(dev_), n);
+    pcg_p(g, s);
     launches += 3;
     return;
   }
@@ -1432,7 +1488,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   launch_pdl(k_dot2<T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(r), static_cast<const T*>(r),
              static_cast<const T*>(r), static_cast<const T*>(z), n, red_->partials, red_->counter, &dev_->rr);
   launch_pdl(k_pcg_check, 1, 1, 0, s, dev_, h, use_cond);
-  launch_pdl(k_pcg_p<T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), static_cast<const PcgDev*>(dev_), n);
+  pcg_p(g, s);
   launches += 5;
 }
 

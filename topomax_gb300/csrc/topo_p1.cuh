@@ -253,6 +253,10 @@ struct P1Stencil {
   int nx, ny;  // cells of this level
   Dir dir;
   const T* s;  // node n, block k, row c, column d at s[n*stride + k*NC*NC + c*NC + d]; block 0: row sum
+  // optional: the one stencil row shared by every interior node (a level with
+  // constant coefficients and no clamped nodes, e.g. the filter): interior
+  // nodes read it instead of their own row (null: every node reads its row)
+  const T* inner = nullptr;
 };
 
 // Stencil row of node (a,b) assembled from the level's coefficients (the
@@ -309,7 +313,8 @@ struct P1StencilKern {
     if (!surely_free(P.dir, a, b) && is_clamped(P.dir, a, b)) return false;
     const int NX = P.nx + 1, NY = P.ny + 1;
     const size_t n = size_t(b) * NX + a;
-    const T* sn = P.s + n * StencilLayout<NC>::stride;
+    const bool interior = P.inner && a > 0 && b > 0 && a < NX - 1 && b < NY - 1;
+    const T* sn = interior ? P.inner : P.s + n * StencilLayout<NC>::stride;
     T un[NC];
     fetch(n, a, b, un);
     for (int c = 0; c < NC; ++c)

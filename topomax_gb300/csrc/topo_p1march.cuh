@@ -22,6 +22,7 @@ struct P1Io {
   const T* u;       // Apply / Res / First operand (x)
   T* y;             // Apply output
   SmoothBufs<T> B;  // smoothing modes
+  T cf[3];          // B.cheb[0..2], copied in by P1March::prepare (registers, not re-read)
 };
 
 template <class T, int NC>
@@ -42,11 +43,17 @@ struct P1Next {
 
 template <class T, int NC>
 struct P1March {
+  // once per launch, before any phase: the smoothing coefficients by value
+  TOPO_HD static void prepare(P1Io<T>& io) {
+    const bool smooth = io.mode == kP2Pre || io.mode == kP2First || io.mode == kP2Post2;
+    for (int k = 0; k < 3; ++k) io.cf[k] = (smooth && io.B.cheb) ? io.B.cheb[k] : T(0);
+  }
+
   TOPO_HD static void operand(const P1Io<T>& io, size_t n, T (&v)[NC]) {
     for (int c = 0; c < NC; ++c) {
       const size_t i = NC * n + c;
       switch (io.mode) {
-        case kP2Pre: v[c] = io.B.cheb[0] * io.B.dinv[i] * io.B.b[i]; break;
+        case kP2Pre: v[c] = io.cf[0] * io.B.dinv[i] * io.B.b[i]; break;
         case kP2Post2: v[c] = io.B.d[i]; break;
         default: v[c] = io.u[i];
       }
@@ -130,9 +137,38 @@ struct P1March {
     tri<1>(P, L, j);
   }
 
-  // finish node (a,b) with the complete sum t (clamped rows act as identity rows)
+  // The finish phase's per-node vectors of the lane's row-0 node at step j,
+  // loaded before the step's arithmetic so that it hides their latency:
+  //   Pre, First: b, Dinv   Res: b   Post2: r, x2, Dinv
+  struct Fin {
+    T v[3][NC];
+  };
+  TOPO_HD static void fin_load(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, Fin& F) {
+    const size_t n = size_t(b) * (P.nx + 1) + a;
+    const SmoothBufs<T>& B = io.B;
+    for (int c = 0; c < NC; ++c) {
+      const size_t i = NC * n + c;
+      switch (io.mode) {
+        case kP2Pre:
+        case kP2First:
+          F.v[0][c] = B.b[i];
+          F.v[1][c] = B.dinv[i];
+          break;
+        case kP2Res: F.v[0][c] = B.b[i]; break;
+        case kP2Post2:
+          F.v[0][c] = B.r[i];
+          F.v[1][c] = B.x2[i];
+          F.v[2][c] = B.dinv[i];
+          break;
+        default: break;
+      }
+    }
+  }
+
+  // finish node (a,b) with the complete sum t (clamped rows act as identity rows);
+  // F: the node's finish vectors (fin_load)
   TOPO_HD static void finish_node(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, const T (&sum)[NC],
-                                  const T (&u)[NC]) {
+                                  const T (&u)[NC], const Fin& F) {
     const size_t n = size_t(b) * (P.nx + 1) + a;
     const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
     T un[NC], t[NC];
@@ -150,34 +186,37 @@ struct P1March {
       switch (io.mode) {
         case kP2Apply: io.y[i] = t[c]; break;
         case kP2Pre: {
-          const T r1 = B.b[i] - t[c];
-          B.x[i] = un[c] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
+          const T r1 = F.v[0][c] - t[c];
+          B.x[i] = un[c] + io.cf[1] * un[c] + io.cf[2] * F.v[1][c] * r1;
           break;
         }
-        case kP2Res: B.r[i] = B.b[i] - t[c]; break;
+        case kP2Res: B.r[i] = F.v[0][c] - t[c]; break;
         case kP2First: {
-          const T r0 = B.b[i] - t[c];
-          const T d0 = B.cheb[0] * B.dinv[i] * r0;
+          const T r0 = F.v[0][c] - t[c];
+          const T d0 = io.cf[0] * F.v[1][c] * r0;
           B.r[i] = r0;
           B.d[i] = d0;
           B.x2[i] = un[c] + d0;
           break;
         }
         default: {  // kP2Post2
-          const T r1 = B.r[i] - t[c];
-          B.x[i] = B.x2[i] + B.cheb[1] * un[c] + B.cheb[2] * B.dinv[i] * r1;
+          const T r1 = F.v[0][c] - t[c];
+          B.x[i] = F.v[1][c] + io.cf[1] * un[c] + io.cf[2] * F.v[2][c] * r1;
         }
       }
     }
   }
 
-  // finish the lane's node of row 0 (and of row 1 on the last cell row)
-  TOPO_HD static void finish(const P1Params<T, NC>& P, const P1Io<T>& io, const P1Lane<T, NC>& L, int j, int nrows) {
-#if defined(__CUDA_ARCH__)
-#pragma unroll
-#endif
-    for (int r = 0; r < 2; ++r)
-      if (r < nrows && j + r <= P.ny) finish_node(P, io, L.i, j + r, L.A[r][0], L.U[r][0]);
+  // finish the lane's node of row 0 (F: its preloaded vectors) and, on the
+  // last cell row, of row 1
+  TOPO_HD static void finish(const P1Params<T, NC>& P, const P1Io<T>& io, const P1Lane<T, NC>& L, int j, int nrows,
+                             const Fin& F) {
+    finish_node(P, io, L.i, j, L.A[0][0], L.U[0][0], F);
+    if (nrows > 1 && j + 1 <= P.ny) {
+      Fin F1;
+      fin_load(P, io, L.i, j + 1, F1);
+      finish_node(P, io, L.i, j + 1, L.A[1][0], L.U[1][0], F1);
+    }
   }
 
   // row 1 becomes row 0 of the next step
