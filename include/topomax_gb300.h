@@ -257,6 +257,22 @@ int topo_dem_energy_backward(topo_dem_ctx* ctx, const float* u, const float* den
 int topo_dem_objective_gradient(topo_dem_ctx* ctx, const float* u, const float* density, double* objective,
                                 float* gradient, topo_stream_t stream);
 
+/* ---- DEM density filter: replaces create_density_filter (DEM_src/filter.py:8-31) and
+ * its two uses, W @ rho and W.T @ g (DEM_src/elasisity_problem.py:148, 162, 171). ------
+ * W_ij = (radius - d_ij) / S_i for element points i, j (np.linspace(0, width, Nx) x
+ * np.linspace(0, height, Ny), element i = iy*Nx + ix) within radius, S_i the row sum;
+ * evaluated on the fly in FP64 with the reference's order of operations (bit-identical
+ * to the scipy/sklearn product).  create computes the row sums (synchronises). */
+typedef struct topo_density_filter topo_density_filter;
+topo_density_filter* topo_density_filter_create(int Nx, int Ny, double width, double height, double radius,
+                                                int* status);
+void topo_density_filter_destroy(topo_density_filter* f);
+/* number of stored entries of the reference's sparse W (entries with d_ij <= radius) */
+int topo_density_filter_nnz(const topo_density_filter* f, int64_t* nnz);
+/* y = W x (transpose = 0) or y = W^T x (transpose = 1); device FP64 [Nx*Ny], x != y */
+int topo_density_filter_apply(topo_density_filter* f, const double* x, double* y, int transpose,
+                              topo_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,3 +89,52 @@ def objective_and_gradient(u, rho, Nx, Ny, W, H, young, nu, p):
     rho = np.asarray(rho, float).reshape(Ny, Nx)
     sel = se * detJ
     return float(np.sum((M + rho ** p * (1 - M)) * sel)), -(p * rho ** (p - 1) * (1 - M)) * sel
+
+
+# ---------------------------------------------------------------------------
+# density filter (DEM_src/filter.py:8-31)
+# ---------------------------------------------------------------------------
+
+
+def _linspace(L: float, n: int) -> np.ndarray:
+    return np.linspace(0.0, L, n)
+
+
+def density_filter_rows(Nx: int, Ny: int, W: float, H: float, radius: float):
+    """Row i = iy*Nx + ix: the neighbours j (ascending) with dist <= radius, the weights
+    radius - dist and the row sum, in the reference's order of operations (distances
+    to the element points of np.linspace(0, W, Nx) x np.linspace(0, H, Ny); l1 row
+    normalisation sums the weights in column order and divides each by the sum).
+    Pure-Python loops: small meshes only."""
+    xs, ys = _linspace(W, Nx), _linspace(H, Ny)
+    X = np.tile(xs, Ny)
+    Y = np.repeat(ys, Nx)
+    rows = []
+    for i in range(Nx * Ny):
+        dist = np.sqrt((X - X[i]) ** 2 + (Y - Y[i]) ** 2)
+        (nb,) = np.where(dist <= radius)
+        w = radius - dist[nb]
+        s = 0.0
+        for v in w:
+            s += abs(v)
+        rows.append((nb, w, s))
+    return rows
+
+
+def density_filter_apply(Nx, Ny, W, H, radius, rho, transpose=False):
+    """W @ rho (row sums, then sequential products in column order), or W.T @ g
+    accumulated row by row into the outputs (the CSC product order)."""
+    rows = density_filter_rows(Nx, Ny, W, H, radius)
+    v = np.asarray(rho, dtype=np.float64).ravel()
+    out = np.zeros(Nx * Ny)
+    for i, (nb, w, s) in enumerate(rows):
+        wn = w / s if s != 0.0 else w
+        if not transpose:
+            acc = 0.0
+            for j, c in zip(nb, wn):
+                acc += c * v[j]
+            out[i] = acc
+        else:
+            for j, c in zip(nb, wn):
+                out[j] += c * v[i]
+    return out

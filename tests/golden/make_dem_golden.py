@@ -18,6 +18,13 @@ encoder.  Output: ``tests/golden/dem_energy.npz`` with
 * ``mask*``: ElasticityEnforcer.zero_enforcer (DEM_src/dirichlet_enforcer.py:14-56);
 * ``circle*``: CircleDomain cells and areas (DEM_src/domains.py:56-257);
 * ``side*``: boundary_integral (DEM_src/integrator.py:70-99) of unit node vectors.
+
+and ``tests/golden/dem_density_filter.npz`` with ``filter*``: the reference's
+create_density_filter (DEM_src/filter.py:8-31) applied as ``W @ rho`` and
+``W.T @ g`` (the two uses in DEM_src/elasisity_problem.py:162, 171) to seeded
+vectors, on meshes whose radius spans no neighbour, a few, and an exact
+grid distance.  ``python tests/golden/make_dem_golden.py filter`` writes only
+this file.
 """
 from __future__ import annotations
 
@@ -56,7 +63,46 @@ def _install_stub() -> None:
     sys.path.insert(0, root)
 
 
+FILTER_CASES = [
+    # (Nx, Ny, width, height, radius)
+    (12, 6, 2.0, 1.0, 0.3),
+    (20, 10, 2.0, 1.0, 0.05),   # radius below the spacing: each row is the element itself
+    (11, 5, 2.0, 1.0, 0.4),     # 0.4 is exactly twice the x spacing: weight-0 entries
+    (17, 9, 3.0, 1.0, 0.45),
+    (30, 2, 2.0, 1.0, 0.25),
+]
+
+
+def density_filter_cases() -> None:
+    sys.path.insert(0, REF)
+    from DEM_src.utils import Mesh
+    from DEM_src.filter import create_density_filter
+
+    out = {}
+    rng = np.random.default_rng(5)
+    for k, (Nx, Ny, W, H, r) in enumerate(FILTER_CASES):
+        mesh = Mesh(Nx, Ny, W, H)
+        F = create_density_filter(r, mesh)
+        rho = rng.uniform(0.01, 1.0, (Ny, Nx))
+        g = rng.standard_normal(Nx * Ny)
+        out[f"filter{k}_meta"] = np.array([Nx, Ny, W, H, r])
+        out[f"filter{k}_rho"] = rho
+        out[f"filter{k}_g"] = g
+        out[f"filter{k}_apply"] = F @ rho.flatten()
+        out[f"filter{k}_transpose"] = F.T @ g
+        out[f"filter{k}_nnz"] = np.array(F.nnz)
+    np.savez(os.path.join(HERE, "dem_density_filter.npz"), **out)
+
+
 def main() -> None:
+    if len(sys.argv) > 1 and sys.argv[1] == "filter":
+        density_filter_cases()
+        return
+    energy_cases()
+    density_filter_cases()
+
+
+def energy_cases() -> None:
     import torch
     if not hasattr(np, "trapz"):  # DEM_src/integrator.py uses np.trapz (removed in numpy 2)
         np.trapz = np.trapezoid

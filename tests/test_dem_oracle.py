@@ -118,3 +118,22 @@ def test_quadrature_constants_match_reference_table():
     assert np.allclose(D[3, 3], [0.105662433 * 20, 0.394337567 * 40])
     # partition of unity: the derivatives of the four shape functions sum to zero
     assert np.max(np.abs(D.sum(axis=0))) < 1e-12
+
+
+def test_density_filter_oracle_matches_reference_bitwise():
+    """The oracle's restatement of create_density_filter (DEM_src/filter.py:8-31) applied
+    as W @ rho and W.T @ g equals the reference's scipy products bit for bit (fixtures
+    written by tests/golden/make_dem_golden.py filter)."""
+    d = np.load(os.path.join(GOLDEN, "dem_density_filter.npz"))
+    k = 0
+    while f"filter{k}_meta" in d:
+        Nx, Ny, W, H, r = d[f"filter{k}_meta"]
+        Nx, Ny = int(Nx), int(Ny)
+        a = O.density_filter_apply(Nx, Ny, W, H, r, d[f"filter{k}_rho"])
+        t = O.density_filter_apply(Nx, Ny, W, H, r, d[f"filter{k}_g"], transpose=True)
+        assert np.array_equal(a, d[f"filter{k}_apply"]), k
+        assert np.array_equal(t, d[f"filter{k}_transpose"]), k
+        nnz = sum(len(nb) for nb, _, _ in O.density_filter_rows(Nx, Ny, W, H, r))
+        assert nnz == int(d[f"filter{k}_nnz"]), k
+        k += 1
+    assert k == 5

@@ -150,3 +150,86 @@ def test_network_energy_trains():
         losses.append(float(loss))
     assert all(np.isfinite(losses))
     assert losses[-1] < losses[0]
+
+
+def test_density_filter_matches_reference_bitwise():
+    """create_density_filter on the GPU: W @ rho and W.T @ g equal the reference's scipy
+    products bit for bit, and the stored-entry count matches (DEM_src/filter.py:8-31)."""
+    from topomax_gb300 import dem
+    d = np.load(os.path.join(GOLDEN, "dem_density_filter.npz"))
+    k = 0
+    while f"filter{k}_meta" in d:
+        Nx, Ny, W, H, r = d[f"filter{k}_meta"]
+        mesh = dem.Mesh(int(Nx), int(Ny), W, H)
+        F = dem.create_density_filter(r, mesh)
+        assert F.nnz == int(d[f"filter{k}_nnz"]), k
+        assert np.array_equal(F @ d[f"filter{k}_rho"].flatten(), d[f"filter{k}_apply"]), k
+        assert np.array_equal(F.T @ d[f"filter{k}_g"], d[f"filter{k}_transpose"]), k
+        k += 1
+    assert k == 5
+
+
+def test_density_filter_at_600x300():
+    """The 600x300 DEM workload's filter (radius 0.05 over 180,000 elements): against the
+    oracle on sampled rows, and W.T consistent with W (x . W y == W^T x . y)."""
+    import torch
+    from topomax_gb300 import dem
+    Nx, Ny, W, H, r = 600, 300, 2.0, 1.0, 0.05
+    mesh = dem.Mesh(Nx, Ny, W, H)
+    F = dem.create_density_filter(r, mesh)
+    g = torch.Generator().manual_seed(6)
+    x = torch.rand(Nx * Ny, generator=g, dtype=torch.float64).cuda()
+    y = torch.rand(Nx * Ny, generator=g, dtype=torch.float64).cuda()
+    Wy = F @ y
+    WTx = F.T @ x
+    lhs, rhs = float(x @ Wy), float(WTx @ y)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    # a filter of a constant is the constant (rows sum to one)
+    one = F @ torch.ones(Nx * Ny, dtype=torch.float64, device="cuda")
+    assert float((one - 1).abs().max()) <= 1e-14
+
+
+def test_dem_training_step_and_problem():
+    """The DEM problem of DEM_src/elasisity_problem.py:131-216 end to end on a 40x20
+    cantilever: filter (W of DEM_src/filter.py), L-BFGS training of the network on the
+    fused enforcer + energy kernels (DEM_src/deep_energy_method.py:55-105), objective and
+    gradient mapped back through W^T.  The trained network's energy equals the FP64
+    oracle's energy of the same displacement; the training lowered it."""
+    import torch
+    from topomax_gb300 import dem
+    from topomax_gb300.designs import parse_design_dict
+    dd = {"Elasticity": {
+        "domain_parameters": dict(width=2.0, height=1.0, fem_step_size=0.002, dem_step_size=0.002,
+                                  penalties=[3.0], volume_fraction=0.5),
+        "problem_parameters": dict(fixed_sides=["Left"], body_force=None,
+                                   tractions=[dict(side="Right", center=0.5, length=0.5, value=[0.0, -1.0])],
+                                   filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)}}
+    _, par = parse_design_dict(dd)
+    Nx, Ny = 40, 20
+    mesh = dem.Mesh(Nx, Ny, 2.0, 1.0)
+    torch.manual_seed(2022)
+    prob = dem.ElasticityProblem(mesh, "cuda", False, par)
+    prob.set_penalization(3.0)
+    prob.dem.nn_parameters.iteration_count = 4
+    with pytest.raises(ValueError):
+        prob.calculate_objective_gradient()
+    rho = np.random.default_rng(4).uniform(0.3, 1.0, (Ny, Nx))
+    C = prob.calculate_objective(rho)
+    g = prob.calculate_objective_gradient()
+    assert np.isfinite(C) and C > 0
+    assert g.shape == rho.shape and np.all(np.isfinite(g))
+    losses = prob.dem.loss_array
+    assert len(losses) >= 4 and min(losses) < losses[0]
+    # energy at the trained network: kernel vs FP64 oracle on the same displacement
+    filtered = prob.filter @ rho.flatten()
+    u = prob.dem.get_u(mesh=mesh).detach().double().cpu().numpy()
+    tr = [dem.TractionPoints(mesh, t) for t in par.tractions]
+    wext = dem.external_weights(mesh, None, tr)
+    psi_ref = O.energy(u, filtered, Nx, Ny, 2.0, 1.0, 1.0, 0.3, 3.0, wext)[0]
+    psi = prob.dem.get_loss(filtered, mesh)
+    assert abs(psi - psi_ref) <= 1e-4 * abs(psi_ref)
+    # the objective's gradient is W^T of the per-cell gradient at the trained displacement
+    obj, cell_g = prob.dem.objective_calculator.calculate_objective_and_gradient(
+        prob.dem.get_u(mesh=mesh), mesh.shape, torch.as_tensor(filtered).float().reshape(mesh.intervals).cuda())
+    g_ref = (prob.filter.T @ cell_g.detach().double().cpu().numpy().flatten()).reshape(rho.shape)
+    assert np.array_equal(g, g_ref)

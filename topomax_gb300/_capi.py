@@ -34,6 +34,8 @@ EXPORTED = [
     "topo_dem_create", "topo_dem_destroy", "topo_dem_last_error", "topo_dem_set_penalization",
     "topo_dem_set_external", "topo_dem_set_mask", "topo_dem_enforce", "topo_dem_energy",
     "topo_dem_energy_backward", "topo_dem_objective_gradient",
+    "topo_density_filter_create", "topo_density_filter_destroy", "topo_density_filter_nnz",
+    "topo_density_filter_apply",
 ]
 
 
@@ -126,8 +128,15 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_dem_energy.argtypes = [P, P, P, I, P, P]
     lib.topo_dem_energy_backward.argtypes = [P, P, P, I, P, P, P, P]
     lib.topo_dem_objective_gradient.argtypes = [P, P, P, P, P, P]
+    lib.topo_density_filter_create.restype = P
+    lib.topo_density_filter_create.argtypes = [I, I, D, D, D, PI]
+    lib.topo_density_filter_destroy.restype = None
+    lib.topo_density_filter_destroy.argtypes = [P]
+    lib.topo_density_filter_nnz.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    lib.topo_density_filter_apply.argtypes = [P, P, P, I, P]
     no_int = ("topo_create", "topo_create_filter", "topo_destroy", "topo_last_error", "topo_dem_create",
-              "topo_dem_destroy", "topo_dem_last_error")
+              "topo_dem_destroy", "topo_dem_last_error", "topo_density_filter_create",
+              "topo_density_filter_destroy")
     for name in EXPORTED:
         if name not in no_int:
             getattr(lib, name).restype = I

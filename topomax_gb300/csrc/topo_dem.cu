@@ -13,6 +13,7 @@
 // node-centric: every node gathers the contributions of its <= 4 cells.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -303,9 +304,160 @@ int upload(topo_dem_ctx* C, float*& dst, const float* host) {
   return TOPO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// density filter (DEM_src/filter.py:8-31)
+// ---------------------------------------------------------------------------
+// W_ij = (radius - d_ij) / S_i for d_ij <= radius, d_ij the distance between the
+// element points (np.linspace(0, W, Nx) x np.linspace(0, H, Ny), element i =
+// iy*Nx + ix) and S_i the row sum.  Evaluated on the fly with the reference's
+// rounding, term by term: d = sqrt(dx*dx + dy*dy), the row sum accumulated in
+// ascending column order, each weight divided by it, products summed in column
+// order (W x: the CSR product; W^T g: the CSC product, which accumulates the
+// rows in ascending order into each output).  No FMA contraction.
+struct DensGrid {
+  int Nx, Ny, rx, ry;
+  double W, H, radius, sx, sy;
+};
+
+__device__ __forceinline__ double dens_pt(int k, int n, double L, double step) {
+  if (n <= 1) return 0.0;
+  return k == n - 1 ? L : __dmul_rn(double(k), step);  // np.linspace: k * step, endpoint exact
+}
+
+// calls f(j, w_ij) for the neighbours j of element i in ascending order
+template <class F>
+__device__ __forceinline__ void dens_row(const DensGrid& G, int i, F&& f) {
+  const int iy = i / G.Nx, ix = i - iy * G.Nx;
+  const double xi = dens_pt(ix, G.Nx, G.W, G.sx), yi = dens_pt(iy, G.Ny, G.H, G.sy);
+  const int y0 = max(0, iy - G.ry), y1 = min(G.Ny - 1, iy + G.ry);
+  const int x0 = max(0, ix - G.rx), x1 = min(G.Nx - 1, ix + G.rx);
+  for (int jy = y0; jy <= y1; ++jy) {
+    const double dy = __dsub_rn(dens_pt(jy, G.Ny, G.H, G.sy), yi);
+    const double dy2 = __dmul_rn(dy, dy);
+    for (int jx = x0; jx <= x1; ++jx) {
+      const double dx = __dsub_rn(dens_pt(jx, G.Nx, G.W, G.sx), xi);
+      const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), dy2));
+      if (d <= G.radius) f(jy * G.Nx + jx, __dsub_rn(G.radius, d));
+    }
+  }
+}
+
+__global__ void k_dens_rowsum(DensGrid G, double* __restrict__ S, unsigned long long* __restrict__ nnz) {
+  const int n = G.Nx * G.Ny;
+  unsigned long long cnt = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    dens_row(G, i, [&](int, double w) {
+      s = __dadd_rn(s, fabs(w));
+      ++cnt;
+    });
+    S[i] = s;
+  }
+  if (cnt) atomicAdd(nnz, cnt);  // integer count: order-independent
+}
+
+template <bool TRANSPOSE>
+__global__ void k_dens_apply(DensGrid G, const double* __restrict__ S, const double* __restrict__ x,
+                             double* __restrict__ y) {
+  const int n = G.Nx * G.Ny;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    if (!TRANSPOSE) {
+      const double s = S[i];
+      dens_row(G, i, [&](int j, double w) {
+        const double wn = s != 0.0 ? __ddiv_rn(w, s) : w;
+        acc = __dadd_rn(acc, __dmul_rn(wn, x[j]));
+      });
+    } else {  // the neighbours of i are the rows that hold column i (symmetric distances)
+      dens_row(G, i, [&](int j, double w) {
+        const double s = S[j];
+        const double wn = s != 0.0 ? __ddiv_rn(w, s) : w;
+        acc = __dadd_rn(acc, __dmul_rn(wn, x[j]));
+      });
+    }
+    y[i] = acc;
+  }
+}
+
 }  // namespace
 
+struct topo_density_filter {
+  DensGrid G;
+  double* S = nullptr;
+  int64_t nnz = 0;
+};
+
 extern "C" {
+
+topo_density_filter* topo_density_filter_create(int Nx, int Ny, double width, double height, double radius,
+                                                int* status) {
+  auto fail = [&](int rc) -> topo_density_filter* {
+    if (status) *status = rc;
+    return nullptr;
+  };
+  if (Nx < 1 || Ny < 1 || !(width > 0) || !(height > 0) || !(radius >= 0) || !std::isfinite(radius) ||
+      double(Nx) * Ny > 2.0e9)
+    return fail(TOPO_ERR_ARG);
+  auto* F = new topo_density_filter();
+  DensGrid& G = F->G;
+  G.Nx = Nx;
+  G.Ny = Ny;
+  G.W = width;
+  G.H = height;
+  G.radius = radius;
+  G.sx = Nx > 1 ? width / double(Nx - 1) : 0.0;
+  G.sy = Ny > 1 ? height / double(Ny - 1) : 0.0;
+  // neighbour box: every point within radius, with one step of margin for rounding
+  G.rx = Nx > 1 ? int(std::min<double>(Nx, std::floor(radius / G.sx) + 1.0)) : 0;
+  G.ry = Ny > 1 ? int(std::min<double>(Ny, std::floor(radius / G.sy) + 1.0)) : 0;
+  const size_t n = size_t(Nx) * Ny;
+  unsigned long long* cnt = nullptr;
+  if (cudaMalloc(&F->S, n * sizeof(double)) != cudaSuccess || cudaMalloc(&cnt, sizeof(*cnt)) != cudaSuccess) {
+    cudaFree(F->S);
+    cudaFree(cnt);
+    delete F;
+    cudaGetLastError();
+    return fail(TOPO_ERR_CUDA);
+  }
+  cudaMemset(cnt, 0, sizeof(*cnt));
+  const int blocks = int(std::min<size_t>((n + 255) / 256, 65535));
+  k_dens_rowsum<<<blocks, 256>>>(G, F->S, cnt);
+  unsigned long long h = 0;
+  const cudaError_t e = cudaMemcpy(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(cnt);
+  if (e != cudaSuccess) {
+    cudaFree(F->S);
+    delete F;
+    cudaGetLastError();
+    return fail(TOPO_ERR_CUDA);
+  }
+  F->nnz = int64_t(h);
+  if (status) *status = TOPO_OK;
+  return F;
+}
+
+void topo_density_filter_destroy(topo_density_filter* f) {
+  if (!f) return;
+  cudaFree(f->S);
+  delete f;
+}
+
+int topo_density_filter_nnz(const topo_density_filter* f, int64_t* nnz) {
+  if (!f || !nnz) return TOPO_ERR_ARG;
+  *nnz = f->nnz;
+  return TOPO_OK;
+}
+
+int topo_density_filter_apply(topo_density_filter* f, const double* x, double* y, int transpose,
+                              topo_stream_t stream) {
+  if (!f || !x || !y || x == y) return TOPO_ERR_ARG;
+  const size_t n = size_t(f->G.Nx) * f->G.Ny;
+  const int blocks = int(std::min<size_t>((n + 255) / 256, 65535));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (transpose) k_dens_apply<true><<<blocks, 256, 0, s>>>(f->G, f->S, x, y);
+  else k_dens_apply<false><<<blocks, 256, 0, s>>>(f->G, f->S, x, y);
+  return cudaGetLastError() == cudaSuccess ? TOPO_OK : TOPO_ERR_CUDA;
+}
 
 topo_dem_ctx* topo_dem_create(const topo_dem_desc* desc, int* status) {
   std::lock_guard<std::recursive_mutex> lock(device_lock());

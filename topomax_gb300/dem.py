@@ -4,9 +4,12 @@ Mirrors ``DEM_src`` of topomax: ``Mesh`` and ``flatten``/``unflatten``
 (``DEM_src/utils.py``), ``SideDomain``/``CircleDomain`` (``DEM_src/domains.py``),
 ``TractionPoints``/``BodyForce``/``StrainEnergy`` (``DEM_src/elasisity_problem.py:19-129``),
 ``ElasticityEnforcer`` (``DEM_src/dirichlet_enforcer.py:14-56``) and ``MultiLayerNet``
-(``DEM_src/deep_energy_method.py:149-184``).  The energy, its gradients and the Dirichlet
-mask run in the CUDA kernels of ``csrc/topo_dem.cu`` through the C ABI; the network stays in
-torch.  The external work (traction and body-force integrals) is linear in u, so the host
+(``DEM_src/deep_energy_method.py:149-184``), ``create_density_filter``
+(``DEM_src/filter.py:8-31``), the training step ``DeepEnergyMethod``
+(``DEM_src/deep_energy_method.py:28-146``) and the DEM ``ElasticityProblem``
+(``DEM_src/elasisity_problem.py:131-216``).  The energy, its gradients, the Dirichlet mask and the density
+filter run in the CUDA kernels of ``csrc/topo_dem.cu`` through the C ABI; the network stays
+in torch.  The external work (traction and body-force integrals) is linear in u, so the host
 turns the reference's integration rules into per-node weights once.
 
 There is no CPU path: without the library or a CUDA device these classes raise.
@@ -14,6 +17,7 @@ There is no CPU path: without the library or a CUDA device these classes raise.
 from __future__ import annotations
 
 import ctypes
+from dataclasses import dataclass
 import math
 from typing import Iterable
 
@@ -342,6 +346,72 @@ class _DemContext:
             self.lib.topo_dem_destroy(ptr)
 
 
+# ---------------------------------------------------------------------------
+# density filter (DEM_src/filter.py:8-31)
+# ---------------------------------------------------------------------------
+
+
+class DensityFilter:
+    """The reference's density filter W (a row-normalised radius-neighbour matrix over
+    the element points) as a GPU operator: ``W @ rho`` and ``W.T @ g`` as the reference's
+    ``DEM_src/elasisity_problem.py:162, 171`` use it, bit-identical to the scipy product.
+    Accepts numpy arrays (returns numpy) or torch tensors (returns a CUDA FP64 tensor)
+    of Nx*Ny values in the reference's flatten order (element iy*Nx + ix)."""
+
+    def __init__(self, radius: float, mesh: Mesh):
+        if not torch.cuda.is_available():
+            raise RuntimeError("topomax_gb300.dem needs a CUDA device (there is no CPU path)")
+        self.lib = _capi.load_library()
+        self.n = mesh.Nx * mesh.Ny
+        self.shape = (self.n, self.n)
+        st = ctypes.c_int(0)
+        self.ptr = self.lib.topo_density_filter_create(mesh.Nx, mesh.Ny, float(mesh.width), float(mesh.height),
+                                                       float(radius), ctypes.byref(st))
+        if not self.ptr:
+            if st.value == _capi.TOPO_ERR_CUDA:
+                raise RuntimeError("topo_density_filter_create: CUDA error")
+            raise ValueError(f"invalid density filter (radius {radius}, mesh {mesh.Nx}x{mesh.Ny})")
+        self._transpose = False
+
+    @property
+    def nnz(self) -> int:
+        v = ctypes.c_int64(0)
+        self.lib.topo_density_filter_nnz(self.ptr, ctypes.byref(v))
+        return int(v.value)
+
+    @property
+    def T(self) -> "DensityFilter":
+        t = object.__new__(DensityFilter)
+        t.__dict__.update(self.__dict__)
+        t._owner = self  # keeps the device object alive
+        t._transpose = not self._transpose
+        return t
+
+    def __matmul__(self, v):
+        as_numpy = isinstance(v, np.ndarray)
+        x = torch.as_tensor(np.asarray(v) if as_numpy else v).to(device="cuda", dtype=torch.float64)
+        x = x.reshape(-1).contiguous()
+        if x.numel() != self.n:
+            raise ValueError(f"dimension mismatch: filter of size {self.n}, vector of size {x.numel()}")
+        y = torch.empty_like(x)
+        rc = self.lib.topo_density_filter_apply(self.ptr, _ptr(x), _ptr(y), int(self._transpose), _stream())
+        if rc != _capi.TOPO_OK:
+            raise RuntimeError(f"topo_density_filter_apply failed ({rc})")
+        return y.cpu().numpy() if as_numpy else y
+
+    def __del__(self):
+        if getattr(self, "_owner", None) is not None:
+            return
+        ptr, self.ptr = getattr(self, "ptr", None), None
+        if ptr:
+            self.lib.topo_density_filter_destroy(ptr)
+
+
+def create_density_filter(radius: float, mesh: Mesh) -> DensityFilter:
+    """Replaces DEM_src/filter.py:8-31 (same weights, no O(N^2) host construction)."""
+    return DensityFilter(radius, mesh)
+
+
 def _as_u(u: torch.Tensor, mesh: Mesh) -> torch.Tensor:
     nn = (mesh.Nx + 1) * (mesh.Ny + 1)
     if u.shape != (nn, 2):
@@ -533,3 +603,155 @@ class MultiLayerNet(torch.nn.Module):
         for i in range(1, self.layer_count - 1):
             y = self.activation_function(self.linears[i](y))
         return self.linears[-1](y)
+
+
+# ---------------------------------------------------------------------------
+# training step and problem (DEM_src/deep_energy_method.py:28-146,
+# DEM_src/elasisity_problem.py:131-216, DEM_src/problem.py:13-41)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class NNParameters:
+    layer_count: int
+    neuron_count: int
+    learning_rate: float
+    iteration_count: int
+    weight_deviation: float
+    fourier_deviation: float
+    activation_function: str
+    convergence_tolerance: float
+
+
+def _network(input_size: int, output_size: int, p: NNParameters) -> MultiLayerNet:
+    return MultiLayerNet(input_size, output_size, p.layer_count, p.neuron_count, p.weight_deviation,
+                         p.fourier_deviation, p.activation_function)
+
+
+class DeepEnergyMethod:
+    """DeepEnergyMethod of DEM_src/deep_energy_method.py:28-146.  One L-BFGS closure
+    evaluation = the network forward and backward in torch plus ONE fused kernel launch
+    for the Dirichlet mask and the strain energy (and one for its gradient)."""
+
+    def __init__(self, device, verbose: bool, output_size: int, nn_parameters: NNParameters,
+                 dirichlet_enforcer: "ElasticityEnforcer", objective_calculator: StrainEnergy):
+        self.device = torch.device(device) if device is not None else torch.device("cuda")
+        self.model = _network(2, output_size, nn_parameters).to(self.device)
+        self.verbose = verbose
+        self.output_size = output_size
+        self.nn_parameters = nn_parameters
+        self.dirichlet_enforcer = dirichlet_enforcer
+        self.objective_calculator = objective_calculator
+        self.loss_array: list[float] = []
+
+    def set_nn_parameters(self, nn_parameters: NNParameters):
+        self.model = _network(2, self.output_size, nn_parameters).to(self.device)
+        self.nn_parameters = nn_parameters
+
+    def _coordinates(self, mesh: Mesh) -> torch.Tensor:
+        return torch.from_numpy(flatten([mesh.x_grid, mesh.y_grid])).float().to(self.device)
+
+    def train_model(self, rho, mesh: Mesh):
+        """L-BFGS on the energy (lr, max_iter 20, strong-Wolfe line search, the loss-mean
+        convergence test), then (objective, gradient) at the trained displacement."""
+        x = self._coordinates(mesh)
+        x.requires_grad_(True)
+        density = torch.as_tensor(np.asarray(rho)).float().reshape(mesh.intervals).to(self.device)
+        opt = torch.optim.LBFGS(self.model.parameters(), lr=self.nn_parameters.learning_rate, max_iter=20,
+                                line_search_fn="strong_wolfe")
+        energy = self.objective_calculator
+
+        def closure_generator(t: int):
+            def closure():
+                loss = energy.calculate_energy_enforced(self.model(x), self.dirichlet_enforcer, density)
+                opt.zero_grad()
+                loss.backward()
+                value = float(loss)
+                if self.verbose:
+                    print(f"\rIter: {t + 1:^3} - Loss: {value:.6g}", end="")
+                self.loss_array.append(value)
+                return value
+            return closure
+
+        for t in range(self.nn_parameters.iteration_count):
+            opt.step(closure_generator(t))
+            if self.convergence_check(self.loss_array, self.nn_parameters.convergence_tolerance):
+                break
+        if self.verbose:
+            print()
+        return energy.calculate_objective_and_gradient(self.get_u(x), mesh.shape, density)
+
+    def get_loss(self, rho, mesh: Mesh) -> float:
+        density = torch.as_tensor(np.asarray(rho)).float().reshape(mesh.intervals).to(self.device)
+        return float(self.objective_calculator.calculate_energy(self.get_u(mesh=mesh), mesh.shape, density))
+
+    def get_u(self, x: torch.Tensor | None = None, mesh: Mesh | None = None) -> torch.Tensor:
+        if x is None:
+            if mesh is None:
+                raise ValueError("get_u must get either x or mesh, they can't both be None")
+            x = self._coordinates(mesh)
+        return self.dirichlet_enforcer(self.model(x))
+
+    @staticmethod
+    def convergence_check(loss_array, tolerance: float) -> bool:
+        """The mean of the last 10 losses against the 10 before (at least 20 evaluations)."""
+        num_check = 10
+        if len(loss_array) < 2 * num_check:
+            return False
+        mean1 = float(np.mean(loss_array[-2 * num_check:-num_check]))
+        mean2 = float(np.mean(loss_array[-num_check:]))
+        if abs(mean2) < 1e-6:
+            return True
+        return abs(mean1 - mean2) / abs(mean2) < tolerance
+
+
+class ElasticityProblem:
+    """The DEM compliance problem of DEM_src/elasisity_problem.py:131-216: the density is
+    filtered (classical radius = 2 sqrt(3) x the Helmholtz radius), the network trained
+    on it, and the gradient mapped back through the filter's transpose."""
+
+    def __init__(self, mesh: Mesh, device, verbose: bool, parameters):
+        self.parameters = parameters
+        self.mesh = mesh
+        self.device = device
+        self.verbose = verbose
+        dirichlet_enforcer, objective_calculator = self.create_dem_parameters()
+        self.dem = self.create_dem(dirichlet_enforcer, objective_calculator)
+        self.filter = create_density_filter(self.parameters.filter_radius * 2 * np.sqrt(3), self.mesh)
+        self.objective_gradient: np.ndarray | None = None
+
+    def set_penalization(self, penalization: float):
+        self.dem.objective_calculator.set_penalization(penalization)
+
+    def calculate_objective_gradient(self):
+        if self.objective_gradient is None:
+            raise ValueError("You must call calculate_objective before calling calculate_objective_gradient")
+        return self.objective_gradient
+
+    def calculate_objective(self, rho) -> float:
+        rho = np.asarray(rho)
+        filtered_rho = self.filter @ rho.flatten()
+        objective, gradient = self.dem.train_model(filtered_rho, self.mesh)
+        g = gradient.detach().double().cpu().numpy().flatten()
+        self.objective_gradient = (self.filter.T @ g).reshape(rho.shape)
+        return float(objective)
+
+    def forward(self, rho):
+        return None
+
+    def create_dem_parameters(self):
+        body_force = BodyForce(self.mesh, self.parameters.body_force, self.device) if self.parameters.body_force \
+            else None
+        tractions = [TractionPoints(self.mesh, t) for t in self.parameters.tractions] \
+            if self.parameters.tractions else None
+        enforcer = ElasticityEnforcer(self.parameters, self.mesh, self.device)
+        energy = StrainEnergy(self.mesh, body_force, self.parameters.young_modulus, self.parameters.poisson_ratio,
+                              tractions)
+        return enforcer, energy
+
+    def create_dem(self, dirichlet_enforcer, objective_calculator) -> DeepEnergyMethod:
+        nn_parameters = NNParameters(layer_count=5, neuron_count=68, learning_rate=1.73553, iteration_count=100,
+                                     weight_deviation=0.062264, fourier_deviation=0.119297,
+                                     activation_function="rrelu", convergence_tolerance=5e-5)
+        return DeepEnergyMethod(self.device, self.verbose, 2, nn_parameters, dirichlet_enforcer,
+                                objective_calculator)
