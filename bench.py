@@ -17,8 +17,8 @@ state solve + compliance).
   design resident in HBM, CUDA events per step, L2 flushed (256 MB write)
   before every step.
 * ``fp64``: the same loop with plain FP64 multigrid CG (the metric's
-  comparison) over the same design steps as the first timed mixed steps, and the
-  max relative compliance difference between the two.
+  comparison) over the same design steps as the timed mixed steps (by default all
+  of them), and the max relative compliance difference between the two.
 * ``e2e``: the same steps (same warm-up, same step sizes) through the
   reference-facing API with host (pinned) arrays, as the reference's
   Solver.step/project/set_from_array drive it.
@@ -54,18 +54,23 @@ PENALTY = 3.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=1000)
     ap.add_argument("--ny", type=int, default=500)
     ap.add_argument("--rtol", type=float, default=1e-8)
-    ap.add_argument("--fp64-steps", type=int, default=4)
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--fp64-steps", type=int, default=None, help="default: --steps (the same design steps)")
+    ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps (the same design steps)")
     ap.add_argument("--c2-steps", type=int, default=2,
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
     ap.add_argument("--cpu-sample", default="160x80,320x160", help="oracle grids timed for the CPU baseline")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.fp64_steps is None:
+        args.fp64_steps = args.steps
+    if args.e2e_steps is None:
+        args.e2e_steps = args.steps
+    return args
 
 
 def design_dict():
@@ -384,6 +389,7 @@ def main():
     # --- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
     alg_bytes = 2 * dofs(args.nx, args.ny) * 4 + nv * 4
+    flops = 104.0 * 7 * 2 * args.nx * args.ny
     op = float(np.mean(op_ms))
     achieved = alg_bytes / (op * 1e-3) / 1e9
     traffic = ncu_traffic(args.nx, args.ny)
@@ -409,7 +415,10 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_p2_march<float, Apply> (FP32 matrix-free P2 operator)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
-                     "launch_ms": op},
+                     "launch_ms": op,
+                     # the same launch in FP32 flops: 104 flops per quadrature point of
+                     # the 7-point rule per triangle (the element product of the form)
+                     "algorithmic_flops": flops, "achieved_tflops": flops / (op * 1e-3) / 1e12},
         "cpu_baseline": {k: v for k, v in cpu.items() if k != "seconds_per_iteration_at_target"},
         "gpu_launches": int(nlaunch),
         "c2_2000x1000": c2,
