@@ -51,6 +51,17 @@ STEP = 0.002           # EMD step size of the benchmark design
 PENALTY = 3.0
 
 
+def job_throughput(total_ms: float, steps: int, world: int, dist=None, device="cuda"):
+    """Replicas: the job takes as long as its slowest rank, and every rank did `steps`
+    design iterations.  Returns (max-over-ranks total ms, whole-job iterations/s)."""
+    if dist is not None:
+        import torch
+        t = torch.tensor([float(total_ms)], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * steps / (total_ms / 1000.0)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -346,13 +357,8 @@ def main():
     clocks.start(local if not os.environ.get("CUDA_VISIBLE_DEVICES") else 0)
     times, objs, nlaunch, op_ms = device_loop(prob, args.steps, args.warmup, time_operator=True, profile=True)
     ck = clocks.stop()
-    total_ms = float(np.sum(times))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = job_throughput(float(np.sum(times)), args.steps, world, dist)
     ms = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1000.0)
     e2e_times = e2e_loop(prob, args.e2e_steps, args.warmup)
     e2e_value = 1.0 / float(np.mean(e2e_times))
     stats = dict(prob.stats)
