@@ -202,6 +202,10 @@ struct topo_ctx {
   bool verify_residual = false;  // TOPO_VERIFY_RESIDUAL=1: confirm FGMRES convergence with a true residual
   // tightest relative tolerance of an FP32 inner solve (TOPO_INNER_FLOOR_STATE / _FILTER)
   double inner_floor_state = 1e-4, inner_floor_filter = 1e-5;
+  // lower end of the Chebyshev smoothing interval (fraction of lambda_max) per
+  // hierarchy (TOPO_CHEB_LO_STATE / _FILTER): the high-contrast elasticity levels
+  // converge best with a wide interval, the filter's with a narrower one
+  double cheb_lo_state = 0.05, cheb_lo_filter = 0.2;
   double* fst64_stiff = nullptr;  // filter level-0 stencils (FP64): eps^2 K + M, and M
   double* fst64_mass = nullptr;
   float* rm_op32 = nullptr;   // FP32 copies for the mixed mode's FP32 operator and preconditioner
@@ -319,6 +323,8 @@ int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
     C->inner_floor_state = std::max(1e-8, std::min(0.5, std::atof(e)));
   if (const char* e = std::getenv("TOPO_INNER_FLOOR_FILTER"))
     C->inner_floor_filter = std::max(1e-8, std::min(0.5, std::atof(e)));
+  if (const char* e = std::getenv("TOPO_CHEB_LO_STATE")) C->cheb_lo_state = std::max(1e-3, std::min(0.9, std::atof(e)));
+  if (const char* e = std::getenv("TOPO_CHEB_LO_FILTER")) C->cheb_lo_filter = std::max(1e-3, std::min(0.9, std::atof(e)));
   if (!g || g->nx < 1 || g->ny < 1 || !(g->width > 0) || !(g->height > 0))
     return C->fail(TOPO_ERR_ARG, "invalid grid description");
   if (precision != TOPO_PREC_FP64 && precision != TOPO_PREC_MIXED)
@@ -378,6 +384,7 @@ int init_filter(topo_ctx* C, double eps) {
   if (C->precision == TOPO_PREC_MIXED) {
     C->fmg32.use_graphs = graphs_enabled();
     C->fmg32.fp64_solution = true;  // FGMRES directions keep the inner solutions in FP64
+    C->fmg32.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg32.use_tail = env_flag("TOPO_TAIL", true);
     C->fmg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
@@ -388,6 +395,7 @@ int init_filter(topo_ctx* C, double eps) {
     st = C->fmg32.setup(s);
   } else {
     C->fmg64.use_graphs = graphs_enabled();
+    C->fmg64.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg64.use_tail = env_flag("TOPO_TAIL", true);
     C->fmg64.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
@@ -725,6 +733,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       if (precision == TOPO_PREC_MIXED) {
         C->smg32.use_graphs = graphs_enabled();
         C->smg32.fp64_solution = true;
+        C->smg32.cheb_lo_frac = C->cheb_lo_state;
         C->smg32.trace_setup = C->trace_solves;
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
@@ -736,6 +745,7 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->sens_tri = C->arena.alloc_n<float>(size_t(3) * C->sspec[0].ntri());
       } else {
         C->smg64.use_graphs = graphs_enabled();
+        C->smg64.cheb_lo_frac = C->cheb_lo_state;
         C->smg64.use_tail = env_flag("TOPO_TAIL", true);
         C->smg64.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
