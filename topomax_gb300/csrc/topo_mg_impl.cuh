@@ -822,6 +822,10 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
   red_ = red;
   sms_ = red->sms;
   prime_march_occupancy<T>();
+  if (const char* e = std::getenv("TOPO_POWER_WARM")) {  // warm-started power-iteration steps
+    const int v = std::atoi(e);
+    if (v >= 1 && v <= 50) power_iters_warm = v;
+  }
   lv_.assign(specs.size(), Lev{});
   for (size_t l = 0; l < specs.size(); ++l) {
     const size_t n = specs[l].ndof();
