@@ -34,22 +34,10 @@ __global__ void k_axpy(T* __restrict__ y, T a, const T* __restrict__ x, size_t n
   TOPO_GRID_STRIDE(i, n) y[i] += a * x[i];
 }
 
-// p = z + b p
-template <class T>
-__global__ void k_xpby(T* __restrict__ p, const T* __restrict__ z, T b, size_t n) { TOPO_PDL_ENTRY();
-  TOPO_GRID_STRIDE(i, n) p[i] = z[i] + b * p[i];
-}
-
 // r = b - y
 template <class T>
 __global__ void k_sub(T* __restrict__ r, const T* __restrict__ b, const T* __restrict__ y, size_t n) { TOPO_PDL_ENTRY();
   TOPO_GRID_STRIDE(i, n) r[i] = b[i] - y[i];
-}
-
-// u += s * d  (d in lower precision)
-template <class TU, class TD>
-__global__ void k_add_scaled(TU* __restrict__ u, double s, const TD* __restrict__ d, size_t n) { TOPO_PDL_ENTRY();
-  TOPO_GRID_STRIDE(i, n) u[i] += TU(s * double(d[i]));
 }
 
 template <class T>
@@ -59,11 +47,6 @@ __global__ void k_mul(T* __restrict__ y, const T* __restrict__ a, const T* __res
 
 template <class T>
 __global__ void k_scale(T* __restrict__ x, T a, size_t n) { TOPO_PDL_ENTRY(); TOPO_GRID_STRIDE(i, n) x[i] *= a; }
-
-template <class T>
-__global__ void k_recip(T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
-  TOPO_GRID_STRIDE(i, n) x[i] = T(1) / x[i];
-}
 
 template <class T>
 __global__ void k_inverse(T* __restrict__ y, const T* __restrict__ x, size_t n) { TOPO_PDL_ENTRY();
@@ -81,38 +64,6 @@ __global__ void k_scale_unit(T* __restrict__ x, const double* __restrict__ nrm2,
   __syncthreads();
   const T a = a_s;
   TOPO_GRID_STRIDE(i, n) x[i] *= a;
-}
-
-// Chebyshev smoother pieces (preconditioner Dinv).  The coefficients live in
-// device memory (coef[0] = 1/theta, coef[2k-1], coef[2k] = step-k weights) so a
-// captured graph stays valid when a new set-up changes the eigenvalue bounds.
-// first step: r = b - t (t == nullptr: r = b, the x = 0 start)
-//             d = coef[0] Dinv r ; x = (xzero ? 0 : x) + d
-template <class T>
-__global__ void k_cheb_first(const T* __restrict__ b, const T* __restrict__ t, T* __restrict__ r,
-                             const T* __restrict__ dinv, T* __restrict__ d, T* __restrict__ x,
-                             const double* __restrict__ coef, size_t n) { TOPO_PDL_ENTRY();
-  const T c0 = T(coef[0]);
-  TOPO_GRID_STRIDE(i, n) {
-    const T ri = t ? b[i] - t[i] : b[i];
-    r[i] = ri;
-    const T di = c0 * dinv[i] * ri;
-    d[i] = di;
-    x[i] = t ? x[i] + di : di;
-  }
-}
-// later steps: r -= t ; d = c1 d + c2 Dinv r ; x += d
-template <class T>
-__global__ void k_cheb_next(T* __restrict__ r, const T* __restrict__ t, const T* __restrict__ dinv,
-                            T* __restrict__ d, T* __restrict__ x, const double* __restrict__ coef, size_t n) { TOPO_PDL_ENTRY();
-  const T c1 = T(coef[0]), c2 = T(coef[1]);
-  TOPO_GRID_STRIDE(i, n) {
-    const T ri = r[i] - t[i];
-    r[i] = ri;
-    const T di = c1 * d[i] + c2 * dinv[i] * ri;
-    d[i] = di;
-    x[i] += di;
-  }
 }
 
 // ---------------------------------------------------------------------------
