@@ -13,7 +13,10 @@ It reads, without importing any reference module:
   unpickler restricted to numpy types -> ``tests/golden/triangle_N10.json``;
 * ``tests/test_data/DEM/{short_cantilever,bridge}/problem_data.dat`` -- the
   known answers of ``tests/test_DEM_problem.py:14-43`` ->
-  ``tests/golden/dem_<design>.npz``.
+  ``tests/golden/dem_<design>.npz``;
+* ``designs/diffuser.json`` and ``tests/test_data/FEM/diffuser/data/correct_{data,rho}.dat``
+  -- the known answer of ``tests/test_fluid_solver.py`` (the pickled ``IterationData``
+  is read into a plain attribute holder) -> ``tests/golden/diffuser_N20.json``.
 
 The fixtures are committed so the tests never need the reference at run time.
 """
@@ -41,6 +44,25 @@ class _NumpyOnly(pickle.Unpickler):
 def _load(path):
     with open(path, "rb") as f:
         return _NumpyOnly(f).load()
+
+
+class _Record:
+    """Holds the attributes of a pickled record (no methods, no reference code)."""
+
+    def __setstate__(self, state):
+        self.__dict__.update(state if isinstance(state, dict) else {"state": state})
+
+
+class _RecordData(_NumpyOnly):
+    def find_class(self, module, name):
+        if (module, name) == ("src.utils", "IterationData"):
+            return _Record
+        return super().find_class(module, name)
+
+
+def _load_record(path):
+    with open(path, "rb") as f:
+        return _RecordData(f).load()
 
 
 def main():
@@ -73,6 +95,20 @@ def main():
     }
     with open(os.path.join(HERE, "triangle_N10.json"), "w") as f:
         json.dump(out, f, indent=1)
+
+    with open(os.path.join(REF, "designs", "diffuser.json")) as f:
+        diffuser = json.load(f)
+    with open(os.path.join(HERE, "designs", "diffuser.json"), "w") as f:
+        json.dump(diffuser, f, indent=2)
+    base = os.path.join(REF, "tests", "test_data", "FEM", "diffuser", "data")
+    rec = _load_record(os.path.join(base, "correct_data.dat"))
+    rho = _load(os.path.join(base, "correct_rho.dat"))
+    vec = np.asarray(rho["vector"], dtype=np.float64)
+    with open(os.path.join(HERE, "diffuser_N20.json"), "w") as f:
+        json.dump({"design": "diffuser.json", "N": int(rho["N"]), "objective": float(rec.objective),
+                   "iteration": int(rec.iteration), "penalty": float(rec.penalty),
+                   "rho_sorted": np.sort(vec).tolist(), "rho_sum": float(vec.sum()),
+                   "note": "rho is in dolfin dof order in the reference; compared sorted"}, f, indent=1)
 
     for design in ("short_cantilever", "bridge"):
         p = os.path.join(REF, "tests", "test_data", "DEM", design, "problem_data.dat")
