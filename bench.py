@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--fp64-steps", type=int, default=None, help="default: --steps (the same design steps)")
     ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps (the same design steps)")
-    ap.add_argument("--c2-steps", type=int, default=2,
+    ap.add_argument("--c2-steps", type=int, default=50,
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
     ap.add_argument("--cpu-sample", default="160x80,320x160", help="oracle grids timed for the CPU baseline")
     args = ap.parse_args()
