@@ -179,7 +179,7 @@ struct topo_ctx {
   bool penal_set = false;
   double p = 0;
   long long launches = 0;          // kernels launched by the context itself
-  const double* xi_last = nullptr;  // design of the last state solve
+  bool state_ready = false;  // a state solve has set up the operator of a design
   Dir dir_p2{};
   Arena arena;
   Reducer red;
@@ -858,7 +858,7 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
       std::fprintf(stderr, "[topo solve] state set-up %.3f ms\n",
                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     }
-    ctx->xi_last = xi;
+    ctx->state_ready = true;
     const size_t n = 2 * ctx->nn2;
     const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
     SolveStats st;
@@ -962,6 +962,7 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
     if (!(hs.done && hs.ok)) {
       // bracketing fallback (src/utils.py:138-157): grow [-r, r] from 2 while r <= 2000
       auto F = [&](double cc) {
+        ctx->launches += 1;
         k_eval_volume<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, cc, ctx->red.partials,
                                                                 ctx->red.counter, ctx->red.out);
         cudaMemcpyAsync(ctx->red.host, ctx->red.out, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -1024,6 +1025,7 @@ int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t st
   return guarded(ctx, [&]() {
     if (!f || !out) return ctx->fail(TOPO_ERR_ARG, "invalid integrate arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    ctx->launches += 1;
     k_dot<double, double><<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->vw, f, ctx->nv, ctx->red.partials,
                                                                 ctx->red.counter, out);
     return ctx->cuda_check("integrate");
@@ -1037,6 +1039,7 @@ int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y
     if (!xi || !u || !y) return ctx->fail(TOPO_ERR_ARG, "invalid apply arguments");
     if (!aligned16(u) || !aligned16(y)) return ctx->fail(TOPO_ERR_ARG, "displacement arrays must be 16-byte aligned");
     p2_apply_f64(ctx->p2params<double>(), xi, u, y, reinterpret_cast<cudaStream_t>(stream));
+    ctx->launches += 1;
     return ctx->cuda_check("apply");
   });
 }
@@ -1045,6 +1048,7 @@ int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream) {
   return guarded(ctx, [&]() {
     if (!ctx->has_state || !ms) return ctx->fail(TOPO_ERR_ARG, "invalid arguments");
     if (!ctx->penal_set) return ctx->fail(TOPO_ERR_STATE, "You must set penalization before calling penalizer");
+    if (!ctx->state_ready) return ctx->fail(TOPO_ERR_STATE, "no state solve has set up the operator yet");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -1057,7 +1061,7 @@ int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream) {
       cudaEventRecord(e1, s);
     } else {
       cudaEventRecord(e0, s);
-      p2_apply_f64(ctx->p2params<double>(0, ctx->rm_op64), ctx->xi_last, ctx->r64, ctx->y64, s);
+      p2_apply_f64(ctx->p2params<double>(0, ctx->rm_op64), ctx->xi64, ctx->r64, ctx->y64, s);
       cudaEventRecord(e1, s);
     }
     ctx->launches += 1;
