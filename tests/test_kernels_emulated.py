@@ -97,7 +97,30 @@ def test_p2_fp32_operator_consistent_at_smooth_fields():
     assert arithmetic <= 3e-4 and arithmetic <= 0.1 * representation
 
 
-@pytest.mark.parametrize("case", CASES)
+TINY = [
+    # one-cell strips and a single-row warp segment: the halo columns and rows of
+    # the march fall outside the lattice on both sides
+    (1.0, 1.0, 1, 1, ["Left"], 3.0),
+    (1.0, 1.0, 1, 1, [], 3.0),
+    (1.0, 1.0, 1, 5, ["Bottom"], 3.0),
+    (1.0, 1.0, 5, 1, ["Left"], 3.0),
+    (4.0, 1.0, 31, 1, ["Left"], 3.0),
+    (4.0, 1.0, 32, 2, ["Top"], 3.0),
+]
+
+
+@pytest.mark.parametrize("case", TINY)
+def test_p2_apply_on_tiny_lattices(case):
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    ref = o.apply_state(xi, u)
+    for prec, tol in ((0, 1e-12), (1, 2e-5)):
+        y = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=prec)
+        assert np.max(np.abs(y - ref)) <= tol * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", CASES + TINY[:2])
 def test_p2_diag_matches_oracle(case):
     W, H, nx, ny, sides, p = case
     d, L, o, xi, u, dirv = _problem(*case)
