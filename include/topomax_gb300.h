@@ -273,6 +273,54 @@ int topo_density_filter_nnz(const topo_density_filter* f, int64_t* nnz);
 int topo_density_filter_apply(topo_density_filter* f, const double* x, double* y, int transpose,
                               topo_stream_t stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Stokes-Brinkman fluid problem (Taylor-Hood P2 velocity / P1 pressure), FP64
+ * ---------------------------------------------------------------------------------------
+ * Replaces FluidProblem (FEM_src/fluid_problem.py:48-155) with the FluidPenalizer of
+ * src/penalizers.py:49-67: forward (:168-169), calculate_objective (:152-166) and
+ * calculate_objective_gradient (:134-150).  Velocities are interleaved [(2nx+1)(2ny+1)][2]
+ * on the P2 lattice, pressures and designs are CG1 [(nx+1)(ny+1)], all device FP64.  Every
+ * side is a Dirichlet side: the flow profiles of BoundaryFlows (:12-45) on the flow sides,
+ * no slip (applied last) on the others.  The pressure is returned with zero sum: the state
+ * system is singular in the pressure constant and, with the interpolated profiles, slightly
+ * inconsistent; the continuity right-hand side is projected to zero sum. */
+typedef struct {
+  int side;      /* TOPO_SIDE_* */
+  double center; /* profile centre along the side */
+  double length; /* profile width */
+  double rate;   /* peak velocity (rate * (1 - (2 t / length)^2)) */
+} topo_flow;
+
+typedef struct topo_fluid_ctx topo_fluid_ctx;
+topo_fluid_ctx* topo_fluid_create(const topo_grid_desc* grid, double viscosity, const topo_flow* flows, int n_flows,
+                                  int* status);
+void topo_fluid_destroy(topo_fluid_ctx* ctx);
+const char* topo_fluid_last_error(const topo_fluid_ctx* ctx);
+int topo_fluid_sizes(const topo_fluid_ctx* ctx, int64_t* n_vertices, int64_t* n_velocity);
+/* FluidPenalizer.set_penalization (src/penalizers.py:9-14): q > 0 */
+int topo_fluid_set_penalization(topo_fluid_ctx* ctx, double q);
+/* the Dirichlet data (zero at interior nodes) into u [2 n2] */
+int topo_fluid_boundary_values(topo_fluid_ctx* ctx, double* u, topo_stream_t stream);
+/* y = A x for x = [u (2 n2) | p (nv)] (n = 2 n2 + nv), A the state operator with the
+ * continuity rows negated (symmetric on velocities vanishing on the boundary); clamp = 1
+ * makes the boundary velocity rows identity rows.  x != y. */
+int topo_fluid_apply(topo_fluid_ctx* ctx, const double* rho, const double* x, double* y, int clamp,
+                     topo_stream_t stream);
+/* forward: velocity u [2 n2] (boundary data included) and pressure p [nv] (may be null),
+ * flexible GMRES to |r| <= rtol |b| on the reduced system; synchronises */
+int topo_fluid_state_solve(topo_fluid_ctx* ctx, const double* rho, double* u, double* p, double rtol, int* iters,
+                           topo_stream_t stream);
+/* 1/2 int alpha(rho) |u|^2 + viscosity |grad u|^2 dx into a device double */
+int topo_fluid_objective(topo_fluid_ctx* ctx, const double* rho, const double* u, double* objective,
+                         topo_stream_t stream);
+/* b_k = int 1/2 alpha'(rho) |u|^2 phi_k (the projection's right-hand side, degree-7 rule) */
+int topo_fluid_gradient_rhs(topo_fluid_ctx* ctx, const double* rho, const double* u, double* b,
+                            topo_stream_t stream);
+/* g = M1^-1 b: the CG1 L2 projection of 1/2 alpha'(rho) |u|^2 (df.project); synchronises */
+int topo_fluid_gradient(topo_fluid_ctx* ctx, const double* rho, const double* u, double* g, double rtol,
+                        int* iters, topo_stream_t stream);
+int topo_fluid_launch_count(const topo_fluid_ctx* ctx, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

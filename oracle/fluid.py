@@ -210,6 +210,8 @@ class FluidOracle:
 
     def state_solve(self, rho):
         """Velocity (2*n2, interleaved) and pressure (n_vertices)."""
+        if self.pressure == "mean":
+            return self._state_solve_mean(rho)
         K = self.assemble(rho)
         b = np.zeros(self.n)
         keep = np.ones(self.n)
@@ -236,6 +238,28 @@ class FluidOracle:
         b[self.nuv] = 0.0
         x = spla.spsolve((sp.diags(keep1) @ K0 + sp.diags(id1)).tocsc(), b)
         return x[:self.nuv], x[self.nuv:]
+
+    def _state_solve_mean(self, rho):
+        """The closure of the reduced system: the Dirichlet velocity dofs eliminated, the
+        continuity right-hand side projected to zero sum (its Euclidean least-squares
+        part), the pressure fixed by sum(p) = 0 through a bordering row."""
+        K = self.assemble(rho).tocsr()
+        nuv = self.nuv
+        bc = np.zeros(nuv, bool)
+        bc[self.bc_dofs] = True
+        I = np.nonzero(~bc)[0]
+        uB = np.zeros(nuv)
+        uB[self.bc_dofs] = self.bc_vals
+        A, G, D = K[:nuv, :nuv], K[:nuv, nuv:], K[nuv:, :nuv]
+        f = -(A[I] @ uB)
+        g = -(D @ uB)
+        g = g - g.mean()
+        ones = sp.csr_matrix(np.ones((self.nv, 1)))
+        S = sp.bmat([[A[I][:, I], G[I], None], [D[:, I], None, ones], [None, ones.T, None]]).tocsc()
+        x = spla.spsolve(S, np.concatenate([f, g, [0.0]]))
+        u = uB.copy()
+        u[I] = x[:I.size]
+        return u, x[I.size:I.size + self.nv]
 
     def boundary_flux(self, rho=None) -> float:
         """int div u_h dx of the interpolated boundary data (zero for a compatible one)."""

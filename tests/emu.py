@@ -171,3 +171,77 @@ def coarse_cheb(nx, ny, hx, hy, eps2, b, deg=0):
     rc = E.emu_coarse_cheb(nx, ny, hx, hy, eps2, deg, dp(b), dp(x), dp(info))
     assert rc == 0
     return x, info[0], info[1], int(info[2])
+
+
+# ---- Stokes-Brinkman fluid ------------------------------------------------------------
+def _fluid(E):
+    E.emu_fluid_tables.argtypes = [C_D, C_D, P_D]
+    E.emu_fluid_bc.argtypes = [C_I, C_I, C_D, C_D, C_I, P_D, P_D]
+    E.emu_fluid_bc.restype = C_I
+    E.emu_fluid_alpha.argtypes = [C_D, C_D, C_I]
+    E.emu_fluid_alpha.restype = C_D
+    E.emu_fluid_apply.argtypes = [C_I, C_I, C_D, C_D, C_D, P_D, P_D, P_D, C_I]
+    E.emu_fluid_objective.argtypes = [C_I, C_I, C_D, C_D, C_D, C_D, P_D, P_D]
+    E.emu_fluid_objective.restype = C_D
+    E.emu_fluid_gradient_rhs.argtypes = [C_I, C_I, C_D, C_D, C_D, P_D, P_D, P_D]
+    E.emu_p2_node_incidence.argtypes = [C_I, C_I, C_I, C_I, ctypes.POINTER(ctypes.c_longlong), P_I]
+    return E
+
+
+FLUID_TABLES = [  # (name, shape) in FluidTables' member order
+    ("area", ()), ("lam6", (12, 3)), ("w6", (12,)), ("lam7", (16, 3)), ("w7", (16,)),
+    ("N6", (12, 6)), ("N7", (16, 6)), ("dN6", (2, 12, 6, 2)), ("lap", (2, 6, 6)),
+    ("grad", (2, 6, 2, 3)), ("div", (2, 3, 6, 2)),
+]
+
+
+def fluid_tables(hx, hy):
+    E = _fluid(lib())
+    n = E.emu_fluid_tables_doubles()
+    buf = np.zeros(n)
+    E.emu_fluid_tables(hx, hy, dp(buf))
+    out, off = {}, 0
+    for name, shape in FLUID_TABLES:
+        size = int(np.prod(shape)) if shape else 1
+        out[name] = buf[off:off + size].reshape(shape) if shape else float(buf[off])
+        off += size
+    assert off == n
+    return out
+
+
+def fluid_bc(nx, ny, W, H, flows):
+    E = _fluid(lib())
+    f = np.array([[SIDE[s], c, l, r] for s, c, l, r in flows], dtype=np.float64).reshape(-1)
+    ub = np.zeros(2 * (2 * nx + 1) * (2 * ny + 1))
+    assert E.emu_fluid_bc(nx, ny, W, H, len(flows), dp(f) if len(flows) else None, dp(ub)) == 0
+    return ub
+
+
+def fluid_alpha(q, rho, derivative=False):
+    return _fluid(lib()).emu_fluid_alpha(q, rho, int(derivative))
+
+
+def fluid_apply(nx, ny, W, H, q, rho, x, clamp=False):
+    y = np.zeros_like(x)
+    _fluid(lib()).emu_fluid_apply(nx, ny, W, H, q, dp(np.ascontiguousarray(rho)), dp(np.ascontiguousarray(x)),
+                                  dp(y), int(clamp))
+    return y
+
+
+def fluid_objective(nx, ny, W, H, q, mu, rho, u):
+    return _fluid(lib()).emu_fluid_objective(nx, ny, W, H, q, mu, dp(np.ascontiguousarray(rho)),
+                                             dp(np.ascontiguousarray(u)))
+
+
+def fluid_gradient_rhs(nx, ny, W, H, q, rho, u):
+    b = np.zeros((nx + 1) * (ny + 1))
+    _fluid(lib()).emu_fluid_gradient_rhs(nx, ny, W, H, q, dp(np.ascontiguousarray(rho)),
+                                         dp(np.ascontiguousarray(u)), dp(b))
+    return b
+
+
+def p2_node_incidence(a, b, nx, ny):
+    t = (ctypes.c_longlong * 6)()
+    loc = (ctypes.c_int * 6)()
+    n = _fluid(lib()).emu_p2_node_incidence(a, b, nx, ny, t, loc)
+    return [(int(t[e]), int(loc[e])) for e in range(n)]

@@ -16,6 +16,8 @@
 #include "topo_p2.cuh"
 #include "topo_p1march.cuh"
 #include "topo_setup.h"
+#include "topo_fluid.cuh"
+#include "topo_fluid_setup.h"
 
 using namespace topo;
 
@@ -516,6 +518,135 @@ int emu_coarse_cheb(int nx, int ny, double hx, double hy, double eps2, int deg_f
   }
   for (int n = 0; n < nn; ++n) CoarseChebNode<double, 1>::finish(size_t(n), dc, xv.data(), x);
   return 0;
+}
+
+// ---- Stokes-Brinkman fluid: the kernels' triangle phases and gathers, run per
+// triangle / node in the kernels' order
+int emu_fluid_tables_doubles() { return int(sizeof(FluidTables) / sizeof(double)); }
+
+void emu_fluid_tables(double hx, double hy, double* out) {
+  FluidTables E;
+  fluid_tables(hx, hy, E);
+  std::memcpy(out, &E, sizeof(E));
+}
+
+// flows [nf][4] = side, center, length, rate
+int emu_fluid_bc(int nx, int ny, double W, double H, int nf, const double* flows, double* ub) {
+  std::vector<topo_flow> F(nf);
+  for (int f = 0; f < nf; ++f) {
+    F[f].side = int(flows[4 * f]);
+    F[f].center = flows[4 * f + 1];
+    F[f].length = flows[4 * f + 2];
+    F[f].rate = flows[4 * f + 3];
+  }
+  std::vector<double> v;
+  std::string msg;
+  if (fluid_boundary_values(nx, ny, W, H, F.data(), nf, v, msg)) return 1;
+  std::memcpy(ub, v.data(), v.size() * sizeof(double));
+  return 0;
+}
+
+static FluidPenal emu_fluid_penal(double q) {
+  FluidPenal pen;
+  pen.q = q;
+  pen.amin = 2.5 / (100.0 * 100.0);
+  pen.amax = 2.5 / (0.01 * 0.01);
+  return pen;
+}
+
+double emu_fluid_alpha(double q, double rho, int derivative) {
+  const FluidPenal pen = emu_fluid_penal(q);
+  return derivative ? pen.da(rho) : pen.a(rho);
+}
+
+void emu_fluid_apply(int nx, int ny, double W, double H, double q, const double* rho, const double* x, double* y,
+                     int clamp) {
+  FluidTables E;
+  fluid_tables(W / nx, H / ny, E);
+  const FluidPenal pen = emu_fluid_penal(q);
+  const size_t nt = size_t(2) * nx * ny, n2 = size_t(2 * nx + 1) * (2 * ny + 1), nv = size_t(nx + 1) * (ny + 1);
+  std::vector<double> mass(nt * kFluidMass), out(nt * kFluidOut);
+  for (size_t t = 0; t < nt; ++t) {
+    double r[3];
+    fluid_tri_rho(rho, nx, t, r);
+    fluid_tri_mass(E, pen, r, mass.data() + t * kFluidMass);
+  }
+  for (size_t t = 0; t < nt; ++t) {
+    size_t nd[6], vt[3];
+    fluid_tri_nodes(nx, t, nd);
+    fluid_tri_vertices(nx, t, vt);
+    double ue[6][2], pe[3];
+    for (int k = 0; k < 6; ++k) {
+      ue[k][0] = x[2 * nd[k]];
+      ue[k][1] = x[2 * nd[k] + 1];
+    }
+    for (int k = 0; k < 3; ++k) pe[k] = x[2 * n2 + vt[k]];
+    fluid_tri_apply(E, int(t & 1), mass.data() + t * kFluidMass, ue, pe, out.data() + t * kFluidOut);
+  }
+  const int NX = 2 * nx + 1;
+  for (size_t i = 0; i < n2; ++i) {
+    double v[2];
+    fluid_gather_node(out.data(), nx, ny, int(i % NX), int(i / NX), clamp != 0, x, v);
+    y[2 * i] = v[0];
+    y[2 * i + 1] = v[1];
+  }
+  for (size_t k = 0; k < nv; ++k)
+    y[2 * n2 + k] = fluid_gather_vertex(out.data(), nx, ny, int(k % (nx + 1)), int(k / (nx + 1)), kFluidOut, 12);
+}
+
+double emu_fluid_objective(int nx, int ny, double W, double H, double q, double mu, const double* rho,
+                           const double* u) {
+  FluidTables E;
+  fluid_tables(W / nx, H / ny, E);
+  const FluidPenal pen = emu_fluid_penal(q);
+  double s = 0.0;
+  for (size_t t = 0; t < size_t(2) * nx * ny; ++t) {
+    size_t nd[6];
+    fluid_tri_nodes(nx, t, nd);
+    double ue[6][2], r[3];
+    for (int k = 0; k < 6; ++k) {
+      ue[k][0] = u[2 * nd[k]];
+      ue[k][1] = u[2 * nd[k] + 1];
+    }
+    fluid_tri_rho(rho, nx, t, r);
+    s += fluid_tri_objective(E, pen, mu, int(t & 1), r, ue);
+  }
+  return 0.5 * s;
+}
+
+void emu_fluid_gradient_rhs(int nx, int ny, double W, double H, double q, const double* rho, const double* u,
+                            double* b) {
+  FluidTables E;
+  fluid_tables(W / nx, H / ny, E);
+  const FluidPenal pen = emu_fluid_penal(q);
+  const size_t nt = size_t(2) * nx * ny;
+  std::vector<double> tri3(3 * nt);
+  for (size_t t = 0; t < nt; ++t) {
+    size_t nd[6];
+    fluid_tri_nodes(nx, t, nd);
+    double ue[6][2], r[3], o3[3];
+    for (int k = 0; k < 6; ++k) {
+      ue[k][0] = u[2 * nd[k]];
+      ue[k][1] = u[2 * nd[k] + 1];
+    }
+    fluid_tri_rho(rho, nx, t, r);
+    fluid_tri_gradient(E, pen, r, ue, o3);
+    for (int k = 0; k < 3; ++k) tri3[3 * t + k] = o3[k];
+  }
+  for (size_t v = 0; v < size_t(nx + 1) * (ny + 1); ++v)
+    b[v] = fluid_gather_vertex(tri3.data(), nx, ny, int(v % (nx + 1)), int(v / (nx + 1)), 3, 0);
+}
+
+// incident (triangle, local node) pairs of P2 node (a, b); returns the count
+int emu_p2_node_incidence(int a, int b, int nx, int ny, long long* tri, int* loc) {
+  size_t t[6];
+  int l[6];
+  const int n = p2_node_incidence(a, b, nx, ny, t, l);
+  for (int e = 0; e < n; ++e) {
+    tri[e] = (long long)t[e];
+    loc[e] = l[e];
+  }
+  return n;
 }
 
 }  // extern "C"

@@ -1,0 +1,171 @@
+"""The fluid kernels' triangle phases and gathers (run on the CPU through the emulator)
+against the Stokes-Brinkman oracle (oracle/fluid.py).
+
+Covers the element tables and quadrature rules, the Dirichlet data of the flow
+profiles, the operator (with the continuity rows negated), its symmetry on
+interior velocities, the objective, the gradient's right-hand side, and the
+reduced-system closure the GPU solve computes (the oracle's ``pressure="mean"``).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.fem import Lattice, rule_degree6
+from oracle.fluid import (A_MAX, A_MIN, FluidDesign, FluidOracle, fluid_penalty, fluid_penalty_derivative,
+                          rule_degree7)
+from tests import emu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+TWIN = dict(Fluid=dict(domain_parameters=dict(width=1.5, height=1.0, fem_step_size=0.001, dem_step_size=0.001,
+                                              penalties=[0.01], volume_fraction=1 / 3),
+                       problem_parameters=dict(flows=[
+                           dict(side="Left", center=0.25, length=0.2, rate=1.0),
+                           dict(side="Left", center=0.75, length=0.2, rate=1.0),
+                           dict(side="Right", center=0.25, length=0.2, rate=-1.0),
+                           dict(side="Top", center=0.75, length=0.3, rate=-1.0)], viscosity=1.0)))
+
+
+def diffuser():
+    return FluidDesign.from_dict(json.load(open(os.path.join(GOLDEN, "designs", "diffuser.json"))))
+
+
+def setup(design, nx, ny, q=0.1, seed=0):
+    L = Lattice(design.width, design.height, nx, ny)
+    o = FluidOracle(L, design)
+    o.set_penalization(q)
+    rng = np.random.default_rng(seed)
+    rho = rng.uniform(0.0, 1.0, L.n_vertices)
+    return L, o, rho
+
+
+def test_quadrature_rules_and_tables_match_the_oracle():
+    L, o, _ = setup(diffuser(), 5, 4)
+    T = emu.fluid_tables(L.hx, L.hy)
+    lam6, w6 = rule_degree6()
+    lam7, w7 = rule_degree7()
+    assert np.array_equal(T["lam6"], lam6) and np.array_equal(T["w6"], w6)
+    assert np.max(np.abs(T["lam7"] - lam7)) < 4e-16 and np.max(np.abs(T["w7"] - w7)) < 4e-16
+    for k in (0, 1):
+        t = o.tab[k]
+        assert abs(T["area"] - t["area"]) < 1e-17
+        assert np.max(np.abs(T["dN6"][k] - t["dN6"])) < 1e-12
+        assert np.max(np.abs(T["lap"][k] - t["lap"])) < 1e-14
+        # grad[i][c][k] = int N_i d_c lambda_k ; the oracle stores (i, c, k) the same way
+        assert np.max(np.abs(T["grad"][k] - t["grad"])) < 1e-16
+        assert np.max(np.abs(T["div"][k] - t["div"])) < 1e-16
+
+
+def test_penalty_matches_the_reference_formula():
+    assert A_MIN == 2.5 / 100 ** 2 and A_MAX == 2.5 / 0.01 ** 2
+    for q in (0.01, 0.1, 1.0):
+        for r in (0.0, 0.3, 1.0, 0.999):
+            assert emu.fluid_alpha(q, r) == fluid_penalty(r, q)
+            assert emu.fluid_alpha(q, r, True) == fluid_penalty_derivative(r, q)
+
+
+@pytest.mark.parametrize("design,nx,ny", [("diffuser", 6, 6), ("twin", 9, 6), ("diffuser", 20, 20)])
+def test_boundary_data_match_the_oracle(design, nx, ny):
+    d = diffuser() if design == "diffuser" else FluidDesign.from_dict(TWIN)
+    L, o, _ = setup(d, nx, ny)
+    ub = emu.fluid_bc(nx, ny, d.width, d.height, d.flows)
+    ref = np.zeros(o.nuv)
+    ref[o.bc_dofs] = o.bc_vals
+    assert np.array_equal(ub, ref)
+
+
+def test_node_incidence_covers_every_triangle_node_once():
+    nx, ny = 4, 3
+    L = Lattice(1.0, 1.0, nx, ny)
+    seen = {}
+    for b in range(2 * ny + 1):
+        for a in range(2 * nx + 1):
+            for t, loc in emu.p2_node_incidence(a, b, nx, ny):
+                nodes = L.triangle_p2_nodes(t & 1)[t >> 1]
+                assert nodes[loc] == b * (2 * nx + 1) + a
+                seen[(t, loc)] = seen.get((t, loc), 0) + 1
+    assert len(seen) == 2 * nx * ny * 6 and set(seen.values()) == {1}
+
+
+def _oracle_operator(o, rho):
+    K = o.assemble(rho).tocsr().astype(np.float64)
+    S = np.ones(o.n)
+    S[o.nuv:] = -1.0  # the kernels negate the continuity rows
+    return K, S
+
+
+@pytest.mark.parametrize("design,nx,ny,q", [("diffuser", 6, 5, 0.1), ("twin", 9, 6, 0.01)])
+def test_operator_matches_the_assembled_oracle(design, nx, ny, q):
+    d = diffuser() if design == "diffuser" else FluidDesign.from_dict(TWIN)
+    L, o, rho = setup(d, nx, ny, q)
+    K, S = _oracle_operator(o, rho)
+    x = np.random.default_rng(3).standard_normal(o.n)
+    y = emu.fluid_apply(nx, ny, d.width, d.height, q, rho, x)
+    ref = S * (K @ x)
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+    # clamped: identity rows on the boundary velocity dofs, the rest unchanged
+    yc = emu.fluid_apply(nx, ny, d.width, d.height, q, rho, x, clamp=True)
+    bc = np.zeros(o.n, bool)
+    bc[o.bc_dofs] = True
+    assert np.array_equal(yc[bc], x[bc])
+    assert np.array_equal(yc[~bc], y[~bc])
+
+
+def test_clamped_operator_is_symmetric_on_interior_velocities():
+    d = diffuser()
+    nx = ny = 6
+    L, o, rho = setup(d, nx, ny)
+    rng = np.random.default_rng(4)
+    bc = np.zeros(o.n, bool)
+    bc[o.bc_dofs] = True
+    x, z = rng.standard_normal(o.n), rng.standard_normal(o.n)
+    x[bc] = 0.0
+    z[bc] = 0.0
+    a = z @ emu.fluid_apply(nx, ny, d.width, d.height, 0.1, rho, x, clamp=True)
+    b = x @ emu.fluid_apply(nx, ny, d.width, d.height, 0.1, rho, z, clamp=True)
+    assert abs(a - b) <= 1e-12 * abs(a)
+
+
+def test_objective_and_gradient_rhs_match_the_oracle():
+    d = diffuser()
+    nx, ny = 8, 8
+    L, o, rho = setup(d, nx, ny, q=0.1)
+    u, _ = o.state_solve(rho)
+    J = emu.fluid_objective(nx, ny, d.width, d.height, 0.1, d.viscosity, rho, u)
+    assert abs(J - o.objective(rho, u)) <= 1e-13 * abs(J)
+    b = emu.fluid_gradient_rhs(nx, ny, d.width, d.height, 0.1, rho, u)
+    ref = o.M1 @ o.gradient(rho, u)
+    assert np.max(np.abs(b - ref)) <= 1e-11 * np.max(np.abs(ref))
+
+
+def test_reduced_closure_reproduces_the_mean_oracle():
+    """The state solve's formulation on the CPU: right-hand side = minus the unclamped
+    operator on the lifted boundary data, boundary rows zero, continuity part centred;
+    the clamped operator solved on the zero-sum pressure subspace.  Equals the oracle's
+    ``pressure="mean"`` closure."""
+    d = diffuser()
+    nx = ny = 6
+    L = Lattice(d.width, d.height, nx, ny)
+    o = FluidOracle(L, d, pressure="mean")
+    o.set_penalization(0.1)
+    rho = np.random.default_rng(5).uniform(0.0, 1.0, L.n_vertices)
+    ub = emu.fluid_bc(nx, ny, d.width, d.height, d.flows)
+    lift = np.zeros(o.n)
+    lift[:o.nuv] = ub
+    rhs = -emu.fluid_apply(nx, ny, d.width, d.height, 0.1, rho, lift)
+    bc = np.zeros(o.n, bool)
+    bc[o.bc_dofs] = True
+    rhs[bc] = 0.0
+    rhs[o.nuv:] -= rhs[o.nuv:].mean()
+    A = np.stack([emu.fluid_apply(nx, ny, d.width, d.height, 0.1, rho, e, clamp=True) for e in np.eye(o.n)], axis=1)
+    # the zero-sum pressure closure: border with the constant pressure vector
+    c = np.zeros(o.n)
+    c[o.nuv:] = 1.0
+    Ab = np.block([[A, c[:, None]], [c[None, :], np.zeros((1, 1))]])
+    x = np.linalg.solve(Ab, np.concatenate([rhs, [0.0]]))[:o.n]
+    u = x[:o.nuv] + ub
+    uo, po = o.state_solve(rho)
+    assert np.max(np.abs(u - uo)) <= 1e-10 * np.max(np.abs(uo))
+    assert np.max(np.abs(x[o.nuv:] - po)) <= 1e-9 * np.max(np.abs(po))

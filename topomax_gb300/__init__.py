@@ -1,20 +1,20 @@
-"""topomax_gb300: the topomax elasticity design loop on one GB300 (sm_103a).
+"""topomax_gb300: the topomax FEM design loops on one GB300 (sm_103a).
 
 Reference-facing classes (same names and call surface as Emilinya/topomax):
-``ElasticityProblem``, ``HelmholtzFilter``, ``FEMSolver``/``Solver``,
+``ElasticityProblem``, ``FluidProblem``, ``HelmholtzFilter``, ``FEMSolver``/``Solver``,
 ``parse_design``.  The arithmetic runs in hand-written CUDA kernels behind the
 C ABI of ``include/topomax_gb300.h`` (``libtopomax_gb300.so``, built by
 ``topomax_gb300.build``).
 """
 from .designs import (DomainParameters, ElasticityParameters, Force, CircularRegion, Side, Traction,
                       parse_design, parse_design_dict)
-from .penalizers import ElasticPenalizer
+from .penalizers import ElasticPenalizer, FluidPenalizer
 from .problem import Problem
 
 __all__ = [
     "DomainParameters", "ElasticityParameters", "Force", "CircularRegion", "Side", "Traction", "parse_design",
-    "parse_design_dict", "ElasticPenalizer", "Problem", "ElasticityProblem", "HelmholtzFilter", "FEMSolver",
-    "Solver", "RectangleMesh", "FunctionSpace", "VectorFunctionSpace", "Function",
+    "parse_design_dict", "ElasticPenalizer", "FluidPenalizer", "Problem", "ElasticityProblem", "FluidProblem",
+    "HelmholtzFilter", "FEMSolver", "Solver", "RectangleMesh", "FunctionSpace", "VectorFunctionSpace", "Function",
 ]
 
 
@@ -24,6 +24,9 @@ def __getattr__(name):
                 "Function"):
         from . import fem
         return getattr(fem, name)
+    if name == "FluidProblem":
+        from . import fluid
+        return fluid.FluidProblem
     if name in ("FEMSolver", "Solver"):
         from . import solver
         return getattr(solver, name)

@@ -36,6 +36,9 @@ EXPORTED = [
     "topo_dem_energy_backward", "topo_dem_objective_gradient",
     "topo_density_filter_create", "topo_density_filter_destroy", "topo_density_filter_nnz",
     "topo_density_filter_apply",
+    "topo_fluid_create", "topo_fluid_destroy", "topo_fluid_last_error", "topo_fluid_sizes",
+    "topo_fluid_set_penalization", "topo_fluid_boundary_values", "topo_fluid_apply", "topo_fluid_state_solve",
+    "topo_fluid_objective", "topo_fluid_gradient_rhs", "topo_fluid_gradient", "topo_fluid_launch_count",
 ]
 
 
@@ -64,6 +67,11 @@ class LoadDesc(ctypes.Structure):
                 ("center_y", ctypes.c_double), ("radius", ctypes.c_double),
                 ("value_x", ctypes.c_double), ("value_y", ctypes.c_double),
                 ("n_tractions", ctypes.c_int), ("tractions", ctypes.POINTER(Traction))]
+
+
+class Flow(ctypes.Structure):
+    _fields_ = [("side", ctypes.c_int), ("center", ctypes.c_double), ("length", ctypes.c_double),
+                ("rate", ctypes.c_double)]
 
 
 class DemDesc(ctypes.Structure):
@@ -134,9 +142,24 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_density_filter_destroy.argtypes = [P]
     lib.topo_density_filter_nnz.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.topo_density_filter_apply.argtypes = [P, P, P, I, P]
+    lib.topo_fluid_create.restype = P
+    lib.topo_fluid_create.argtypes = [ctypes.POINTER(GridDesc), D, ctypes.POINTER(Flow), I, PI]
+    lib.topo_fluid_destroy.restype = None
+    lib.topo_fluid_destroy.argtypes = [P]
+    lib.topo_fluid_last_error.restype = ctypes.c_char_p
+    lib.topo_fluid_last_error.argtypes = [P]
+    lib.topo_fluid_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    lib.topo_fluid_set_penalization.argtypes = [P, D]
+    lib.topo_fluid_boundary_values.argtypes = [P, P, P]
+    lib.topo_fluid_apply.argtypes = [P, P, P, P, I, P]
+    lib.topo_fluid_state_solve.argtypes = [P, P, P, P, D, PI, P]
+    lib.topo_fluid_objective.argtypes = [P, P, P, P, P]
+    lib.topo_fluid_gradient_rhs.argtypes = [P, P, P, P, P]
+    lib.topo_fluid_gradient.argtypes = [P, P, P, P, D, PI, P]
+    lib.topo_fluid_launch_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     no_int = ("topo_create", "topo_create_filter", "topo_destroy", "topo_last_error", "topo_dem_create",
               "topo_dem_destroy", "topo_dem_last_error", "topo_density_filter_create",
-              "topo_density_filter_destroy")
+              "topo_density_filter_destroy", "topo_fluid_create", "topo_fluid_destroy", "topo_fluid_last_error")
     for name in EXPORTED:
         if name not in no_int:
             getattr(lib, name).restype = I

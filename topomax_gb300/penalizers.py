@@ -29,3 +29,22 @@ class ElasticPenalizer:
     def derivative(self, rho):
         p, m = self.assert_has_penalization(), self.minimum
         return p * rho ** (p - 1) * (1 - m)
+
+
+class FluidPenalizer(ElasticPenalizer):
+    """Brinkman inverse permeability alpha(rho) = a_max + (a_min - a_max) rho (1 + q) / (rho + q)
+    with a_min = 2.5 / 100^2 and a_max = 2.5 / 0.01^2 (the reference's src/penalizers.py:49-67);
+    the device evaluates it inside the fluid kernels."""
+
+    def __init__(self):
+        super().__init__()
+        self.minimum = 2.5 / 100 ** 2
+        self.maximum = 2.5 / 0.01 ** 2
+
+    def __call__(self, rho):
+        q, mini, maxi = self.assert_has_penalization(), self.minimum, self.maximum
+        return maxi + (mini - maxi) * rho * (1 + q) / (rho + q)
+
+    def derivative(self, rho):
+        q, mini, maxi = self.assert_has_penalization(), self.minimum, self.maximum
+        return (mini - maxi) * q * (1 + q) / (rho + q) ** 2

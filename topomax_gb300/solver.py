@@ -150,7 +150,8 @@ class FEMSolver(Solver):
             return ElasticityProblem(self.mesh, self.control_space, self.parameters, problem_parameters,
                                      precision=self.precision, rtol=self.rtol)
         if isinstance(problem_parameters, FluidParameters):
-            raise ValueError("the fluid problem is not part of this library")
+            from .fluid import FluidProblem
+            return FluidProblem(self.mesh, problem_parameters, self.parameters, rtol=self.rtol)
         raise ValueError(f"Got unknown problem '{self.parameters.problem}'")
 
     def to_array(self, rho) -> np.ndarray:
