@@ -32,7 +32,7 @@ def lib():
         E.emu_load.argtypes = [C_I, C_I, C_D, C_D, P_I, C_I, C_D, C_D, C_D, C_D, C_D, C_I, P_D, P_D]
         E.emu_vertex_weights.argtypes = [C_I, C_I, C_D, C_D, P_D]
         E.emu_smooth.argtypes = [C_I, C_I, C_I, C_I, C_I, C_D, C_D, C_D, C_D, C_D, C_D, P_I, P_D, P_D,
-                                 ctypes.POINTER(P_D), P_D, C_I, C_I, P_I, P_D, P_D, C_I]
+                                 ctypes.POINTER(P_D), P_D, C_I, C_I, P_I, P_D, P_D, C_I, P_D]
         _E = E
     return _E
 
@@ -148,7 +148,7 @@ MODE = {"pre": 2, "res": 3, "first": 4, "post2": 5}
 
 
 def smooth(mode, p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, NXc=1, NYc=1, dirc=None,
-           xc=None, bc=None, pmin=1e-6, stencil=False, march=False):
+           xc=None, bc=None, pmin=1e-6, stencil=False, march=False, kM=None):
     """Runs one fused smoothing step in place on bufs = dict(b, dinv, x, x2, r, d)."""
     arrs = [bufs[k] for k in ("b", "dinv", "x", "x2", "r", "d")]
     ptrs = (P_D * 6)(*[dp(a) for a in arrs])
@@ -158,7 +158,7 @@ def smooth(mode, p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, N
     lib().emu_smooth(int(p2), NC, MODE[mode], nx, ny, hx, hy, lam, mu, p, pmin, ip(dirv),
                      dp(xi) if xi is not None else None, dp(kK) if kK is not None else None, ptrs, dp(cheb),
                      NXc, NYc, ip(dirc), dp(xc) if xc is not None else None, dp(bc) if bc is not None else None,
-                     2 if march else int(stencil))
+                     2 if march else int(stencil), dp(kM) if kM is not None else None)
 
 
 def coarse_cheb(nx, ny, hx, hy, eps2, b, deg=0):

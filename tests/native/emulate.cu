@@ -269,7 +269,8 @@ int emu_transfer(int NC, int NXf, int NYf, const int* dirf, int NXc, int NYc, co
 // xc / dirc / NXc, NYc: the next coarser lattice (post1 source, resr target bc)
 int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, double lam, double mu, double p,
                double pmin, const int* dir, const double* xi, const double* kK, double* const* bufs,
-               const double* cheb, int NXc, int NYc, const int* dirc, const double* xc, double* bc, int stencil) {
+               const double* cheb, int NXc, int NYc, const int* dirc, const double* xc, double* bc, int stencil,
+               const double* kM) {
   SmoothBufs<double> B{bufs[0], bufs[1], bufs[2], bufs[3], bufs[4], bufs[5], cheb};
   Transfer X;
   X.NXf = p2 ? 2 * nx + 1 : nx + 1;
@@ -302,9 +303,9 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
         for (int b = 0; b < 3; ++b) P.Mm[o][a][b] = R.M1[o][a][b];
     }
     P.kK = kK;
-    P.kM = nullptr;
+    P.kM = K == 1 ? kM : nullptr;  // per-triangle mass coefficients (scalar levels), else 1
     P.kK_c = 0;
-    P.kM_c = K == 1 ? 1.0 : 0.0;
+    P.kM_c = (K == 1 && !kM) ? 1.0 : 0.0;
     auto sweep = [&](const auto& Q) {
       for (int b = 0; b <= ny; ++b)
         for (int a = 0; a <= nx; ++a) {

@@ -226,8 +226,8 @@ def test_p1_level_is_galerkin_projection_of_p2(nx, ny, sides):
     assert np.max(np.abs(z1[free] - y1[free])) <= 1e-12 * np.max(np.abs(y1))
 
 
-@pytest.mark.parametrize("NC", [1, 2])
-def test_p1_coarsening_is_galerkin_on_even_grids(NC):
+@pytest.mark.parametrize("NC,clamp_all", [(1, False), (2, False), (1, True)])
+def test_p1_coarsening_is_galerkin_on_even_grids(NC, clamp_all):
     nx, ny, hx, hy = 16, 8, 0.125, 0.125
     rng = np.random.default_rng(11)
     kf = rng.uniform(1e-3, 1.0, 2 * nx * ny)
@@ -236,6 +236,8 @@ def test_p1_coarsening_is_galerkin_on_even_grids(NC):
     dirv = emu.no_dir(nx + 1, ny + 1)
     if NC == 2:
         dirv[0] = 1
+    if clamp_all:  # the fluid velocity preconditioner's scalar levels: every side clamped
+        dirv = emu.make_dir(nx, ny, hx, hy, ["Left", "Right", "Top", "Bottom"])
     lv = emu.build_levels(False, nx, ny, hx, hy, dirv, NC)
     f, c = lv[0], lv[1]
     assert (c["nx"], c["ny"]) == (8, 4)
@@ -274,19 +276,23 @@ def test_level_chain_shapes():
 
 
 @pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil", "p1x2-march",
-                                   "p1x1-march"])
+                                   "p1x1-march", "p1x1-dir", "p1x1-dir-stencil", "p1x1-dir-march"])
 def test_fused_smoothing_steps_match_composition(level):
     """PRE / RES / FIRST / POST2 against the same steps composed from plain applies
-    (P1 levels also through their assembled 7-point stencil and the column march)."""
+    (P1 levels also through their assembled 7-point stencil and the column march).
+    The "-dir" scalar levels are the fluid velocity preconditioner's: every side
+    clamped, unit stiffness and a mass coefficient spanning six decades."""
     stencil = level.endswith("-stencil")
     march = level.endswith("-march")
-    level = level.replace("-stencil", "").replace("-march", "")
+    dirichlet = "-dir" in level
+    level = level.replace("-stencil", "").replace("-march", "").replace("-dir", "")
     nx, ny, hx, hy, p = 34, 10, 0.05, 0.05, 3.0
     lam, mu = lame(1.0, 0.3)
     rng = np.random.default_rng(21)
     xi = rng.uniform(0.05, 1.0, (nx + 1) * (ny + 1))
     p2 = level == "p2"
     NC = 1 if level == "p1x1" else 2
+    kM = None
     if p2:
         dirv = emu.make_dir(nx, ny, hx, hy, ["Left"])
         lv = emu.build_levels(True, nx, ny, hx, hy, dirv, 2)
@@ -297,10 +303,14 @@ def test_fused_smoothing_steps_match_composition(level):
         dirv = emu.no_dir(nx + 1, ny + 1)
         if NC == 2:
             dirv[0] = 1
+        if dirichlet:
+            dirv = emu.make_dir(nx, ny, hx, hy, ["Left", "Right", "Top", "Bottom"])
+            kM = 10.0 ** rng.uniform(-3.0, 3.0, 2 * nx * ny)
         lv = emu.build_levels(False, nx, ny, hx, hy, dirv, NC)
         f, c = lv[0], lv[1]
-        kK = emu.kappa(nx, ny, p, xi) if NC == 2 else np.full(2 * nx * ny, 0.05 ** 2)
-        A = lambda u: emu.p1_apply(NC, nx, ny, hx, hy, lam, mu, dirv, kK, None, u, kMc=1.0 if NC == 1 else 0.0)
+        kK = emu.kappa(nx, ny, p, xi) if NC == 2 else np.full(2 * nx * ny, 1.0 if dirichlet else 0.05 ** 2)
+        A = lambda u: emu.p1_apply(NC, nx, ny, hx, hy, lam, mu, dirv, kK, kM, u,
+                                   kMc=1.0 if NC == 1 and kM is None else 0.0)
     n = NC * f["NX"] * f["NY"]
     free = _free_rows(f["dir"], f["NX"], f["NY"], NC)
     b = rng.standard_normal(n) * free
@@ -312,14 +322,14 @@ def test_fused_smoothing_steps_match_composition(level):
     bufs = dict(b=b.copy(), dinv=dinv.copy(), x=x.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
     # PRE
     emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
-               march=march)
+               march=march, kM=kM)
     d0 = cheb[0] * dinv * b
     ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
     # RES
     bufs["x"] = x.copy()
     emu.smooth("res", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
-               march=march)
+               march=march, kM=kM)
     rr = b - A(x)
     assert np.max(np.abs(bufs["r"] - rr)) <= 1e-12 * np.max(np.abs(rr))
     # FIRST (coarse correction already added to x) then POST2
@@ -327,7 +337,7 @@ def test_fused_smoothing_steps_match_composition(level):
     u = x + emu.prolong(NC, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], xc)
     bufs["x"] = u.copy()
     emu.smooth("first", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
-               march=march)
+               march=march, kM=kM)
     r0 = b - A(u)
     dd0 = cheb[0] * dinv * r0
     # P2: FIRST stores w = u + d0 + c2 Dinv r0 for the second step (r is not needed)
@@ -336,7 +346,7 @@ def test_fused_smoothing_steps_match_composition(level):
         assert np.max(np.abs(bufs["r"] - r0)) <= 1e-12 * np.max(np.abs(r0))
     assert np.max(np.abs(bufs["x2"] - x2_ref)) <= 1e-12 * np.max(np.abs(x2_ref))
     emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
-               march=march)
+               march=march, kM=kM)
     r1 = r0 - A(dd0)
     ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
