@@ -1,7 +1,7 @@
 """FP64 CPU restatement of the Stokes-Brinkman fluid problem (test infrastructure only).
 
-The product has no fluid path yet; this oracle is its first piece, pinned against
-the reference's own known answer (``tests/test_fluid_solver.py``: the diffuser at
+The checker of the product's fluid path (csrc/topo_fluid.cu), pinned against the
+reference's own known answer (``tests/test_fluid_solver.py``: the diffuser at
 N = 20, penalty 0.1, objective 33.4987342021016 after 20 design steps).
 
 Follows ``FEM_src/fluid_problem.py:12-155`` and ``src/penalizers.py:49-67``:
@@ -22,10 +22,12 @@ above degree 6).  The pressure is determined up to a constant and the discrete
 boundary flux of the diffuser's interpolated outflow profile is not exactly zero
 (-1.7e-4 of 2/3): the reference hands that singular, slightly inconsistent system to
 MUMPS, whose answer depends on its pivoting.  ``pressure = "lsq"`` (default) takes the
-least-squares solution, ``"pin"`` drops the continuity row of vertex 0.  Parity is
-partial: the known answer's iteration count and exit condition are reproduced, its
-objective to 5.6e-4 (``lsq``; 1.4e-3 with ``pin``; no single dropped continuity row
-comes closer than 1.9e-4).
+least-squares solution of the whole system, ``"mean"`` that of the reduced system (the
+Dirichlet rows eliminated, the continuity right-hand side projected to zero sum, zero-sum
+pressure: the closure the GPU solver computes), ``"pin"`` drops the continuity row of
+vertex 0.  Parity is partial: the known answer's iteration count and exit condition are
+reproduced, its objective to 5.6e-4 (``lsq`` and ``mean``; 1.4e-3 with ``pin``; no
+single dropped continuity row comes closer than 1.9e-4).
 """
 from __future__ import annotations
 

@@ -10,6 +10,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 from oracle.fluid import FluidDesign, FluidOracle, FluidOracleSolver, rule_degree7
 
@@ -27,10 +28,13 @@ def test_degree7_rule_is_exact_to_degree_7():
             assert abs(got - exact) < 1e-14
 
 
-def test_diffuser_known_answer():
+@pytest.mark.parametrize("pressure", ["lsq", "mean"])
+def test_diffuser_known_answer(pressure):
+    """Both closures (the full system's least-squares solution, and the reduced system's
+    that the GPU solver computes) end the loop as the reference does."""
     ref = json.load(open(os.path.join(GOLDEN, "diffuser_N20.json")))
     d = FluidDesign.from_dict(json.load(open(os.path.join(GOLDEN, "designs", ref["design"]))))
-    s = FluidOracleSolver(ref["N"], d)
+    s = FluidOracleSolver(ref["N"], d, pressure=pressure)
     flux = s.oracle.boundary_flux()
     assert abs(flux) < 1e-3  # the interpolated outflow profile's mass defect (2/3 in, 2/3 out)
     run = s.solve()[0]
