@@ -9,6 +9,12 @@ CUDA events (an L2 flush before each) and prints one JSON line.  With
 ``--what solve`` it times whole warm state solves instead.  The timed
 launches are bracketed by cudaProfilerStart/Stop, so a profiler started with
 ``--profile-from-start off`` sees only them.
+
+``--what fluid --n N --reps K`` runs K design iterations of the Stokes-Brinkman
+diffuser (1 x 1, parabolic inflow on the left side, a three times faster outflow a
+third as wide on the right, penalty 0.1) at N cells per unit length through
+``FEMSolver`` and prints the wall time per design iteration and the state solve's
+Krylov iterations.
 """
 from __future__ import annotations
 
@@ -29,15 +35,44 @@ DESIGN = {"Elasticity": {
                                filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)}}
 
 
+FLUID = {"Fluid": {
+    "domain_parameters": dict(width=1.0, height=1.0, fem_step_size=0.0011, dem_step_size=0.0002, penalties=[0.1],
+                              volume_fraction=0.5),
+    "problem_parameters": dict(flows=[dict(side="Left", center=0.5, length=1.0, rate=1.0),
+                                      dict(side="Right", center=0.5, length=1.0 / 3.0, rate=-3.0)],
+                               viscosity=1.0)}}
+
+
+def time_fluid(args):
+    import time
+    from .solver import FEMSolver
+    s = FEMSolver(args.n, dict(FLUID, name="diffuser"), precision="fp64", rtol=1e-10, verbose=False, save=False,
+                  max_iterations=args.reps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h = s.solve()[0.1]
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    solves = len(h["objectives"])
+    print(json.dumps({"fluid": "diffuser design loop (FP64)", "N": args.n, "design_iterations": h["iterations"],
+                      "s_per_design_iteration": dt / max(1, h["iterations"]),
+                      "gmres_iterations_per_solve": s.problem.stats["state_iterations"] / solves,
+                      "objective": h["objectives"][-1], "exit": h["exit_condition"],
+                      "launches": s.problem.launch_count()}), flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--nx", type=int, default=1000)
     ap.add_argument("--ny", type=int, default=500)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--reps", type=int, default=20)
-    ap.add_argument("--what", default="operator", choices=["operator", "solve"],
-                    help="time operator launches, or whole warm state solves")
+    ap.add_argument("--what", default="operator", choices=["operator", "solve", "fluid"],
+                    help="time operator launches, whole warm state solves, or fluid design iterations")
+    ap.add_argument("--n", type=int, default=80, help="fluid: cells per unit length")
     args = ap.parse_args(argv)
+    if args.what == "fluid":
+        return time_fluid(args)
 
     dom, par = parse_design_dict(DESIGN)
     mesh = F.RectangleMesh(dom.width, dom.height, args.nx, args.ny)
