@@ -38,6 +38,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -76,6 +77,8 @@ def parse():
     ap.add_argument("--c2-steps", type=int, default=50,
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
     ap.add_argument("--cpu-sample", default="160x80,320x160", help="oracle grids timed for the CPU baseline")
+    ap.add_argument("--clocks-dir", default=None,
+                    help="keep the raw nvidia-smi samples of the timed region here (default: a temporary file)")
     args = ap.parse_args()
     if args.fp64_steps is None:
         args.fp64_steps = args.steps
@@ -169,9 +172,9 @@ def run_reference(args):
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
-    def __init__(self, tag):
+    def __init__(self, tag, out_dir=None):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"bench_clocks_{tag}.csv")
+        self.path = os.path.join(out_dir or tempfile.gettempdir(), f"bench_clocks_{tag}_{os.getpid()}.csv")
 
     def start(self, index):
         try:
@@ -352,7 +355,7 @@ def main():
 
     # --- mixed precision: value, roofline, launches
     prob = make("mixed")
-    clocks = Clocks(f"r{rank}")
+    clocks = Clocks(f"r{rank}", args.clocks_dir)
     barrier()
     clocks.start(local if not os.environ.get("CUDA_VISIBLE_DEVICES") else 0)
     times, objs, nlaunch, op_ms = device_loop(prob, args.steps, args.warmup, time_operator=True, profile=True)
