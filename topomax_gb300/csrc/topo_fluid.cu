@@ -335,6 +335,10 @@ int fluid_setup(topo_fluid_ctx* C, const double* rho, cudaStream_t s) {
     k_fluid_coarsen<<<C->grid(Cc.ntri()), kVecThreads, 0, s>>>(C->pK[l - 1], F.nx, F.ny, C->pK[l], Cc.nx, Cc.ny);
     ++C->launches;
   }
+  // both hierarchies' coefficients follow the design: choose their truncation and
+  // uniform-row shortcuts again
+  C->mgu.coefficients_changed();
+  C->mgp.coefficients_changed();
   int st = C->mgu.setup(s);
   if (!st) st = C->mgp.setup(s);
   if (st == -5) return C->fail(TOPO_ERR_CUDA, "fluid preconditioner set-up: CUDA error");

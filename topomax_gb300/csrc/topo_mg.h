@@ -131,6 +131,11 @@ class MG {
   }
   // constant mass coefficient on level 0 when it is P1 (filter)
   int setup(cudaStream_t s);  // diagonals, eigen bounds, coarse inverse
+  // The coarse-Chebyshev truncation and the shared interior stencil rows are
+  // chosen from the coefficients at the first setup() (a filter's never
+  // change); a caller whose scalar coefficients change between setups calls
+  // this first so that the next setup() chooses them again.
+  void coefficients_changed() { cc_selected_ = false; }
   // y = A_l x; on level 0, op selects the Krylov operator instead of the
   // preconditioner's (they differ only where the penalisation is clamped)
   void apply(int l, const T* x, T* y, cudaStream_t s, bool op = false);
