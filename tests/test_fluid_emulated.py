@@ -3,14 +3,17 @@ against the Stokes-Brinkman oracle (oracle/fluid.py).
 
 Covers the element tables and quadrature rules, the Dirichlet data of the flow
 profiles, the operator (with the continuity rows negated), its symmetry on
-interior velocities, the objective, the gradient's right-hand side, and the
-reduced-system closure the GPU solve computes (the oracle's ``pressure="mean"``).
+interior velocities, the objective, the gradient's right-hand side, the
+reduced-system closure the GPU solve computes (the oracle's ``pressure="mean"``),
+and the block-preconditioned flexible GMRES of the state solve run with the
+emulated multigrid phases.
 """
 import json
 import os
 
 import numpy as np
 import pytest
+import scipy.linalg
 
 from oracle.fem import Lattice, rule_degree6
 from oracle.fluid import (A_MAX, A_MIN, FluidDesign, FluidOracle, fluid_penalty, fluid_penalty_derivative,
@@ -29,7 +32,8 @@ TWIN = dict(Fluid=dict(domain_parameters=dict(width=1.5, height=1.0, fem_step_si
 
 
 def diffuser():
-    return FluidDesign.from_dict(json.load(open(os.path.join(GOLDEN, "designs", "diffuser.json"))))
+    with open(os.path.join(GOLDEN, "designs", "diffuser.json")) as f:
+        return FluidDesign.from_dict(json.load(f))
 
 
 def setup(design, nx, ny, q=0.1, seed=0):
@@ -169,3 +173,142 @@ def test_reduced_closure_reproduces_the_mean_oracle():
     uo, po = o.state_solve(rho)
     assert np.max(np.abs(u - uo)) <= 1e-10 * np.max(np.abs(uo))
     assert np.max(np.abs(x[o.nuv:] - po)) <= 1e-9 * np.max(np.abs(po))
+
+
+def _cheb(lmax, lo_frac=0.1):
+    """Degree-2 Chebyshev coefficients of the smoothing steps on [lo_frac, 1.1] * lmax."""
+    hi, lo = 1.1 * lmax, lo_frac * lmax
+    th, de = 0.5 * (hi + lo), 0.5 * (hi - lo)
+    sg = th / de
+    r0 = 1 / sg
+    r1 = 1 / (2 * sg - r0)
+    return 1 / th, r1 * r0, 2 * r1 / de
+
+
+class _VCycle:
+    """One V-cycle of the scalar P1 hierarchy as the multigrid runs it (Chebyshev degree 2
+    pre/post smoothing on coefficients coarsened level by level, the kernels' transfers,
+    an exact coarsest solve), built from the emulated kernel phases."""
+
+    def __init__(self, nx, ny, hx, hy, dirv, kK, kM):
+        self.lv = emu.build_levels(False, nx, ny, hx, hy, dirv, 1)
+        self.ops = []
+        for l, L in enumerate(self.lv):
+            if l > 0:
+                F = self.lv[l - 1]
+                kK = emu.coarsen_kappa(kK, F["nx"], F["ny"], L["nx"], L["ny"])
+                kM = emu.coarsen_kappa(kM, F["nx"], F["ny"], L["nx"], L["ny"])
+            n = L["NX"] * L["NY"]
+            hl = (hx * nx / L["nx"], hy * ny / L["ny"])
+            A = np.stack([emu.p1_apply(1, L["nx"], L["ny"], *hl, 0, 0, L["dir"], kK, kM, e) for e in np.eye(n)], 1)
+            dinv = 1 / np.diag(A)
+            v = np.random.default_rng(0).standard_normal(n)
+            for _ in range(30):
+                w = dinv * (A @ v)
+                lm = np.linalg.norm(w) / np.linalg.norm(v)
+                v = w / np.linalg.norm(w)
+            last = l == len(self.lv) - 1
+            self.ops.append(dict(A=A, dinv=dinv, c=_cheb(lm), lu=scipy.linalg.lu_factor(A) if last else None))
+
+    def __call__(self, b, l=0):
+        o = self.ops[l]
+        if o["lu"] is not None:
+            return scipy.linalg.lu_solve(o["lu"], b)
+        A, Di, (c0, c1, c2) = o["A"], o["dinv"], o["c"]
+        d0 = c0 * Di * b
+        x = d0 + c1 * d0 + c2 * Di * (b - A @ d0)
+        f, c = self.lv[l], self.lv[l + 1]
+        rc = emu.restrict(1, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], b - A @ x)
+        u = x + emu.prolong(1, f["NX"], f["NY"], f["dir"], c["NX"], c["NY"], c["dir"], self(rc, l + 1))
+        r0 = b - A @ u
+        dd = c0 * Di * r0
+        return u + dd + c1 * dd + c2 * Di * (r0 - A @ dd)
+
+
+def _fgmres(A, P, b, m=30, tol=1e-12, maxit=1000):
+    """Flexible GMRES(m), right preconditioned, stopping on the true residual."""
+    x = np.zeros_like(b)
+    bn = np.linalg.norm(b)
+    its = 0
+    while True:
+        r = b - A(x)
+        beta = np.linalg.norm(r)
+        if beta <= tol * bn or its >= maxit:
+            return x, its, beta / bn
+        V, Z = [r / beta], []
+        H = np.zeros((m + 1, m))
+        for j in range(m):
+            Z.append(P(V[j]))
+            w = A(Z[j])
+            its += 1
+            for _ in range(2):
+                for i in range(j + 1):
+                    h = V[i] @ w
+                    H[i, j] += h
+                    w = w - h * V[i]
+            H[j + 1, j] = np.linalg.norm(w)
+            V.append(w / H[j + 1, j])
+            e1 = np.zeros(j + 2)
+            e1[0] = beta
+            y = np.linalg.lstsq(H[:j + 2, :j + 1], e1, rcond=None)[0]
+            if np.linalg.norm(H[:j + 2, :j + 1] @ y - e1) <= 0.5 * tol * bn or its >= maxit:
+                break
+        x = x + np.stack(Z, 1) @ y
+
+
+def test_block_preconditioned_solve_reaches_the_oracle_closure():
+    """The state solve's algorithm run with the emulated kernel phases: right-hand side and
+    clamped operator as the kernels compute them, the block-diagonal preconditioner (one
+    V-cycle of K + alpha M per velocity component on the (2nx)x(2ny) lattice, lumped mass +
+    one V-cycle of the 1/alpha-weighted Laplacian with a 1e-3 mass shift for the pressure),
+    flexible GMRES(30).  Converges to the oracle's reduced-system closure on a 0/1 design
+    (alpha from 2.5e-4 to 2.5e4) in a few hundred iterations at most."""
+    d = diffuser()
+    N, q = 8, 0.1
+    L = Lattice(1.0, 1.0, N, N)
+    o = FluidOracle(L, d, pressure="mean")
+    o.set_penalization(q)
+    X, Y = L.vertex_coords()
+    rho = np.where(np.abs(Y - 0.5) < 0.5 - X / 3.0, 1.0, 0.0)
+    nuv = o.nuv
+    ub = emu.fluid_bc(N, N, 1.0, 1.0, d.flows)
+    lift = np.zeros(o.n)
+    lift[:nuv] = ub
+    rhs = -emu.fluid_apply(N, N, 1.0, 1.0, q, rho, lift)
+    bc = np.zeros(o.n, bool)
+    bc[o.bc_dofs] = True
+    rhs[bc] = 0.0
+    rhs[nuv:] -= rhs[nuv:].mean()
+    # preconditioner coefficients as the set-up kernels compute them
+    R = rho.reshape(N + 1, N + 1)
+    Rf = np.zeros((2 * N + 1, 2 * N + 1))
+    Rf[0::2, 0::2] = R
+    Rf[0::2, 1::2] = 0.5 * (R[:, :-1] + R[:, 1:])
+    Rf[1::2, 0::2] = 0.5 * (R[:-1, :] + R[1:, :])
+    Rf[1::2, 1::2] = 0.5 * (R[:-1, :-1] + R[1:, 1:])
+    L2 = Lattice(1.0, 1.0, 2 * N, 2 * N)
+    km = np.zeros(2 * (2 * N) ** 2)
+    kk = np.zeros(2 * N * N)
+    for t in (0, 1):
+        km[t::2] = fluid_penalty(Rf.ravel()[L2.triangle_vertices(t)].mean(axis=1), q)
+        kk[t::2] = 1.0 / fluid_penalty(rho[L.triangle_vertices(t)].mean(axis=1), q)
+    vel = _VCycle(2 * N, 2 * N, 0.5 / N, 0.5 / N, emu.make_dir(2 * N, 2 * N, 0.5 / N, 0.5 / N,
+                                                               ["Left", "Right", "Top", "Bottom"]), np.ones_like(km), km)
+    pre = _VCycle(N, N, 1.0 / N, 1.0 / N, emu.no_dir(N + 1, N + 1), kk, np.full_like(kk, 1e-3))
+    ml = emu.vertex_weights(N, N, 1.0 / N, 1.0 / N)
+    nb = bc[0:nuv:2]
+
+    def P(r):
+        z = np.zeros_like(r)
+        for c in (0, 1):
+            z[c:nuv:2] = np.where(nb, 0.0, vel(np.where(nb, 0.0, r[c:nuv:2])))
+        rp = r[nuv:]
+        zp = rp / ml + pre(rp - rp.mean())
+        z[nuv:] = zp - zp.mean()
+        return z
+
+    x, its, rel = _fgmres(lambda v: emu.fluid_apply(N, N, 1.0, 1.0, q, rho, v, clamp=True), P, rhs)
+    assert rel <= 1e-12 and its <= 400
+    u_ref, p_ref = o.state_solve(rho)
+    assert np.max(np.abs(x[:nuv] + ub - u_ref)) <= 1e-10 * np.max(np.abs(u_ref))
+    assert np.max(np.abs(x[nuv:] - p_ref)) <= 1e-9 * np.max(np.abs(p_ref))
