@@ -10,7 +10,8 @@ It reads, without importing any reference module:
 * ``designs/*.json`` (elasticity designs) -> ``tests/golden/designs/``;
 * ``tests/test_data/FEM/triangle/data/correct_{data,rho}.dat`` -- the
   known answer of ``tests/test_elasticity_solver.py:30-55`` -- through an
-  unpickler restricted to numpy types -> ``tests/golden/triangle_N10.json``;
+  unpickler restricted to numpy types -> ``tests/golden/triangle_N10.json`` (the saved
+  design vector kept in its file order: dolfin's serial CG1 dof order);
 * ``tests/test_data/DEM/{short_cantilever,bridge}/problem_data.dat`` -- the
   known answers of ``tests/test_DEM_problem.py:14-43`` ->
   ``tests/golden/dem_<design>.npz``;
@@ -91,7 +92,10 @@ def main():
         "penalty": float(data["penalty"]),
         "rho_sorted": np.sort(vec).tolist(),
         "rho_sum": float(vec.sum()),
-        "note": "rho is in dolfin dof order in the reference; compared sorted",
+        "rho_dolfin": vec.tolist(),
+        "domain_size": [float(x) for x in rho["domain_size"]],
+        "problem": str(rho["problem"]),
+        "note": "rho_dolfin is the reference's saved design vector (dolfin's serial CG1 dof order)",
     }
     with open(os.path.join(HERE, "triangle_N10.json"), "w") as f:
         json.dump(out, f, indent=1)
@@ -108,7 +112,10 @@ def main():
         json.dump({"design": "diffuser.json", "N": int(rho["N"]), "objective": float(rec.objective),
                    "iteration": int(rec.iteration), "penalty": float(rec.penalty),
                    "rho_sorted": np.sort(vec).tolist(), "rho_sum": float(vec.sum()),
-                   "note": "rho is in dolfin dof order in the reference; compared sorted"}, f, indent=1)
+                   "rho_dolfin": vec.tolist(), "domain_size": [float(x) for x in rho["domain_size"]],
+                   "problem": str(rho["problem"]),
+                   "note": "rho_dolfin is the reference's saved design vector (dolfin's serial CG1 dof order)"},
+                  f, indent=1)
 
     for design in ("short_cantilever", "bridge"):
         p = os.path.join(REF, "tests", "test_data", "DEM", design, "problem_data.dat")

@@ -165,6 +165,17 @@ def test_triangle_known_answer(precision, tmp_path):
     rho = np.sort(s.to_array(s.rho))
     assert np.max(np.abs(rho - np.array(gold["rho_sorted"]))) <= 1e-5
     assert os.path.isfile(os.path.join(tmp_path, "FEM", "triangle", "data", "N=10_p=3.0_k=24.dat"))
+    # the saved design is the reference's own file (FEM_src/utils.py:47-69): same keys, the
+    # vector in dolfin's dof order, matching the reference's saved correct_rho.dat
+    import pickle
+    from topomax_gb300.fem import load_function
+    path = os.path.join(tmp_path, "FEM", "triangle", "data", "N=10_p=3.0_k=24_rho.dat")
+    with open(path, "rb") as f:
+        rec = pickle.load(f)
+    assert set(rec) == {"N", "domain_size", "problem", "vector"} and rec["N"] == 10
+    assert np.max(np.abs(np.asarray(rec["vector"]) - np.array(gold["rho_dolfin"]))) <= 1e-5
+    f, mesh, V = load_function(path)
+    assert np.array_equal(f.vector()[:], s.to_array(s.rho))
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])

@@ -17,6 +17,7 @@ node (a, b) at b*(2nx+1)+a with components interleaved.
 from __future__ import annotations
 
 import ctypes
+import pickle
 
 import numpy as np
 import torch
@@ -146,6 +147,85 @@ class Function:
 
     def copy(self):
         return Function(self._V, self.tensor.clone())
+
+
+def dolfin_cg1_order(nx: int, ny: int) -> np.ndarray:
+    """Lattice index of every CG1 dof in the order the reference's (serial) dolfin numbers
+    them on its RectangleMesh with the "right" diagonal: a level structure grown from the
+    top-left vertex -- vertex (i, j) on level i + (ny - j) -- with x increasing inside a
+    level.  It reproduces the design vectors the reference saves
+    (tests/test_data/FEM/{triangle,diffuser}/data/correct_rho.dat, 1 x 1 at N = 10 and 20);
+    on other rectangles the same two corners are the mesh graph's only pair at maximal
+    distance, and the same rule is assumed."""
+    I, J = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1))
+    I, J = I.ravel(), J.ravel()
+    return (J * (nx + 1) + I)[np.lexsort((I, I + (ny - J)))]
+
+
+def to_dolfin_order(values, nx: int, ny: int) -> np.ndarray:
+    """CG1 values in lattice order -> dolfin's dof order."""
+    return np.asarray(values)[dolfin_cg1_order(nx, ny)]
+
+
+def from_dolfin_order(values, nx: int, ny: int) -> np.ndarray:
+    """CG1 values in dolfin's dof order -> lattice order."""
+    v = np.asarray(values)
+    out = np.empty_like(v)
+    out[dolfin_cg1_order(nx, ny)] = v
+    return out
+
+
+def mesh_to_N(mesh: RectangleMesh) -> int:
+    """Cells per unit length (FEM_src/utils.py:29-37: 1 / (hmin / sqrt 2))."""
+    N = 1 / (mesh.hmin() / np.sqrt(2))
+    if abs(N - int(round(N))) / N > 1e-10:
+        print(f"save_function: got non-integer N: {N}, this could result in wrong data getting saved")
+    return int(round(N))
+
+
+def mesh_to_domain_size(mesh: RectangleMesh) -> tuple:
+    """Largest vertex coordinates (FEM_src/utils.py:40-44), as the mesh computes them."""
+    return (0.0 + mesh.nx * (mesh.width / mesh.nx), 0.0 + mesh.ny * (mesh.height / mesh.ny))
+
+
+def design_record(values, mesh: RectangleMesh, N: int | None = None, domain_size=None) -> dict:
+    """The pickled record of a CG1 design (FEM_src/utils.py:47-69 ``save_function``):
+    N, domain size, problem "design" and the vector in dolfin's dof order."""
+    return {"N": mesh_to_N(mesh) if N is None else N,
+            "domain_size": mesh_to_domain_size(mesh) if domain_size is None else domain_size,
+            "problem": "design", "vector": to_dolfin_order(values, mesh.nx, mesh.ny)}
+
+
+def save_function(f: "Function", filename: str, problem: str = "design", N: int | None = None,
+                  domain_size=None):
+    """``save_function`` (FEM_src/utils.py:47-69) for CG1 designs: the reference's pickle,
+    the vector in dolfin's dof order, readable by the reference's ``load_function``."""
+    V = f.function_space()
+    if V.vector or V.degree != 1 or problem != "design":
+        raise ValueError("save_function writes CG1 designs (problem 'design')")
+    with open(filename, "wb") as datafile:
+        pickle.dump(design_record(f.vector()[:], V.mesh(), N, domain_size), datafile)
+
+
+def load_function(filename: str, mesh: RectangleMesh | None = None, function_space: FunctionSpace | None = None):
+    """``load_function`` (FEM_src/utils.py:72-109) for design files -- the reference's own
+    or this package's: returns (Function, mesh, function space), the vector in lattice order."""
+    with open(filename, "rb") as datafile:
+        data = pickle.load(datafile)
+    if data["problem"] != "design":
+        raise ValueError(f"load_function reads CG1 designs; got problem '{data['problem']}'")
+    if mesh is None:
+        w, h = data["domain_size"]
+        mesh = RectangleMesh(w, h, int(w * data["N"]), int(h * data["N"]))
+    if function_space is None:
+        function_space = FunctionSpace(mesh, "CG", 1)
+    m = function_space.mesh()
+    values = np.asarray(data["vector"], dtype=np.float64)
+    if values.size != function_space.dim():
+        raise ValueError(f"design vector of {values.size} values does not fit {function_space.dim()} vertices")
+    f = Function(function_space)
+    f.vector()[:] = from_dolfin_order(values, m.nx, m.ny)
+    return f, mesh, function_space
 
 
 def as_cg1_tensor(value, V: FunctionSpace) -> torch.Tensor:

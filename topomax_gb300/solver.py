@@ -19,7 +19,7 @@ import torch
 from . import _capi
 from .designs import ElasticityParameters, FluidParameters, parse_design, parse_design_dict
 from .fem import (DEFAULT_RTOL, ElasticityProblem, Function, FunctionSpace, RectangleMesh, _device, _ptr,
-                  _stream, as_cg1_tensor)
+                  _stream, as_cg1_tensor, design_record)
 from .utils import IterationData, SolverResult, Timer
 
 
@@ -168,10 +168,10 @@ class FEMSolver(Solver):
         return float(out.item())
 
     def save_rho(self, rho, file_root: str):
+        """FEM_src/solver.py:86-89: the design in the reference's pickle, dolfin's dof order."""
         rho_file = file_root + "_rho.dat"
         with open(rho_file, "wb") as f:
-            pickle.dump({"N": self.full_N, "domain_size": (self.width, self.height), "problem": "design",
-                         "vector": self.to_array(rho), "order": "lattice"}, f)
+            pickle.dump(design_record(self.to_array(rho), self.mesh), f)
         return os.path.basename(rho_file)
 
     # -- EMD ------------------------------------------------------------------
