@@ -7,7 +7,7 @@ Run in a container where the reference checkout is mounted (default path
 
 It reads, without importing any reference module:
 
-* ``designs/*.json`` (elasticity designs) -> ``tests/golden/designs/``;
+* ``designs/*.json`` (elasticity and fluid designs) -> ``tests/golden/designs/``;
 * ``tests/test_data/FEM/triangle/data/correct_{data,rho}.dat`` -- the
   known answer of ``tests/test_elasticity_solver.py:30-55`` -- through an
   unpickler restricted to numpy types -> ``tests/golden/triangle_N10.json`` (the saved
@@ -75,7 +75,7 @@ def main():
             continue
         with open(os.path.join(REF, "designs", name)) as f:
             d = json.load(f)
-        if "Elasticity" not in d:
+        if "Elasticity" not in d and "Fluid" not in d:
             continue
         with open(os.path.join(HERE, "designs", name), "w") as f:
             json.dump(d, f, indent=2)

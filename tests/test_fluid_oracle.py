@@ -69,3 +69,26 @@ def test_state_solution_is_divergence_free_and_meets_the_boundary_data():
         dr = fluid_penalty_derivative(o._rho_at(rho, t, t["lam7"]), 0.1)
         rhs += float(np.sum(0.5 * dr * np.sum(uq * uq, axis=2) * t["w7"][None] * t["area"]))
     assert abs(total - rhs) <= 1e-10 * abs(rhs)
+
+
+def test_twin_pipe_gradient_matches_finite_differences():
+    """tests/test_fluid_gradient.py of the reference, on the oracle: the twin pipe at N = 10,
+    penalty 0.1, forward differences of the objective along the constant direction
+    volume / volume_fraction against int 1/2 alpha'(rho) direction |u|^2 dx, at t = 1e-3 and
+    1e-7.  The reference's check is kept as it is written: ``Polynomial.fit`` works in a
+    scaled variable, so its ``coef[1] >= 4`` asks for a log-log slope of at least
+    4 / 4.6 (4.6 = half the width of log t over the two steps), i.e. first order."""
+    with open(os.path.join(GOLDEN, "designs", "twin_pipe.json")) as f:
+        d = FluidDesign.from_dict(json.load(f))
+    s = FluidOracleSolver(10, d)
+    o = s.oracle
+    s.problem.set_penalization(0.1)
+    rho = s.rho.copy()
+    J = s.problem.calculate_objective(rho)
+    direction = np.full_like(rho, s.volume / d.volume_fraction)
+    gradient = float(direction @ (o.M1 @ o.gradient(rho, s.problem.u)))
+    ts = [1e-3, 1e-7]
+    errors = [abs((s.problem.calculate_objective(rho + t * direction) - J) / t - gradient) for t in ts]
+    poly = np.polynomial.Polynomial.fit(np.log(ts), np.log(errors), 1)
+    assert poly.coef[1] >= 4
+    assert poly.convert().coef[1] > 0.9  # the plain slope: first-order forward differences

@@ -97,3 +97,23 @@ def test_fluid_design_loop_matches_oracle_and_known_answer(tmp_path):
     assert h["exit_condition"] == "Convergence treshold reached"
     assert abs(h["objectives"][-1] - orun.objectives[-1]) <= 1e-6 * abs(orun.objectives[-1])
     assert abs(h["objectives"][-1] - ref["objective"]) <= 1e-3 * ref["objective"]
+
+
+def test_twin_pipe_gradient_matches_finite_differences(tmp_path):
+    """tests/test_fluid_gradient.py of the reference, through FEMSolver on the GPU: forward
+    differences of the objective along volume / volume_fraction against
+    int 1/2 alpha'(rho) direction |u|^2 dx at t = 1e-3 and 1e-7, with the reference's
+    own (scaled-variable) fit."""
+    import torch
+    from topomax_gb300.solver import FEMSolver
+    s = FEMSolver(10, os.path.join(GOLDEN, "designs", "twin_pipe.json"), data_path=str(tmp_path),
+                  precision="fp64", rtol=1e-13, verbose=False, save=False)
+    s.problem.set_penalization(0.1)
+    rho = s.rho.tensor.clone()
+    J = s.problem.calculate_objective(rho)
+    direction = torch.full_like(rho, s.volume / s.parameters.volume_fraction)
+    gradient = float(torch.dot(s.problem.gradient_rhs(rho, s.problem.u), direction))
+    ts = [1e-3, 1e-7]
+    errors = [abs((s.problem.calculate_objective(rho + t * direction) - J) / t - gradient) for t in ts]
+    poly = np.polynomial.Polynomial.fit(np.log(ts), np.log(errors), 1)
+    assert poly.coef[1] >= 4

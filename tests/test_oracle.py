@@ -26,6 +26,12 @@ def test_triangle_known_answer():
     assert abs(run.objectives[-1] - gold["objective"]) <= 1e-12 * gold["objective"]
     assert np.max(np.abs(np.sort(run.rho) - np.array(gold["rho_sorted"]))) <= 1e-10
     assert abs(run.rho.sum() - gold["rho_sum"]) <= 1e-10
+    # the reference's own bar (tests/test_elasticity_solver.py:54-55): int (rho - rho*)^2 dx
+    # < 1e-14 against its saved design, read in dolfin's dof order
+    from topomax_gb300.fem import from_dolfin_order
+    e = np.asarray(run.rho) - from_dolfin_order(np.asarray(gold["rho_dolfin"]), 10, 10)
+    M1 = FEMOracle(Lattice(1.0, 1.0, 10, 10), d).M1
+    assert float(e @ (M1 @ e)) < 1e-14
 
 
 @pytest.mark.parametrize("rule", [rule_degree5, rule_degree6])
