@@ -22,18 +22,26 @@ from tests import emu
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
-TWIN = dict(Fluid=dict(domain_parameters=dict(width=1.5, height=1.0, fem_step_size=0.001, dem_step_size=0.001,
-                                              penalties=[0.01], volume_fraction=1 / 3),
-                       problem_parameters=dict(flows=[
-                           dict(side="Left", center=0.25, length=0.2, rate=1.0),
-                           dict(side="Left", center=0.75, length=0.2, rate=1.0),
-                           dict(side="Right", center=0.25, length=0.2, rate=-1.0),
-                           dict(side="Top", center=0.75, length=0.3, rate=-1.0)], viscosity=1.0)))
+# four flows on three sides (two on one side, one on the top): exercises every branch of
+# the flow profiles and the no-slip override at the corners
+MIXED = dict(Fluid=dict(domain_parameters=dict(width=1.5, height=1.0, fem_step_size=0.001, dem_step_size=0.001,
+                                               penalties=[0.01], volume_fraction=1 / 3),
+                        problem_parameters=dict(flows=[
+                            dict(side="Left", center=0.25, length=0.2, rate=1.0),
+                            dict(side="Left", center=0.75, length=0.2, rate=1.0),
+                            dict(side="Right", center=0.25, length=0.2, rate=-1.0),
+                            dict(side="Top", center=0.75, length=0.3, rate=-1.0)], viscosity=1.0)))
+
+
+def design(name):
+    if name == "mixed":
+        return FluidDesign.from_dict(MIXED)
+    with open(os.path.join(GOLDEN, "designs", f"{name}.json")) as f:
+        return FluidDesign.from_dict(json.load(f))
 
 
 def diffuser():
-    with open(os.path.join(GOLDEN, "designs", "diffuser.json")) as f:
-        return FluidDesign.from_dict(json.load(f))
+    return design("diffuser")
 
 
 def setup(design, nx, ny, q=0.1, seed=0):
@@ -70,9 +78,10 @@ def test_penalty_matches_the_reference_formula():
             assert emu.fluid_alpha(q, r, True) == fluid_penalty_derivative(r, q)
 
 
-@pytest.mark.parametrize("design,nx,ny", [("diffuser", 6, 6), ("twin", 9, 6), ("diffuser", 20, 20)])
-def test_boundary_data_match_the_oracle(design, nx, ny):
-    d = diffuser() if design == "diffuser" else FluidDesign.from_dict(TWIN)
+@pytest.mark.parametrize("name,nx,ny", [("diffuser", 6, 6), ("mixed", 9, 6), ("diffuser", 20, 20),
+                                         ("twin_pipe", 15, 10), ("pipe_bend", 10, 10)])
+def test_boundary_data_match_the_oracle(name, nx, ny):
+    d = design(name)
     L, o, _ = setup(d, nx, ny)
     ub = emu.fluid_bc(nx, ny, d.width, d.height, d.flows)
     ref = np.zeros(o.nuv)
@@ -100,9 +109,9 @@ def _oracle_operator(o, rho):
     return K, S
 
 
-@pytest.mark.parametrize("design,nx,ny,q", [("diffuser", 6, 5, 0.1), ("twin", 9, 6, 0.01)])
-def test_operator_matches_the_assembled_oracle(design, nx, ny, q):
-    d = diffuser() if design == "diffuser" else FluidDesign.from_dict(TWIN)
+@pytest.mark.parametrize("name,nx,ny,q", [("diffuser", 6, 5, 0.1), ("mixed", 9, 6, 0.01), ("pipe_bend", 7, 7, 0.1)])
+def test_operator_matches_the_assembled_oracle(name, nx, ny, q):
+    d = design(name)
     L, o, rho = setup(d, nx, ny, q)
     K, S = _oracle_operator(o, rho)
     x = np.random.default_rng(3).standard_normal(o.n)
