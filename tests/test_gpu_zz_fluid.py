@@ -2,7 +2,8 @@
 
 Opt-in (TOPO_FLUID_GPU=1) until the fluid solver has run on a GB300: its kernels'
 triangle phases and gathers, and the formulation of the state solve, are checked on
-the CPU in test_fluid_emulated.py.
+the CPU in test_fluid_emulated.py.  The file name makes pytest collect it after the
+elasticity tests.
 """
 import json
 import os
