@@ -257,7 +257,6 @@ struct topo_fluid_ctx {
   std::vector<double*> uK, uM, pK, pM;
   MG<double> mgu, mgp;
   topo_ctx* proj = nullptr;  // the CG1 projection (mass-matrix solve: a filter of radius 0)
-  const double* rho_last = nullptr;
 
   ~topo_fluid_ctx() {
     if (proj) topo_destroy(proj);
@@ -343,7 +342,6 @@ int fluid_setup(topo_fluid_ctx* C, const double* rho, cudaStream_t s) {
   if (!st) st = C->mgp.setup(s);
   if (st == -5) return C->fail(TOPO_ERR_CUDA, "fluid preconditioner set-up: CUDA error");
   if (st) return C->fail(TOPO_ERR_NOT_CONVERGED, "fluid preconditioner set-up: coarse operator not positive definite");
-  C->rho_last = rho;
   return C->cuda_check("fluid set-up");
 }
 
