@@ -85,3 +85,10 @@ def test_design_parser_matches_reference_semantics(tmp_path):
         parse_design_dict({"Elasticity": {}, "Fluid": {}})
     with pytest.raises(ValueError):
         Side.from_string("Middle")
+    # every design the reference ships parses (fluid designs into Flow records)
+    from topomax_gb300.designs import FluidParameters, Flow
+    for name in sorted(os.listdir(os.path.join(GOLDEN, "designs"))):
+        dom, par = parse_design(os.path.join(GOLDEN, "designs", name))
+        if isinstance(par, FluidParameters):
+            assert all(isinstance(f, Flow) and isinstance(f.side, Side) for f in par.flows)
+            assert par.flows[0].to_tuple()[1:] == (par.flows[0].center, par.flows[0].length, par.flows[0].rate)

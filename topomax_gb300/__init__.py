@@ -6,13 +6,14 @@ Reference-facing classes (same names and call surface as Emilinya/topomax):
 C ABI of ``include/topomax_gb300.h`` (``libtopomax_gb300.so``, built by
 ``topomax_gb300.build``).
 """
-from .designs import (DomainParameters, ElasticityParameters, Force, CircularRegion, Side, Traction,
-                      parse_design, parse_design_dict)
+from .designs import (DomainParameters, ElasticityParameters, FluidParameters, Flow, Force, CircularRegion, Side,
+                      Traction, parse_design, parse_design_dict)
 from .penalizers import ElasticPenalizer, FluidPenalizer
 from .problem import Problem
 
 __all__ = [
-    "DomainParameters", "ElasticityParameters", "Force", "CircularRegion", "Side", "Traction", "parse_design",
+    "DomainParameters", "ElasticityParameters", "FluidParameters", "Flow", "Force", "CircularRegion", "Side",
+    "Traction", "parse_design",
     "parse_design_dict", "ElasticPenalizer", "FluidPenalizer", "Problem", "ElasticityProblem", "FluidProblem",
     "HelmholtzFilter", "FEMSolver", "Solver", "RectangleMesh", "FunctionSpace", "VectorFunctionSpace", "Function",
 ]

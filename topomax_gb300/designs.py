@@ -115,13 +115,29 @@ class ElasticityParameters:
 
 
 @dataclass
+class Flow:
+    """A parabolic in- or outflow on one side (designs/definitions.py:105-121)."""
+    side: Side
+    center: float
+    length: float
+    rate: float
+
+    @classmethod
+    def from_dict(cls, d: dict):
+        return cls(Side.from_string(d["side"]), d["center"], d["length"], d["rate"])
+
+    def to_tuple(self):
+        return (self.side, self.center, self.length, self.rate)
+
+
+@dataclass
 class FluidParameters:
     flows: list
     viscosity: float
 
     @classmethod
     def from_dict(cls, d: dict):
-        return cls(list(d["flows"]), d["viscosity"])
+        return cls([Flow.from_dict(f) for f in d["flows"]], d["viscosity"])
 
 
 @dataclass
