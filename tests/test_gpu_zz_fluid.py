@@ -104,11 +104,13 @@ def test_twin_pipe_gradient_matches_finite_differences(tmp_path):
     """tests/test_fluid_gradient.py of the reference, through FEMSolver on the GPU: forward
     differences of the objective along volume / volume_fraction against
     int 1/2 alpha'(rho) direction |u|^2 dx at t = 1e-3 and 1e-7, with the reference's
-    own (scaled-variable) fit."""
+    own (scaled-variable) fit.  The objective is the energy the state minimises under the
+    divergence constraint, so a solve error enters it at second order: rtol 1e-12 leaves
+    the t = 1e-7 difference intact."""
     import torch
     from topomax_gb300.solver import FEMSolver
     s = FEMSolver(10, os.path.join(GOLDEN, "designs", "twin_pipe.json"), data_path=str(tmp_path),
-                  precision="fp64", rtol=1e-13, verbose=False, save=False)
+                  precision="fp64", rtol=1e-12, verbose=False, save=False)
     s.problem.set_penalization(0.1)
     rho = s.rho.tensor.clone()
     J = s.problem.calculate_objective(rho)
