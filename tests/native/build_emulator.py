@@ -24,7 +24,7 @@ def build() -> str:
     if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    cmd = [nvcc, "-std=c++17", "-O1", "-Xcompiler", "-fPIC", "-shared", "-I", INCLUDE, "-I", CSRC,
+    cmd = [nvcc, "-std=c++17", "-O1", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared", "-I", INCLUDE, "-I", CSRC,
            "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a", *srcs,
            "-o", LIB + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,9 +1,8 @@
 """The Stokes-Brinkman fluid problem on the GPU against the oracle (oracle/fluid.py).
 
-Opt-in (TOPO_FLUID_GPU=1) until the fluid solver has run on a GB300: its kernels'
-triangle phases and gathers, and the formulation of the state solve, are checked on
-the CPU in test_fluid_emulated.py.  The file name makes pytest collect it after the
-elasticity tests.
+The kernels' triangle phases and gathers, and the formulation of the state solve,
+are also checked on the CPU in test_fluid_emulated.py.  The file name makes pytest
+collect it after the elasticity tests.
 """
 import json
 import os
@@ -11,9 +10,7 @@ import os
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("TOPO_FLUID_GPU") != "1",
-                                 reason="fluid GPU solver: opt-in (TOPO_FLUID_GPU=1) until run on a GB300")]
+pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 

@@ -21,8 +21,11 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtopomax_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
-         "--expt-relaxed-constexpr"]
+# Host code is compiled without floating-point contraction: gcc fuses a*b+c into
+# one FMA by default on aarch64 but not on x86-64, and the set-up values (node
+# coordinates, flow profiles, load weights) must round the same on both.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
