@@ -106,6 +106,13 @@ int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs);
 /* Replaces Problem.set_penalization (src/problem.py:13, src/penalizers.py:14-20). */
 int topo_set_penalization(topo_ctx* ctx, double p);
 
+/* Cap on the Krylov iterations of one filter or state solve (0 restores the defaults: 200
+ * for the filter, 500 for the state; in mixed precision the cap counts the FP32 inner
+ * iterations over all refinement steps of the solve).  A solve that reaches the cap
+ * without meeting its tolerance returns TOPO_ERR_NOT_CONVERGED.  No counterpart in the
+ * reference, whose SmartMumpsSolver (FEM_src/pde_solver.py:106-133) is a direct solver. */
+int topo_set_iteration_limit(topo_ctx* ctx, int max_iterations);
+
 /* xi = A_f^-1 M1 f for a CG1 field f: replaces HelmholtzFilter.apply
  * (FEM_src/filter.py:40-41).  iters receives the inner CG iterations (may be NULL). */
 int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, int* iters,

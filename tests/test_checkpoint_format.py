@@ -73,3 +73,24 @@ def test_design_record_has_the_reference_layout(tmp_path):
         back = pickle.load(f)
     assert np.array_equal(back["vector"], rec["vector"])
     assert mesh_to_N(RectangleMesh(2.0, 1.0, 80, 40)) == 40
+
+
+def test_function_space_host_order():
+    """CG1 spaces speak dolfin's dof order on the host by default (arrays handed in and out
+    by the API, as the reference's to_array/set_from_array, FEM_src/solver.py:75-79) and the
+    lattice order on request; the vector CG2 space is always the lattice."""
+    import pytest
+    from topomax_gb300.fem import FunctionSpace, VectorFunctionSpace
+    gold = _gold("triangle_N10.json")
+    mesh = RectangleMesh(1.0, 1.0, 10, 10)
+    V = FunctionSpace(mesh, "CG", 1)
+    assert V.dof_order == "dolfin"
+    ref = np.asarray(gold["rho_dolfin"])
+    lattice = V.from_host_order(ref)
+    assert np.array_equal(lattice, from_dolfin_order(ref, 10, 10))
+    assert np.array_equal(V.to_host_order(lattice), ref)
+    L = FunctionSpace(mesh, "CG", 1, dof_order="lattice")
+    assert L.dolfin_permutation() is None and np.array_equal(L.from_host_order(ref), ref)
+    assert VectorFunctionSpace(mesh).dof_order == "lattice"
+    with pytest.raises(ValueError):
+        FunctionSpace(mesh, "CG", 1, dof_order="vertex")

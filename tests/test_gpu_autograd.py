@@ -24,7 +24,7 @@ def _problem(precision, rtol):
                                    filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)}}
     dom, par = parse_design_dict(dd)
     mesh = tg.RectangleMesh(2.0, 1.0, 400, 200)
-    V = tg.FunctionSpace(mesh, "CG", 1)
+    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
     prob = tg.ElasticityProblem(mesh, V, dom, par, precision=precision, rtol=rtol)
     prob.set_penalization(3.0)
     return prob, V

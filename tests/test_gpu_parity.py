@@ -37,7 +37,7 @@ def _gpu_problem(d: Design, nx, ny, precision="mixed", rtol=1e-12):
                                                     fixed_points=d.fixed_points)}}
     dom, par = parse_design_dict(dd)
     mesh = tg.RectangleMesh(d.width, d.height, nx, ny)
-    V = tg.FunctionSpace(mesh, "CG", 1)
+    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")   # the oracle's vertex order
     return tg.ElasticityProblem(mesh, V, dom, par, precision=precision, rtol=rtol), V
 
 
@@ -67,7 +67,7 @@ def test_filter_matches_oracle(precision):
     d = _design()
     nx, ny = 80, 40
     mesh = tg.RectangleMesh(2.0, 1.0, nx, ny)
-    V = tg.FunctionSpace(mesh, "CG", 1)
+    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
     f = tg.HelmholtzFilter(0.05, V, precision=precision, rtol=1e-12)
     o = FEMOracle(Lattice(2.0, 1.0, nx, ny), d)
     rho = np.random.default_rng(1).uniform(0, 1, o.L.n_vertices)
@@ -118,6 +118,7 @@ def test_state_compliance_gradient_match_oracle(precision, case):
 
 
 def test_projection_matches_oracle():
+    import torch
     import topomax_gb300 as tg
     d = _design()
     solver_o = OracleSolver(40, d)
@@ -127,9 +128,14 @@ def test_projection_matches_oracle():
     from tests.test_gpu_parity import _write_design
     path = _write_design(d)
     s = tg.FEMSolver(40, path, verbose=False, save=False)
-    psi = s.project(half, s.volume).cpu().numpy()
+    psi = s.project(torch.as_tensor(half), s.volume).cpu().numpy()    # tensors: lattice order
     assert np.max(np.abs(psi - ref)) <= 1e-10
-    assert abs(s.integrate(1.0 / (1.0 + np.exp(-psi))) - s.volume) <= 1e-11
+    assert abs(s.integrate(torch.sigmoid(torch.as_tensor(psi))) - s.volume) <= 1e-11
+    # host arrays in the solver's (dolfin) dof order, as the reference's project takes them
+    V = s.control_space
+    psi_host = s.project(V.to_host_order(half), s.volume)
+    assert isinstance(psi_host, np.ndarray)
+    assert np.max(np.abs(V.from_host_order(psi_host) - ref)) <= 1e-10
 
 
 def _write_design(d: Design, name="design.json"):
@@ -192,7 +198,8 @@ def test_cantilever_design_loop_parity(precision):
     robjs = np.array(ref.objectives)
     assert len(objs) == len(robjs)
     assert np.max(np.abs(objs - robjs) / np.abs(robjs)) <= 1e-6
-    assert np.max(np.abs(s.to_array(s.rho) - ref.rho)) <= 1e-5
+    assert np.max(np.abs(s.rho.tensor.cpu().numpy() - ref.rho)) <= 1e-5
+    assert np.max(np.abs(s.to_array(s.rho) - s.control_space.to_host_order(ref.rho))) <= 1e-5
 
 
 def test_call_order_errors():
@@ -268,3 +275,28 @@ def test_contexts_of_different_sizes_interleave():
         xi = F.Function(V, torch.full((V.dim(),), 0.5, dtype=torch.float64, device="cuda"))
         c = prob.calculate_objective(xi)
         assert np.isfinite(c) and c > 0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_reference_design_vector_at_the_api(precision):
+    """The reference's saved triangle design (tests/test_data/FEM/triangle/data/correct_rho.dat,
+    dolfin's CG1 dof order) goes straight into calculate_objective on a default CG1 space
+    and gives the objective the reference saved beside it; read in lattice order the same
+    numbers are a different design."""
+    import json
+    import os
+    import topomax_gb300 as tg
+    gold = json.load(open(os.path.join(GOLDEN, "triangle_N10.json")))
+    dom, par = tg.parse_design(os.path.join(GOLDEN, "designs", "triangle.json"))
+    mesh = tg.RectangleMesh(1.0, 1.0, 10, 10)
+    results = {}
+    for order in ("dolfin", "lattice"):
+        V = tg.FunctionSpace(mesh, "CG", 1, dof_order=order)
+        prob = tg.ElasticityProblem(mesh, V, dom, par, precision=precision, rtol=1e-11)
+        prob.set_penalization(gold["penalty"])
+        results[order] = prob.calculate_objective(np.array(gold["rho_dolfin"]))
+        if order == "dolfin":
+            xi = prob.filtered_rho.vector()[:]             # host view: dolfin order again
+            assert np.max(np.abs(xi - prob.filter.apply(np.array(gold["rho_dolfin"])).vector()[:])) == 0
+    assert abs(results["dolfin"] - gold["objective"]) <= 1e-6 * gold["objective"]
+    assert abs(results["lattice"] - gold["objective"]) > 1e-3 * gold["objective"]

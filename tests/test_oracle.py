@@ -92,3 +92,24 @@ def test_design_parser_matches_reference_semantics(tmp_path):
         if isinstance(par, FluidParameters):
             assert all(isinstance(f, Flow) and isinstance(f.side, Side) for f in par.flows)
             assert par.flows[0].to_tuple()[1:] == (par.flows[0].center, par.flows[0].length, par.flows[0].rate)
+
+
+def test_oracle_projection_failure_paths():
+    """The oracle's projection follows src/solver.py:149-186 and src/utils.py:138-157: an
+    unreachable volume ends in smart_brentq's ValueError; a Newton breakdown falls back to
+    the bracketing search (radius doubled from 2) and still meets the volume."""
+    import pytest
+    from oracle.fem import Design, OracleSolver, expit
+    d = Design(width=2.0, height=1.0, fem_step_size=0.002, penalties=[3.0], volume_fraction=0.5,
+               fixed_sides=["Left"], body_force=None,
+               tractions=[dict(side="Right", center=0.5, length=0.5, value=[0.0, -1.0])],
+               filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)
+    s = OracleSolver(10, d)
+    n = s.lattice.n_vertices
+    with pytest.raises(ValueError, match=r"^f\(-max_radius\) and f\(max_radius\) must have different signs!$"):
+        s.project(np.zeros(n), 3.0)
+    half = -40.0 + np.random.default_rng(5).uniform(-0.5, 0.5, n)
+    psi = s.project(half, s.volume)
+    c = float(np.mean(psi - half))
+    assert 32.0 < c < 64.0 and np.allclose(psi - half, c, rtol=0, atol=1e-13)
+    assert abs(s.integrate(expit(psi)) - s.volume) <= 1e-12

@@ -38,7 +38,7 @@ def _problem():
                                    tractions=[dict(side="Right", center=0.5, length=0.5, value=[0.0, -1.0])],
                                    filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)}})
     mesh = tg.RectangleMesh(2.0, 1.0, NX, NY)
-    V = tg.FunctionSpace(mesh, "CG", 1)
+    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
     prob = tg.ElasticityProblem(mesh, V, dom, par, precision="mixed", rtol=1e-10)
     prob.set_penalization(3.0)
     return prob, V

@@ -202,6 +202,8 @@ struct topo_ctx {
   bool verify_residual = false;  // TOPO_VERIFY_RESIDUAL=1: confirm FGMRES convergence with a true residual
   // tightest relative tolerance of an FP32 inner solve (TOPO_INNER_FLOOR_STATE / _FILTER)
   double inner_floor_state = 1e-4, inner_floor_filter = 1e-5;
+  // cap on the Krylov iterations of one solve (topo_set_iteration_limit; 0: the defaults)
+  int iter_limit = 0;
   // lower end of the Chebyshev smoothing interval (fraction of lambda_max) per
   // hierarchy (TOPO_CHEB_LO_STATE / _FILTER): the high-contrast elasticity levels
   // converge best with a wide interval, the filter's with a narrower one
@@ -278,6 +280,8 @@ struct topo_ctx {
     return TOPO_OK;
   }
   int grid(size_t n) const { return vec_grid(n, sms); }
+  // Krylov iteration cap of one solve: the context's limit if set, else the default
+  int max_iterations(int dflt) const { return iter_limit > 0 ? iter_limit : dflt; }
 
   template <class T>
   P2Params<T> p2params(int clamp = 0, const T* rmass = nullptr) const {
@@ -469,6 +473,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
     cudaStreamSynchronize(s);
   };
   double prev = 0.0;
+  bool capped = false;  // the context's iteration limit was reached
   for (int cycle = 0; cycle < kMaxOuter; ++cycle) {
     double* r = W.V;
     C->launches += 4;
@@ -510,6 +515,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
         std::fprintf(stderr, "[topo solve]   inner %d: tol %.1e, %d iterations, FP32 relres %.3e, rc %d\n", j, inner,
                      is.iterations, is.relres, rc);
       st.minres |= is.minres;
+      if (C->iter_limit > 0 && st.iterations >= C->iter_limit) capped = true;
       if (rc == -4) return C->fail(TOPO_ERR_NAN, "non-finite value in the FP32 inner solve");
       if (rc == -5) return C->fail(TOPO_ERR_CUDA, "inner solve: CUDA graph recording or launch failed");
       double* w = W.V + size_t(j + 1) * n;
@@ -555,7 +561,7 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
       gv[j + 1] = -sn[j] * gv[j];
       gv[j] = cs[j] * gv[j];
       k = j + 1;
-      if (std::fabs(gv[j + 1]) <= 0.5 * rtol * bn || hn == 0.0) break;
+      if (std::fabs(gv[j + 1]) <= 0.5 * rtol * bn || hn == 0.0 || capped) break;
     }
     double y[m] = {};
     for (int i = k - 1; i >= 0; --i) {
@@ -578,12 +584,14 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
                      st.relres, st.iterations);
       return TOPO_OK;
     }
+    if (capped) break;
   }
   apply64(x, W.t, s);
   k_sub<double><<<g, kVecThreads, 0, s>>>(W.V, b, W.t, n);
   st.relres = std::sqrt(C->dot64(W.V, W.V, n, s)) / bn;
   if (st.relres <= rtol) return TOPO_OK;
-  return C->fail(TOPO_ERR_NOT_CONVERGED, "refinement did not reach rtol %.3g (relres %.3g)", rtol, st.relres);
+  return C->fail(TOPO_ERR_NOT_CONVERGED, "refinement did not reach rtol %.3g (relres %.3g after %d inner iterations)",
+                 rtol, st.relres, st.iterations);
 }
 
 int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int* iters, cudaStream_t s) {
@@ -591,9 +599,10 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   int rc;
   if (C->precision == TOPO_PREC_MIXED) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
-    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, kFilterMaxIt, C->inner_floor_filter, st, s);
+    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
+                   C->inner_floor_filter, st, s);
   } else {
-    rc = C->fmg64.pcg(b, xi, false, rtol, kFilterMaxIt, st, s);
+    rc = C->fmg64.pcg(b, xi, false, rtol, C->max_iterations(kFilterMaxIt), st, s);
     if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
     else if (rc == -5) rc = C->fail(TOPO_ERR_CUDA, "filter solve: CUDA graph recording or launch failed");
     else if (rc) rc = C->fail(TOPO_ERR_NOT_CONVERGED, "filter CG did not converge (relres %.3g)", st.relres);
@@ -806,6 +815,14 @@ int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs) {
   return TOPO_OK;
 }
 
+int topo_set_iteration_limit(topo_ctx* ctx, int max_iterations) {
+  return guarded(ctx, [&]() {
+    if (max_iterations < 0) return ctx->fail(TOPO_ERR_ARG, "negative iteration limit");
+    ctx->iter_limit = max_iterations;
+    return TOPO_OK;
+  });
+}
+
 int topo_set_penalization(topo_ctx* ctx, double p) {
   return guarded(ctx, [&]() {
     if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context has no penaliser");
@@ -865,10 +882,10 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     if (ctx->precision == TOPO_PREC_MIXED) {
       P2Params<double> P64 = ctx->p2params<double>(0, ctx->rm_op64);
       auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
-      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, kStateMaxIt, ctx->inner_floor_state,
-                     st, s);
+      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, ctx->max_iterations(kStateMaxIt),
+                     ctx->inner_floor_state, st, s);
     } else {
-      rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, kStateMaxIt, st, s);
+      rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, ctx->max_iterations(kStateMaxIt), st, s);
       if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");
       else if (rc == -5) rc = ctx->fail(TOPO_ERR_CUDA, "state solve: CUDA graph recording or launch failed");
       else if (rc) rc = ctx->fail(TOPO_ERR_NOT_CONVERGED, "state CG did not converge (relres %.3g)", st.relres);
@@ -982,7 +999,9 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
         }
         r *= 2;
       }
-      if (!found) return ctx->fail(TOPO_ERR_PROJECTION, "Projection failed to converge");
+      // smart_brentq's error when no sign change is found up to the largest radius
+      // (src/utils.py:147-151); the caller's design loop stops with this message
+      if (!found) return ctx->fail(TOPO_ERR_PROJECTION, "f(-max_radius) and f(max_radius) must have different signs!");
       if (flo == 0) c = lo;
       else if (fhi == 0) c = hi;
       else {

@@ -11,8 +11,16 @@ Mirrors the pieces of FEniCS the reference's elasticity path touches:
 * ``ElasticityProblem`` -- FEM_src/elasisity_problem.py:76-196.
 
 All arithmetic runs in ``libtopomax_gb300.so`` on the GPU; this module only
-marshals arguments.  Vector ordering: CG1 vertex (i, j) at j*(nx+1)+i, P2
-node (a, b) at b*(2nx+1)+a with components interleaved.
+marshals arguments.
+
+Vector ordering.  On the device (``Function.tensor``, torch tensors passed
+in): CG1 vertex (i, j) at j*(nx+1)+i, P2 node (a, b) at b*(2nx+1)+a with
+components interleaved.  On the host side of a CG1 space -- ``.vector()``
+views and numpy arrays or lists passed to the problem and filter methods --
+the space's ``dof_order``: "dolfin" (the default) is the numbering the
+reference's serial dolfin gives the CG1 dofs of its RectangleMesh, so arrays
+from the reference (``to_array``, saved designs) are read as the reference
+reads them; "lattice" is the device order.
 """
 from __future__ import annotations
 
@@ -82,16 +90,46 @@ class RectangleMesh:
 
 
 class FunctionSpace:
-    """CG1 scalar space (degree 1) or vector CG2 space (``vector=True``, degree 2)."""
+    """CG1 scalar space (degree 1) or vector CG2 space (``vector=True``, degree 2).
 
-    def __init__(self, mesh: RectangleMesh, family: str = "CG", degree: int = 1, vector: bool = False):
+    ``dof_order`` (CG1 only) is the order of the space's host-side arrays: "dolfin"
+    (default; the reference's CG1 dof numbering, FEM_src/solver.py:75-79 hands such
+    arrays to the design loop) or "lattice" (the device order).  The vector CG2 space
+    is always in lattice order."""
+
+    def __init__(self, mesh: RectangleMesh, family: str = "CG", degree: int = 1, vector: bool = False,
+                 dof_order: str = "dolfin"):
         if family not in ("CG", "Lagrange", "P"):
             raise ValueError(f"unsupported family {family}")
         if (degree, vector) not in ((1, False), (2, True)):
             raise ValueError("supported spaces: scalar CG1 and vector CG2")
+        if dof_order not in ("dolfin", "lattice"):
+            raise ValueError(f"dof_order must be 'dolfin' or 'lattice', got {dof_order!r}")
         self._mesh = mesh
         self.degree = degree
         self.vector = vector
+        self.dof_order = "lattice" if vector else dof_order
+        self._perm = None
+
+    def dolfin_permutation(self):
+        """Lattice index of each host-side dof (None when the host order is the lattice)."""
+        if self.dof_order == "lattice":
+            return None
+        if self._perm is None:
+            self._perm = dolfin_cg1_order(self._mesh.nx, self._mesh.ny)
+        return self._perm
+
+    def to_host_order(self, lattice_values: np.ndarray) -> np.ndarray:
+        perm = self.dolfin_permutation()
+        return lattice_values if perm is None else lattice_values[perm]
+
+    def from_host_order(self, values: np.ndarray) -> np.ndarray:
+        perm = self.dolfin_permutation()
+        if perm is None:
+            return values
+        out = np.empty_like(values)
+        out[perm] = values
+        return out
 
     def mesh(self):
         return self._mesh
@@ -108,6 +146,8 @@ def VectorFunctionSpace(mesh: RectangleMesh, family: str = "CG", degree: int = 2
 
 
 class _VectorView:
+    """``Function.vector()``: the coefficients in the space's host-side dof order."""
+
     def __init__(self, f: "Function"):
         self._f = f
 
@@ -115,14 +155,20 @@ class _VectorView:
         return self._f.tensor.numel()
 
     def __getitem__(self, idx):
-        return self._f.tensor.detach().cpu().numpy()[idx]
+        return self._f._V.to_host_order(self._f.tensor.detach().cpu().numpy())[idx]
 
     def __setitem__(self, idx, value):
-        if isinstance(value, torch.Tensor):
-            self._f.tensor[idx] = value.to(self._f.tensor)
-        else:
-            v = np.asarray(value, dtype=np.float64)
-            self._f.tensor[idx] = torch.as_tensor(v, device=self._f.tensor.device) if v.ndim else float(v)
+        V, t = self._f._V, self._f.tensor
+        if V.dolfin_permutation() is None:
+            if isinstance(value, torch.Tensor):
+                t[idx] = value.to(t)
+            else:
+                v = np.asarray(value, dtype=np.float64)
+                t[idx] = torch.as_tensor(v, device=t.device) if v.ndim else float(v)
+            return
+        host = self[:]
+        host[idx] = value.detach().cpu().numpy() if isinstance(value, torch.Tensor) else value
+        t.copy_(torch.as_tensor(V.from_host_order(host), device=t.device))
 
     def get_local(self):
         return self[:]
@@ -189,8 +235,8 @@ def mesh_to_domain_size(mesh: RectangleMesh) -> tuple:
 
 
 def design_record(values, mesh: RectangleMesh, N: int | None = None, domain_size=None) -> dict:
-    """The pickled record of a CG1 design (FEM_src/utils.py:47-69 ``save_function``):
-    N, domain size, problem "design" and the vector in dolfin's dof order."""
+    """The pickled record of a CG1 design (FEM_src/utils.py:47-69 ``save_function``) from
+    lattice-order values: N, domain size, problem "design" and the vector in dolfin's dof order."""
     return {"N": mesh_to_N(mesh) if N is None else N,
             "domain_size": mesh_to_domain_size(mesh) if domain_size is None else domain_size,
             "problem": "design", "vector": to_dolfin_order(values, mesh.nx, mesh.ny)}
@@ -204,12 +250,12 @@ def save_function(f: "Function", filename: str, problem: str = "design", N: int 
     if V.vector or V.degree != 1 or problem != "design":
         raise ValueError("save_function writes CG1 designs (problem 'design')")
     with open(filename, "wb") as datafile:
-        pickle.dump(design_record(f.vector()[:], V.mesh(), N, domain_size), datafile)
+        pickle.dump(design_record(f.tensor.cpu().numpy(), V.mesh(), N, domain_size), datafile)
 
 
 def load_function(filename: str, mesh: RectangleMesh | None = None, function_space: FunctionSpace | None = None):
     """``load_function`` (FEM_src/utils.py:72-109) for design files -- the reference's own
-    or this package's: returns (Function, mesh, function space), the vector in lattice order."""
+    or this package's: returns (Function, mesh, function space)."""
     with open(filename, "rb") as datafile:
         data = pickle.load(datafile)
     if data["problem"] != "design":
@@ -223,19 +269,23 @@ def load_function(filename: str, mesh: RectangleMesh | None = None, function_spa
     values = np.asarray(data["vector"], dtype=np.float64)
     if values.size != function_space.dim():
         raise ValueError(f"design vector of {values.size} values does not fit {function_space.dim()} vertices")
-    f = Function(function_space)
-    f.vector()[:] = from_dolfin_order(values, m.nx, m.ny)
+    f = Function(function_space, torch.as_tensor(from_dolfin_order(values, m.nx, m.ny)).to(_device()))
     return f, mesh, function_space
 
 
 def as_cg1_tensor(value, V: FunctionSpace) -> torch.Tensor:
-    """CG1 coefficients of a Function, a tensor or an array-like (copied to HBM)."""
+    """CG1 coefficients in device (lattice) order of a Function, a torch tensor (taken to be
+    in lattice order) or a numpy array / list (in the space's host-side dof order), copied
+    to HBM where needed."""
     if isinstance(value, Function):
         return value.tensor
     if isinstance(value, torch.Tensor):
         t = value.to(device=_device(), dtype=torch.float64).contiguous()
     else:
-        t = torch.as_tensor(np.ascontiguousarray(value, dtype=np.float64)).to(_device())
+        v = np.ascontiguousarray(value, dtype=np.float64).reshape(-1)
+        if v.size == V.dim():
+            v = np.ascontiguousarray(V.from_host_order(v))
+        t = torch.as_tensor(v).to(_device())
     if t.numel() != V.dim():
         raise ValueError(f"expected {V.dim()} CG1 values, got {t.numel()}")
     return t.reshape(-1)
@@ -379,6 +429,12 @@ class ElasticityProblem(Problem):
         if not ptr:
             raise _capi.TopoError(st.value, f"could not create the elasticity problem (status {st.value})")
         return _Context(ptr)
+
+    def set_iteration_limit(self, max_iterations: int = 0):
+        """Cap the Krylov iterations of every filter and state solve of this problem (0: the
+        defaults).  A solve that reaches the cap without meeting rtol raises ValueError
+        (``TopoError`` with code TOPO_ERR_NOT_CONVERGED)."""
+        self._ctx.check(self._ctx._lib.topo_set_iteration_limit(self._ctx.ptr, int(max_iterations)))
 
     # -- Problem interface -------------------------------------------------
     def set_penalization(self, penalization: float):

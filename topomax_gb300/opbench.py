@@ -76,7 +76,7 @@ def main(argv=None):
 
     dom, par = parse_design_dict(DESIGN)
     mesh = F.RectangleMesh(dom.width, dom.height, args.nx, args.ny)
-    V = F.FunctionSpace(mesh, "CG", 1)
+    V = F.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
     prob = F.ElasticityProblem(mesh, V, dom, par, precision=args.precision, rtol=1e-8)
     prob.set_penalization(3.0)
     g = torch.Generator().manual_seed(0)

@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes
 import os
 import pickle
+import time
 from abc import ABC, abstractmethod
 
 import numpy as np
@@ -20,7 +21,7 @@ from . import _capi
 from .designs import ElasticityParameters, FluidParameters, parse_design, parse_design_dict
 from .fem import (DEFAULT_RTOL, ElasticityProblem, Function, FunctionSpace, RectangleMesh, _device, _ptr,
                   _stream, as_cg1_tensor, design_record)
-from .utils import IterationData, SolverResult, Timer
+from .utils import IterationData, SolverResult
 
 
 def expit(x):
@@ -155,6 +156,8 @@ class FEMSolver(Solver):
         raise ValueError(f"Got unknown problem '{self.parameters.problem}'")
 
     def to_array(self, rho) -> np.ndarray:
+        """The design's values in the control space's host dof order (dolfin's, as the
+        reference's FEM_src/solver.py:75-76)."""
         return rho.vector()[:]
 
     def set_from_array(self, rho, values):
@@ -171,15 +174,21 @@ class FEMSolver(Solver):
         """FEM_src/solver.py:86-89: the design in the reference's pickle, dolfin's dof order."""
         rho_file = file_root + "_rho.dat"
         with open(rho_file, "wb") as f:
-            pickle.dump(design_record(self.to_array(rho), self.mesh), f)
+            pickle.dump(design_record(rho.tensor.cpu().numpy(), self.mesh), f)
         return os.path.basename(rho_file)
 
     # -- EMD ------------------------------------------------------------------
-    def project(self, half_step, volume: float) -> torch.Tensor:
-        """half_step + c with int expit(half_step + c) dx = volume (src/solver.py:149-186)."""
+    def project(self, half_step, volume: float):
+        """half_step + c with int expit(half_step + c) dx = volume (src/solver.py:149-186).
+
+        A numpy array (in the control space's host dof order) gives a numpy array in the
+        same order, as the reference's; a tensor or Function gives a lattice-order tensor."""
         h = as_cg1_tensor(half_step, self.control_space)
         zero = torch.zeros_like(h)
-        return self._emd(h, zero, 0.0, volume)
+        psi = self._emd(h, zero, 0.0, volume)
+        if isinstance(half_step, (torch.Tensor, Function)):
+            return psi
+        return self.control_space.to_host_order(psi.cpu().numpy())
 
     def _emd(self, psi_prev: torch.Tensor, g: torch.Tensor, alpha: float, volume: float) -> torch.Tensor:
         psi = torch.empty_like(psi_prev)
@@ -204,14 +213,13 @@ class FEMSolver(Solver):
 
     def solve(self):
         """Solve the topology optimisation problem (src/solver.py:208-302)."""
-        total_timer = Timer()
-        objective_timer = Timer()
+        t_total = time.perf_counter()
         psi = logit(self.rho.tensor.clone())
         for penalty in self.parameters.penalties:
             self.problem.set_penalization(penalty)
-            objective_timer.restart()
+            t_step = time.perf_counter()
             objectives = [self.problem.calculate_objective(self.rho)]
-            times = [objective_timer.get_time_seconds()]
+            times = [time.perf_counter() - t_step]
             deltas = []
             if self.verbose:
                 print(f"penalty {penalty}: k=0 objective={objectives[0]:.6g}")
@@ -220,7 +228,7 @@ class FEMSolver(Solver):
             for k in range(self.max_iterations):
                 if self.save and k % self.skip_multiple == 0:
                     self.save_iteration(self.rho, objectives[-1], k, penalty)
-                objective_timer.restart()
+                t_step = time.perf_counter()
                 previous_psi = psi.clone()
                 try:
                     psi = self.step(previous_psi, self.step_size_at_iter(k))
@@ -231,7 +239,7 @@ class FEMSolver(Solver):
                     break
                 difference = self._finish(psi, previous_psi)
                 objectives.append(self.problem.calculate_objective(self.rho))
-                times.append(objective_timer.get_time_seconds())
+                times.append(time.perf_counter() - t_step)
                 deltas.append(difference)
                 if self.verbose:
                     print(f"k={k + 1} objective={objectives[-1]:.10g} delta_rho={difference:.3e} "
@@ -259,7 +267,7 @@ class FEMSolver(Solver):
                 self.save_iteration(self.rho, objectives[-1], k + 1, penalty)
                 self.save_result(objectives, times, penalty, exit_condition)
         if self.verbose:
-            print(f"Topology optimization took {total_timer.get_time_string()}")
+            print(f"design loop: {time.perf_counter() - t_total:.3f} s")
         return self.history
 
     def save_iteration(self, rho, objective: float, k: int, penalty: float):
