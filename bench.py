@@ -126,9 +126,13 @@ def _grid(text):
 def _blas_threads():
     try:
         from threadpoolctl import threadpool_info
-        return max((i.get("num_threads", 1) for i in threadpool_info() if i.get("user_api") == "blas"), default=1)
+        return str(max((i.get("num_threads", 1) for i in threadpool_info() if i.get("user_api") == "blas"),
+                       default=1))
     except Exception:
-        return int(os.environ.get("OMP_NUM_THREADS", "0")) or None
+        for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS"):
+            if os.environ.get(var):
+                return os.environ[var]
+        return "the BLAS library's default"
 
 
 class OracleLoop:
@@ -175,7 +179,8 @@ def oracle_sample(nx, ny, steps, warmup, sec):
     return (f"{steps} timed FP64 oracle design iterations (after {warmup} untimed) on the {nx}x{ny} cantilever "
             f"({dofs(nx, ny)} P2 dofs; the reference algorithm: filter solves, sparse P2 assembly, SuperLU with "
             f"a minimum-degree ordering, Newton volume projection), {sec:.2f} s each, measured on this host; "
-            f"single-threaded sparse solve (BLAS threads {_blas_threads()}, host cores {os.cpu_count()})")
+            f"SuperLU and the assembly run on one core, BLAS ({_blas_threads()} threads) is not on the path; "
+            f"host cores {os.cpu_count()}")
 
 
 def run_reference(args):
@@ -189,8 +194,9 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": 1000.0 * sec, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U(0.01,1) density)", "impl": "reference",
            "config": {"workload": f"cantilever 2x1, {nx}x{ny} squares, vector P2, {dofs(nx, ny)} dofs "
-                                  f"(the largest grid whose design iterations fit the run; the GPU arm's "
-                                  f"{args.nx}x{args.ny} grid takes tens of minutes per iteration here)",
+                                  f"(sized so that the run ends in about a minute; on the GPU arm's "
+                                  f"{args.nx}x{args.ny} grid SuperLU cannot factor the state matrix on a "
+                                  f"62 GB host)",
                       "same_config": False},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -1,6 +1,6 @@
 """Operator micro-benchmark: the matrix-free P2 state operator alone.
 
-    python -m topomax_gb300.opbench --nx 1000 --ny 500 --precision mixed --reps 20
+    python opbench.py --nx 1000 --ny 500 --precision mixed --reps 20
 
 Sets up a cantilever (2 x 1, left side clamped, unit downward traction on the
 central half of the right side) with a seeded density, runs one state solve so that the operator
@@ -22,10 +22,14 @@ import argparse
 import ctypes
 import json
 
+import os
+import sys
+
 import torch
 
-from . import fem as F
-from .designs import parse_design_dict
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from topomax_gb300 import fem as F  # noqa: E402
+from topomax_gb300.designs import parse_design_dict  # noqa: E402
 
 DESIGN = {"Elasticity": {
     "domain_parameters": dict(width=2.0, height=1.0, fem_step_size=0.002, dem_step_size=0.002,
@@ -45,7 +49,7 @@ FLUID = {"Fluid": {
 
 def time_fluid(args):
     import time
-    from .solver import FEMSolver
+    from topomax_gb300.solver import FEMSolver
     s = FEMSolver(args.n, dict(FLUID, name="diffuser"), precision="fp64", rtol=1e-10, verbose=False, save=False,
                   max_iterations=args.reps)
     torch.cuda.synchronize()

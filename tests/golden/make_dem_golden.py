@@ -1,9 +1,9 @@
 """Generate DEM golden vectors by running the reference's own DEM classes.
 
-Run where the topomax reference checkout is mounted (default ``/root/reference``,
-override with ``TOPOMAX_REFERENCE``); torch and scipy must import::
+Run where a topomax reference checkout is available, naming its root in
+``TOPOMAX_REFERENCE`` (required; there is no default); torch and scipy must import::
 
-    python tests/golden/make_dem_golden.py
+    TOPOMAX_REFERENCE=/path/to/topomax python tests/golden/make_dem_golden.py
 
 The reference imports ``rff`` (random_fourier_features_pytorch), which is not
 installed; a stub module written from the encoder's definition (gamma(x) =
@@ -35,7 +35,7 @@ import tempfile
 
 import numpy as np
 
-REF = os.environ.get("TOPOMAX_REFERENCE", "/root/reference")
+REF = os.environ.get("TOPOMAX_REFERENCE", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 STUB = '''
@@ -185,4 +185,7 @@ def energy_cases() -> None:
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set TOPOMAX_REFERENCE to the root of a topomax checkout"
+                 + (f" ({REF} is not a directory)" if REF else ""))
     main()

@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the topomax reference.
 
-Run in a container where the reference checkout is mounted (default path
-``/root/reference``, override with ``TOPOMAX_REFERENCE``)::
+Run where a topomax reference checkout is available, naming its root in
+``TOPOMAX_REFERENCE`` (required; there is no default)::
 
-    python tests/golden/make_golden.py
+    TOPOMAX_REFERENCE=/path/to/topomax python tests/golden/make_golden.py
 
 It reads, without importing any reference module:
 
@@ -31,7 +31,7 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("TOPOMAX_REFERENCE", "/root/reference")
+REF = os.environ.get("TOPOMAX_REFERENCE", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -67,8 +67,9 @@ def _load_record(path):
 
 
 def main():
-    if not os.path.isdir(REF):
-        sys.exit(f"reference checkout not found at {REF}")
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set TOPOMAX_REFERENCE to the root of a topomax checkout"
+                 + (f" ({REF} is not a directory)" if REF else ""))
     os.makedirs(os.path.join(HERE, "designs"), exist_ok=True)
     for name in sorted(os.listdir(os.path.join(REF, "designs"))):
         if not name.endswith(".json"):
