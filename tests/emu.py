@@ -21,6 +21,7 @@ def lib():
     if _E is None:
         E = load()
         E.emu_dir_ints.restype = C_I
+        E.emu_lean_warps.restype = ctypes.c_long
         E.emu_p2_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, C_D, C_D, P_I, P_D, P_D, P_D, C_I]
         E.emu_p1_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, P_I, P_D, P_D, C_D, C_D, P_D, P_D, C_I]
         E.emu_transfer.argtypes = [C_I, C_I, C_I, P_I, C_I, C_I, P_I, P_D, P_D, C_I]
@@ -73,6 +74,11 @@ def p2_apply(nx, ny, hx, hy, lam, mu, p, dirv, xi, u, prec=0, mode=0, pmin=1e-6)
     uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
     lib().emu_p2_apply(prec, nx, ny, hx, hy, lam, mu, p, pmin, ip(dirv), dp(xi), dp(uu), dp(y), mode)
     return y
+
+
+def lean_warps() -> int:
+    """Warps of the last emulated P2 launch that ran the lean (unchecked) phases."""
+    return int(lib().emu_lean_warps())
 
 
 def p1_apply(NC, nx, ny, hx, hy, lam, mu, dirv, kK, kM, u, kKc=0.0, kMc=0.0, diag=False):

@@ -45,11 +45,15 @@ void dir_to(const Dir& r, int* d) {
   for (int k = 0; k < 2 * kMaxDirPoints; ++k) d[5 + k] = r.pts[k];
 }
 
+// Warps of the last emulated P2 march that took the lean phases.
+static long lean_warps = 0;
+
 // Runs the column-march P2 kernel on the CPU: the 32 lanes of a warp execute
 // each phase in turn and the shuffles become copies between lane states.
 template <class T>
 void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
   P2March<T>::prepare(io);
+  lean_warps = 0;
   if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   const bool operand = io.mode != kP2Diag;
@@ -73,27 +77,47 @@ void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
   for (int w = 0; w < nxw; ++w)
     for (int js = 0; js < P.ny; js += seg) {
       const int je = std::min(js + seg, P.ny);
-      for (int l = 0; l < 32; ++l) P2March<T>::begin(L[l], w * P2M_OWN - 1 + l, l == 31);
+      for (int l = 0; l < 32; ++l) P2March<T>::begin(P, L[l], w * P2M_OWN - 1 + l, l == 31);
       int j = js > 0 ? js - 1 : 0;
+      // the kernel's warp-uniform choice between the masked and the lean phases
+      const bool lean = P2March<T>::lean_region(P, w * P2M_OWN - 1, j, je);
+      lean_warps += lean;
       for (int l = 0; l < 32; ++l) {
-        P2March<T>::template load<0>(P, io, xi, L[l], j);
-        P2March<T>::load_mass(P, L[l].i, j, L[l].M);
+        if (lean) {
+          P2March<T>::template load<0, true>(P, io, xi, L[l], j);
+          P2March<T>::template load_mass<true>(P, L[l].K, L[l].i, j, L[l].M);
+        } else {
+          P2March<T>::template load<0>(P, io, xi, L[l], j);
+          P2March<T>::load_mass(P, L[l].K, L[l].i, j, L[l].M);
+        }
       }
       down(0);
       std::vector<P2Next<T>> N(32);
       for (;;) {
         const bool more = j + 1 < je;
         if (more)
-          for (int l = 0; l < 32; ++l) P2March<T>::prefetch(P, io, xi, L[l], j + 1, N[l]);
+          for (int l = 0; l < 32; ++l) {
+            if (lean) P2March<T>::template prefetch<true>(P, io, xi, L[l], j + 1, N[l]);
+            else P2March<T>::prefetch(P, io, xi, L[l], j + 1, N[l]);
+          }
         std::vector<typename P2March<T>::Fin> F(32);
         if (j >= js)
           for (int l = 1; l < 32; ++l)
-            if (L[l].i <= P.nx) P2March<T>::fin_load(P, io, L[l], j, F[l]);
-        for (int l = 0; l < 32; ++l) P2March<T>::compute(P, L[l], j, io.mode);
+            if (L[l].i <= P.nx) {
+              if (lean) P2March<T>::template fin_load<true>(P, io, L[l], j, F[l]);
+              else P2March<T>::fin_load(P, io, L[l], j, F[l]);
+            }
+        for (int l = 0; l < 32; ++l) {
+          if (lean) P2March<T>::template compute<true>(P, L[l], j, io.mode);
+          else P2March<T>::compute(P, L[l], j, io.mode);
+        }
         up();
         if (j >= js)
           for (int l = 1; l < 32; ++l)
-            if (L[l].i <= P.nx) P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, F[l], acc);
+            if (L[l].i <= P.nx) {
+              if (lean) P2March<T>::template finish<true>(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, F[l], acc);
+              else P2March<T>::finish(P, io, L[l], j, j == P.ny - 1 ? 3 : 2, F[l], acc);
+            }
         if (!more) break;
         ++j;
         for (int l = 0; l < 32; ++l) {
@@ -184,6 +208,8 @@ P2Params<T> p2params(int nx, int ny, double hx, double hy, double lam, double mu
 }  // namespace
 
 extern "C" {
+
+long emu_lean_warps() { return lean_warps; }
 
 int emu_dir_ints() { return kDirInts; }
 

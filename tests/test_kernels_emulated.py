@@ -54,6 +54,20 @@ def test_p2_apply_fp64_matches_oracle(case):
     assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("case", CASES[3:])
+def test_p2_lean_warps_match_oracle(case):
+    """Interior warps skip every per-node test (P2March::lean_region); on these lattices
+    some warps take that path and the result still matches the oracle."""
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    for prec, tol in ((0, 1e-12), (1, 2e-5)):
+        y = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=prec)
+        assert emu.lean_warps() > 0
+        ref = o.apply_state(xi, u)
+        assert np.max(np.abs(y - ref)) <= tol * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("case", CASES[:3])
 def test_p2_apply_fp32_matches_oracle(case):
     W, H, nx, ny, sides, p = case
@@ -275,18 +289,20 @@ def test_level_chain_shapes():
     assert c2["nx"] == 3 and c2["dir"][2] == 2
 
 
-@pytest.mark.parametrize("level", ["p2", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil", "p1x2-march",
+@pytest.mark.parametrize("level", ["p2", "p2-wide", "p1x2", "p1x1", "p1x2-stencil", "p1x1-stencil", "p1x2-march",
                                    "p1x1-march", "p1x1-dir", "p1x1-dir-stencil", "p1x1-dir-march"])
 def test_fused_smoothing_steps_match_composition(level):
     """PRE / RES / FIRST / POST2 against the same steps composed from plain applies
     (P1 levels also through their assembled 7-point stencil and the column march).
     The "-dir" scalar levels are the fluid velocity preconditioner's: every side
-    clamped, unit stiffness and a mass coefficient spanning six decades."""
+    clamped, unit stiffness and a mass coefficient spanning six decades.  "p2-wide"
+    is wide and tall enough for interior warps, which take the lean phases."""
     stencil = level.endswith("-stencil")
     march = level.endswith("-march")
     dirichlet = "-dir" in level
-    level = level.replace("-stencil", "").replace("-march", "").replace("-dir", "")
-    nx, ny, hx, hy, p = 34, 10, 0.05, 0.05, 3.0
+    wide = level.endswith("-wide")
+    level = level.replace("-stencil", "").replace("-march", "").replace("-dir", "").replace("-wide", "")
+    nx, ny, hx, hy, p = (70, 17, 0.025, 0.05, 3.0) if wide else (34, 10, 0.05, 0.05, 3.0)
     lam, mu = lame(1.0, 0.3)
     rng = np.random.default_rng(21)
     xi = rng.uniform(0.05, 1.0, (nx + 1) * (ny + 1))
@@ -323,6 +339,8 @@ def test_fused_smoothing_steps_match_composition(level):
     # PRE
     emu.smooth("pre", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
                march=march, kM=kM)
+    if wide:
+        assert emu.lean_warps() > 0
     d0 = cheb[0] * dinv * b
     ref = d0 + cheb[1] * d0 + cheb[2] * dinv * (b - A(d0))
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))
@@ -347,6 +365,8 @@ def test_fused_smoothing_steps_match_composition(level):
     assert np.max(np.abs(bufs["x2"] - x2_ref)) <= 1e-12 * np.max(np.abs(x2_ref))
     emu.smooth("post2", p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, stencil=stencil,
                march=march, kM=kM)
+    if wide:
+        assert emu.lean_warps() > 0
     r1 = r0 - A(dd0)
     ref = u + dd0 + cheb[1] * dd0 + cheb[2] * dinv * r1
     assert np.max(np.abs(bufs["x"] - ref)) <= 1e-12 * np.max(np.abs(ref))

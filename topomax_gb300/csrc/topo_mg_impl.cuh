@@ -91,41 +91,53 @@ __device__ inline void pcg_check_dev(PcgDev* dv, cudaGraphConditionalHandle h, i
   if (use_cond) cudaGraphSetConditional(h, st == 1 ? 1u : 0u);
 }
 
+// One warp's march over cell rows js .. je-1 (see P2March).  LEAN: the warp's
+// region passed P2March::lean_region, so the phases make no per-node tests.
+template <class T, int MODE, bool LEAN>
+__device__ __forceinline__ void p2_march_run(const P2Params<T>& P, const T* __restrict__ xi, const P2Io<T>& io,
+                                             int lane, int js, int je, T (&acc)[2]) {
+  constexpr bool OPERAND = MODE != kP2Diag;
+  P2Lane<T> L;
+  P2March<T>::begin(P, L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
+  const bool owner = lane > 0 && L.i <= P.nx;
+  int j = js > 0 ? js - 1 : 0;
+  P2March<T>::template load<0, LEAN>(P, io, xi, L, j);
+  P2March<T>::template load_mass<LEAN>(P, L.K, L.i, j, L.M);
+  p2m_exchange_down<T, 0, OPERAND>(L);
+  P2Next<T> N;
+  for (;;) {
+    const bool more = j + 1 < je;
+    if (more) P2March<T>::template prefetch<LEAN>(P, io, xi, L, j + 1, N);  // in flight during this step's arithmetic
+    const bool fin = owner && j >= js;
+    typename P2March<T>::Fin F;
+    if (MODE != kP2Apply && MODE != kP2Diag && fin) P2March<T>::template fin_load<LEAN>(P, io, L, j, F);
+    P2March<T>::template compute<LEAN>(P, L, j, MODE);
+    p2m_exchange_up<T>(L, lane);
+    if (fin) P2March<T>::template finish<LEAN>(P, io, L, j, j == P.ny - 1 ? 3 : 2, F, acc);
+    if (!more) break;
+    ++j;
+    P2March<T>::advance(L);
+    P2March<T>::take(L, N);
+    p2m_exchange_down<T, 1, OPERAND>(L);
+  }
+}
+
 template <class T, int MODE>
 __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
   TOPO_PDL_ENTRY();
   io.mode = MODE;  // compile-time mode: the per-node switches fold
   P2March<T>::prepare(io);
-  constexpr bool OPERAND = MODE != kP2Diag;
   const int lane = threadIdx.x & 31;
   const int js = (blockIdx.y * P2M_WARPS + (threadIdx.x >> 5)) * seg;
   T acc[2] = {T(0), T(0)};  // fused CG reductions (P2Io::fuse)
   if (js < P.ny) {  // whole warp: warps past the last segment only join the reduction
     const int je = min(js + seg, P.ny);
-    P2Lane<T> L;
-    P2March<T>::begin(L, int(blockIdx.x) * P2M_OWN - 1 + lane, lane == 31);
-    const bool owner = lane > 0 && L.i <= P.nx;
-    int j = js > 0 ? js - 1 : 0;
-    P2March<T>::template load<0>(P, io, xi, L, j);
-    P2March<T>::load_mass(P, L.i, j, L.M);
-    p2m_exchange_down<T, 0, OPERAND>(L);
-    P2Next<T> N;
-    for (;;) {
-      const bool more = j + 1 < je;
-      if (more) P2March<T>::prefetch(P, io, xi, L, j + 1, N);  // in flight during this step's arithmetic
-      const bool fin = owner && j >= js;
-      typename P2March<T>::Fin F;
-      if (MODE != kP2Apply && MODE != kP2Diag && fin) P2March<T>::fin_load(P, io, L, j, F);
-      P2March<T>::compute(P, L, j, MODE);
-      p2m_exchange_up<T>(L, lane);
-      if (fin) P2March<T>::finish(P, io, L, j, j == P.ny - 1 ? 3 : 2, F, acc);
-      if (!more) break;
-      ++j;
-      P2March<T>::advance(L);
-      P2March<T>::take(L, N);
-      p2m_exchange_down<T, 1, OPERAND>(L);
-    }
+    // warp-uniform: the same cell columns and rows for all lanes
+    if (P2March<T>::lean_region(P, int(blockIdx.x) * P2M_OWN - 1, js > 0 ? js - 1 : 0, je))
+      p2_march_run<T, MODE, true>(P, xi, io, lane, js, je, acc);
+    else
+      p2_march_run<T, MODE, false>(P, xi, io, lane, js, je, acc);
   }
   if constexpr (MODE == kP2Apply || MODE == kP2Post2) {
     if (io.fuse != kFuseNone) {

@@ -264,11 +264,24 @@ struct P2Io {
   T cf[3];             // B.cheb[0..2], copied in by P2March::prepare (registers, not re-read)
 };
 
+// Which of a lane's cells and nodes exist and which nodes are clamped.  A lane
+// keeps its columns for the whole march, so this is set once (P2March::begin);
+// the node rows of every step lie inside the lattice (2j + r <= 2 ny), so only
+// their clamps vary, and those are the same for the whole warp.
+struct P2Mask {
+  bool cell;      // cell column i inside the mesh
+  bool col[3];    // node columns 2i, 2i+1, 2i+2 inside the lattice
+  bool ccl[3];    // ... on a clamped left or right side
+  bool vcol[2];   // vertex columns i, i+1 inside the lattice
+  bool pts;       // clamped points exist: tested node by node
+};
+
 template <class T>
 struct P2Lane {
   int i;          // cell column
   bool edge;      // last lane of the warp: loads its column 2 itself
-  T U[3][3][2];   // operand at nodes (2i+c, 2j+r), zero at clamped nodes
+  P2Mask K;       // the lane's cells and node columns
+  T U[3][3][2];   // operand at nodes (2i+c, 2j+r) (raw at clamped nodes, zero outside the lattice)
   T X[2][2];      // density at vertices (i+c, j+r)
   T A[3][3][2];   // element results at the same nodes
   T M[12];        // r-weighted mass matrices of the cell (when precomputed), [o][k]
@@ -331,24 +344,55 @@ struct P2March {
     }
   }
 
-  // operand at node (a,b); zero outside the lattice and at clamped nodes
-  TOPO_HD static void fetch(const P2Params<T>& P, const P2Io<T>& io, int a, int b, T (&v)[2]) {
-    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
-    v[0] = v[1] = T(0);
-    if (a >= 0 && a < NX && b >= 0 && b < NY && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b))) {
-      operand(io, size_t(b) * NX + a, v);
-      if (io.mode == kP2First && io.xc) prolong(P, io.xc, a, b, v);
-    }
+  // Whether a warp's whole march runs on the lean path: every cell it touches
+  // (columns i0 .. i0+31, rows j0 .. je-1) lies inside the mesh, its nodes stay
+  // below the top node row, and none of its nodes is clamped.  The lean phases
+  // then make no per-node tests.  (Indices are 32-bit on both paths: a lattice
+  // holds far fewer than 2^31 values.)
+  TOPO_HD static bool lean_region(const P2Params<T>& P, int i0, int j0, int je) {
+    const int a_lo = 2 * i0, a_hi = 2 * (i0 + 31) + 2, b_lo = 2 * j0, b_hi = 2 * je;
+    const Dir& d = P.dir;
+    return i0 >= 0 && i0 + 31 < P.nx && j0 >= 0 && je < P.ny && d.npts == 0 && !(d.x_lo && a_lo == 0) &&
+           a_hi < d.x_hi_from && !(d.y_lo && b_lo == 0) && b_hi < d.y_hi_from;
   }
 
-  TOPO_HD static T density(const P2Params<T>& P, const T* xi, int i, int j) {
-    const int VX = P.nx + 1, VY = P.ny + 1;
-    return (i >= 0 && i < VX && j >= 0 && j < VY) ? xi[size_t(j) * VX + i] : T(0);
+  // node row b on a clamped bottom or top side (the same for every lane)
+  TOPO_HD static bool row_clamped(const P2Params<T>& P, int b) {
+    return (P.dir.y_lo && b == 0) || b >= P.dir.y_hi_from;
+  }
+
+  // node (a, b) = (2i + c, b) of the lane with mask K is clamped (an identity row)
+  TOPO_HD static bool clamped(const P2Params<T>& P, const P2Mask& K, int c, int a, int b) {
+    return K.ccl[c] || row_clamped(P, b) || (K.pts && is_clamped(P.dir, a, b));
+  }
+
+  // Operand at node (a, b) = (2i + c, b) of the lane, zero outside the lattice.
+  // At a clamped node it is the raw operand (without the First mode's coarse
+  // correction): the element phase zeroes it (tri), and the finish phase uses it
+  // as the identity row's value without loading it again.  LEAN: the node is
+  // known to be inside and free.
+  template <bool LEAN = false>
+  TOPO_HD static void fetch(const P2Params<T>& P, const P2Io<T>& io, const P2Mask& K, int c, int a, int b,
+                            T (&v)[2]) {
+    const int NX = 2 * P.nx + 1;
+    if (!LEAN && !K.col[c]) {
+      v[0] = v[1] = T(0);
+      return;
+    }
+    operand(io, unsigned(b) * unsigned(NX) + unsigned(a), v);
+    if (io.mode == kP2First && io.xc && (LEAN || !clamped(P, K, c, a, b))) prolong(P, io.xc, a, b, v);
+  }
+
+  // density at vertex (i + c, j) of the lane (rows j <= ny always)
+  template <bool LEAN = false>
+  TOPO_HD static T density(const P2Params<T>& P, const T* xi, const P2Mask& K, int c, int i, int j) {
+    if (!LEAN && !K.vcol[c]) return T(0);
+    return xi[unsigned(j) * unsigned(P.nx + 1) + unsigned(i + c)];
   }
 
   // loads of step j: operand rows R0..2 and density rows (R0 == 0 ? 0 : 1)..1,
   // columns 0 (and, on the edge lane, the last column)
-  template <int R0>
+  template <int R0, bool LEAN = false>
   TOPO_HD static void load(const P2Params<T>& P, const P2Io<T>& io, const T* xi, P2Lane<T>& L, int j) {
     if (io.mode != kP2Diag) {
 #if defined(__CUDA_ARCH__)
@@ -356,22 +400,23 @@ struct P2March {
 #endif
       for (int r = R0; r <= 2; ++r) {
         const int b = 2 * j + r;
-        fetch(P, io, 2 * L.i, b, L.U[r][0]);
-        fetch(P, io, 2 * L.i + 1, b, L.U[r][1]);
-        if (L.edge) fetch(P, io, 2 * L.i + 2, b, L.U[r][2]);
+        fetch<LEAN>(P, io, L.K, 0, 2 * L.i, b, L.U[r][0]);
+        fetch<LEAN>(P, io, L.K, 1, 2 * L.i + 1, b, L.U[r][1]);
+        if (L.edge) fetch<LEAN>(P, io, L.K, 2, 2 * L.i + 2, b, L.U[r][2]);
       }
     }
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
     for (int r = (R0 == 0 ? 0 : 1); r <= 1; ++r) {
-      L.X[r][0] = density(P, xi, L.i, j + r);
-      if (L.edge) L.X[r][1] = density(P, xi, L.i + 1, j + r);
+      L.X[r][0] = density<LEAN>(P, xi, L.K, 0, L.i, j + r);
+      if (L.edge) L.X[r][1] = density<LEAN>(P, xi, L.K, 1, L.i, j + r);
     }
   }
 
-  template <int O>
-  TOPO_HD static void tri(const P2Params<T>& P, P2Lane<T>& L, int j, int mode) {
+  // Z: the step's clamped nodes (their operand enters the element as zero)
+  template <int O, bool LEAN = false>
+  TOPO_HD static void tri(const P2Params<T>& P, P2Lane<T>& L, const bool (&Z)[3][3], int mode) {
     const T xe[3] = {L.X[P1Off<O, 0>::b][P1Off<O, 0>::a], L.X[P1Off<O, 1>::b][P1Off<O, 1>::a],
                      L.X[P1Off<O, 2>::b][P1Off<O, 2>::a]};
     T y[6][2];
@@ -379,9 +424,9 @@ struct P2March {
       tri_diag(O, xe, P, y);
     } else {
       T ue[6][2];
-#define TOPO_LD(K)                                             \
-  ue[K][0] = L.U[P2Off<O, K>::b][P2Off<O, K>::a][0];           \
-  ue[K][1] = L.U[P2Off<O, K>::b][P2Off<O, K>::a][1];
+#define TOPO_LD(K)                                                                                      \
+  ue[K][0] = (!LEAN && Z[P2Off<O, K>::b][P2Off<O, K>::a]) ? T(0) : L.U[P2Off<O, K>::b][P2Off<O, K>::a][0]; \
+  ue[K][1] = (!LEAN && Z[P2Off<O, K>::b][P2Off<O, K>::a]) ? T(0) : L.U[P2Off<O, K>::b][P2Off<O, K>::a][1];
       TOPO_LD(0) TOPO_LD(1) TOPO_LD(2) TOPO_LD(3) TOPO_LD(4) TOPO_LD(5)
 #undef TOPO_LD
       // difference form: the element operator annihilates translations, so
@@ -413,15 +458,15 @@ struct P2March {
 #undef TOPO_ST
   }
 
-  // mass matrices of cell (i, j) (zero outside the mesh)
-  TOPO_HD static void load_mass(const P2Params<T>& P, int i, int j, T (&M)[12]) {
+  // mass matrices of the lane's cell (i, j) (zero outside the mesh; 0 <= j < ny always)
+  template <bool LEAN = false>
+  TOPO_HD static void load_mass(const P2Params<T>& P, const P2Mask& K, int i, int j, T (&M)[12]) {
     if (!P.rmass) return;
-    const bool in = i >= 0 && i < P.nx && j >= 0 && j < P.ny;
-    if (!in) {
+    if (!LEAN && !K.cell) {
       for (int k = 0; k < 12; ++k) M[k] = T(0);
       return;
     }
-    const T* src = P.rmass + (size_t(j) * P.nx + i) * 12;
+    const T* src = P.rmass + (unsigned(j) * unsigned(P.nx) + unsigned(i)) * 12u;
 #if defined(__CUDA_ARCH__)
     if constexpr (sizeof(T) == 4) {
       const float4* q = reinterpret_cast<const float4*>(src);
@@ -448,6 +493,7 @@ struct P2March {
   }
 
   // the loads of step j (operand rows 1, 2, density row 1, mass matrices)
+  template <bool LEAN = false>
   TOPO_HD static void prefetch(const P2Params<T>& P, const P2Io<T>& io, const T* xi, const P2Lane<T>& L, int j,
                                P2Next<T>& N) {
     if (io.mode != kP2Diag) {
@@ -456,14 +502,14 @@ struct P2March {
 #endif
       for (int r = 1; r <= 2; ++r) {
         const int b = 2 * j + r;
-        fetch(P, io, 2 * L.i, b, N.U[r - 1][0]);
-        fetch(P, io, 2 * L.i + 1, b, N.U[r - 1][1]);
-        if (L.edge) fetch(P, io, 2 * L.i + 2, b, N.U[r - 1][2]);
+        fetch<LEAN>(P, io, L.K, 0, 2 * L.i, b, N.U[r - 1][0]);
+        fetch<LEAN>(P, io, L.K, 1, 2 * L.i + 1, b, N.U[r - 1][1]);
+        if (L.edge) fetch<LEAN>(P, io, L.K, 2, 2 * L.i + 2, b, N.U[r - 1][2]);
       }
     }
-    N.X[0] = density(P, xi, L.i, j + 1);
-    if (L.edge) N.X[1] = density(P, xi, L.i + 1, j + 1);
-    load_mass(P, L.i, j, N.M);
+    N.X[0] = density<LEAN>(P, xi, L.K, 0, L.i, j + 1);
+    if (L.edge) N.X[1] = density<LEAN>(P, xi, L.K, 1, L.i, j + 1);
+    load_mass<LEAN>(P, L.K, L.i, j, N.M);
   }
 
   // after advance(): the prefetched loads become rows 1, 2 of the step
@@ -476,11 +522,16 @@ struct P2March {
     for (int k = 0; k < 12; ++k) L.M[k] = N.M[k];
   }
 
-  // element results of cell (L.i, j), both triangles
+  // element results of cell (L.i, j), both triangles (0 <= j < ny always)
+  template <bool LEAN = false>
   TOPO_HD static void compute(const P2Params<T>& P, P2Lane<T>& L, int j, int mode) {
-    if (L.i < 0 || L.i >= P.nx || j < 0 || j >= P.ny) return;
-    tri<0>(P, L, j, mode);
-    tri<1>(P, L, j, mode);
+    if (!LEAN && !L.K.cell) return;
+    bool Z[3][3] = {};
+    if (!LEAN)
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Z[r][c] = clamped(P, L.K, c, 2 * L.i + c, 2 * j + r);
+    tri<0, LEAN>(P, L, Z, mode);
+    tri<1, LEAN>(P, L, Z, mode);
   }
 
   // finish node (a,b) with the complete sum r (clamped rows act as identity rows)
@@ -490,16 +541,17 @@ struct P2March {
   struct Fin {
     T v[4][3][2];
   };
+  template <bool LEAN = false>
   TOPO_HD static void fin_load(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, Fin& F) {
-    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+    const int NX = 2 * P.nx + 1;
     const SmoothBufs<T>& B = io.B;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
     for (int q = 0; q < 4; ++q) {
-      const int a = 2 * L.i + (q & 1), b = 2 * j + (q >> 1);
-      if (a < 0 || a >= NX || b >= NY) continue;
-      const size_t i = 2 * (size_t(b) * NX + a);
+      const int a = 2 * L.i + (q & 1), b = 2 * j + (q >> 1);  // b < NY always
+      if (!LEAN && !L.K.col[q & 1]) continue;
+      const size_t i = size_t(2u * (unsigned(b) * unsigned(NX) + unsigned(a)));
       switch (io.mode) {
         case kP2Pre:
         case kP2First:
@@ -535,19 +587,19 @@ struct P2March {
     }
   }
 
-  // v: the node's finish vectors (Fin)
-  TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, const T (&sum)[2],
+  // v: the node's finish vectors (Fin); cl: the node is clamped (an identity row);
+  // u: the node's operand as fetched (raw at a clamped node)
+  TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, bool cl, const T (&sum)[2],
                                   const T (&u)[2], const T (&v)[3][2], T (&acc)[2]) {
     const int NX = 2 * P.nx + 1;
-    const size_t n = size_t(b) * NX + a, i = 2 * n;
-    const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
+    const size_t n = size_t(unsigned(b) * unsigned(NX) + unsigned(a)), i = 2 * n;
     if (io.mode == kP2Diag) {
       st2(io.y + i, cl ? T(1) : sum[0], cl ? T(1) : sum[1]);
       return;
     }
-    T un[2] = {u[0], u[1]}, r[2] = {sum[0], sum[1]};
+    const T un[2] = {u[0], u[1]};
+    T r[2] = {sum[0], sum[1]};
     if (cl) {
-      operand(io, n, un);  // the loaded copy is zero at clamped nodes
       r[0] = un[0];
       r[1] = un[1];
     }
@@ -604,26 +656,29 @@ struct P2March {
   // finish the lane's nodes of rows 0 .. nrows-1 (nrows = 3 on the last cell row)
   // acc: the lane's partial sums of the fused reductions, in the operator's
   // precision (a few dozen terms; blocks combine them in FP64)
+  // (LEAN: nrows is 2 and every node is inside and free)
+  template <bool LEAN = false>
   TOPO_HD static void finish(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, int nrows,
                              const Fin& F, T (&acc)[2]) {
-    const int NX = 2 * P.nx + 1, NY = 2 * P.ny + 1;
+    const int NX = 2 * P.nx + 1;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-    for (int r = 0; r < 3; ++r) {
-      if (r >= nrows || 2 * j + r >= NY) continue;
+    for (int r = 0; r < (LEAN ? 2 : 3); ++r) {
+      if (!LEAN && r >= nrows) continue;  // 2j + r < NY for r < nrows
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
       for (int c = 0; c < 2; ++c) {
         const int a = 2 * L.i + c, b = 2 * j + r;
-        if (a >= NX) continue;
+        if (!LEAN && !L.K.col[c]) continue;
+        const bool cl = !LEAN && clamped(P, L.K, c, a, b);
         if (r < 2) {
-          finish_node(P, io, a, b, L.A[r][c], L.U[r][c], F.v[2 * r + c], acc);
+          finish_node(P, io, a, b, cl, L.A[r][c], L.U[r][c], F.v[2 * r + c], acc);
         } else {  // row 2: only on the last cell row
           T v[3][2] = {};
           fin_load_node(io, 2 * (size_t(b) * NX + a), v);
-          finish_node(P, io, a, b, L.A[r][c], L.U[r][c], v, acc);
+          finish_node(P, io, a, b, cl, L.A[r][c], L.U[r][c], v, acc);
         }
       }
     }
@@ -645,9 +700,19 @@ struct P2March {
     L.X[0][1] = L.X[1][1];
   }
 
-  TOPO_HD static void begin(P2Lane<T>& L, int i, bool edge) {
+  TOPO_HD static void begin(const P2Params<T>& P, P2Lane<T>& L, int i, bool edge) {
     L.i = i;
     L.edge = edge;
+    const int NX = 2 * P.nx + 1;
+    const Dir& d = P.dir;
+    L.K.cell = i >= 0 && i < P.nx;
+    for (int c = 0; c < 3; ++c) {
+      const int a = 2 * i + c;
+      L.K.col[c] = a >= 0 && a < NX;
+      L.K.ccl[c] = (d.x_lo && a == 0) || a >= d.x_hi_from;
+    }
+    for (int c = 0; c < 2; ++c) L.K.vcol[c] = i + c >= 0 && i + c <= P.nx;
+    L.K.pts = d.npts > 0;
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c)
         for (int d = 0; d < 2; ++d) L.U[r][c][d] = L.A[r][c][d] = T(0);
