@@ -262,14 +262,16 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(nx, ny):
-    """DRAM bytes per launch of the FP32 operator from the committed ncu summary, scaled to this grid."""
+def ncu_counts(nx, ny):
+    """DRAM bytes and executed FP32 thread instructions per launch of the FP32 operator from
+    the committed ncu summary, scaled to this grid by the dof count."""
     try:
         with open(os.path.join(ROOT, "profiles", "p2_operator_fp32_traffic.json")) as f:
             d = json.load(f)
-        return d["bytes_per_launch"] * dofs(nx, ny) / d["dofs"]
+        s = dofs(nx, ny) / d["dofs"]
+        return d["bytes_per_launch"] * s, d.get("fp32_thread_inst_per_launch", 0) * s or None
     except Exception:
-        return None
+        return None, None
 
 
 def main():
@@ -448,10 +450,9 @@ def main():
     # --- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
     alg_bytes = 2 * dofs(args.nx, args.ny) * 4 + nv * 4
-    flops = 104.0 * 7 * 2 * args.nx * args.ny
     op = float(np.mean(op_ms))
     achieved = alg_bytes / (op * 1e-3) / 1e9
-    traffic = ncu_traffic(args.nx, args.ny)
+    traffic, fp32_inst = ncu_counts(args.nx, args.ny)
 
     if rank != 0:
         if dist is not None:
@@ -480,9 +481,10 @@ def main():
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
                      "launch_ms": op,
-                     # the same launch in FP32 flops: 104 flops per quadrature point of
-                     # the 7-point rule per triangle (the element product of the form)
-                     "algorithmic_flops": flops, "achieved_tflops": flops / (op * 1e-3) / 1e12},
+                     # FP32 work the launch executes (ncu instruction counters, an FMA
+                     # counted once), over this run's CUDA-event launch time
+                     "executed_fp32_inst": fp32_inst,
+                     "executed_fp32_tinst_per_s": fp32_inst / (op * 1e-3) / 1e12 if fp32_inst else None},
         "cpu_baseline": cpu,
         "same_grid": same_grid,
         "gpu_launches": int(nlaunch),
