@@ -186,15 +186,19 @@ int topo_load_vector(topo_ctx* ctx, double* b, topo_stream_t stream);
 #define TOPO_NOALLOC_MAX_TRIANGLES (1 << 20)
 
 /* topo_sensitivity_rhs without a context and without any device allocation -- it has no
- * counterpart in the reference.  For callers that cannot call cudaMalloc (code recording a
- * stream into a CUDA graph, hosts that only hand out memory from their own fixed pool):
+ * counterpart in the reference.  For callers that cannot call cudaMalloc (hosts that only hand
+ * out device memory from their own fixed pool, callers inside a fixed memory budget, loops that
+ * must not pay an allocation's device-wide synchronisation):
  * the per-triangle scratch is a fixed 12 MiB device array inside this library, held by every
  * GPU that loads it until the process exits.  Computes b exactly as topo_sensitivity_rhs on a
  * TOPO_PREC_MIXED context of the same grid and material (FP64 inputs/outputs, FP32 quadrature).
  * Returns TOPO_ERR_ARG when 2*nx*ny > TOPO_NOALLOC_MAX_TRIANGLES.  The first call on a device
  * looks up the array's device address (make it before any stream capture on that device).
  * Every call shares the one array: calls whose work overlaps on the GPU (different streams,
- * threads or processes sharing the context) race and must be serialised by the caller. */
+ * threads or processes sharing the context) race and must be serialised by the caller.
+ * The status covers this call's launch errors; a CUDA error already pending on the calling
+ * thread is left in place and the call returns TOPO_ERR_CUDA without launching.  The device
+ * address is looked up once per process: do not use the entry point across a cudaDeviceReset. */
 int topo_sensitivity_rhs_noalloc(const topo_grid_desc* grid, double young_modulus, double poisson_ratio,
                                  double penalization, double penal_min, const double* u, const double* xi,
                                  double* b, topo_stream_t stream);

@@ -300,3 +300,42 @@ def test_reference_design_vector_at_the_api(precision):
             assert np.max(np.abs(xi - prob.filter.apply(np.array(gold["rho_dolfin"])).vector()[:])) == 0
     assert abs(results["dolfin"] - gold["objective"]) <= 1e-6 * gold["objective"]
     assert abs(results["lattice"] - gold["objective"]) > 1e-3 * gold["objective"]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_filter_manufactured_solution_converges(precision):
+    """tests/test_filter.py:37-60 on the GPU filter: rho = (8 eps^2 pi^2 + 1) cos(2 pi x)
+    cos(2 pi y) interpolated on the unit square with eps = e / pi filters to cos(2 pi x)
+    cos(2 pi y); the L2 error (12-point rule per triangle, the exact solution evaluated at
+    the quadrature points) over N = 10, 20, ..., 90 passes the reference's own test:
+    tests/utils.py get_convergance returns Polynomial.fit(log N, log error, 1).coef[1],
+    the slope in the fit's scaled window ([log 10, log 90] -> [-1, 1], a factor 1.0986),
+    and requires it <= -2.  The unscaled slope is also checked (<= -1.9; the oracle's is
+    -1.96).  At N = 40 the filtered field equals the oracle's."""
+    import topomax_gb300 as tg
+    from oracle.fem import rule_degree6
+    eps = np.e / np.pi
+    lam, w = rule_degree6()
+    errs = []
+    Ns = list(range(10, 91, 10))
+    for N in Ns:
+        L = Lattice(1.0, 1.0, N, N)
+        X, Y = L.vertex_coords()
+        rho = (8 * eps * eps * np.pi ** 2 + 1) * np.cos(2 * np.pi * X) * np.cos(2 * np.pi * Y)
+        V = tg.FunctionSpace(tg.RectangleMesh(1.0, 1.0, N, N), "CG", 1, dof_order="lattice")
+        xi = tg.HelmholtzFilter(eps, V, precision=precision, rtol=1e-12).apply(rho).vector()[:]
+        e2 = 0.0
+        for o in (0, 1):
+            tv = L.triangle_vertices(o)
+            area, _ = L.triangle_geometry(o)
+            xq = lam @ X[tv].T                       # (12, T) quadrature points
+            yq = lam @ Y[tv].T
+            diff = lam @ xi[tv].T - np.cos(2 * np.pi * xq) * np.cos(2 * np.pi * yq)
+            e2 += area * float(w @ (diff ** 2).sum(axis=1))
+        errs.append(np.sqrt(e2))
+        if N == 40:
+            ref = FEMOracle(L, _design(width=1.0, height=1.0, filter_radius=eps)).filter_apply(rho)
+            assert np.max(np.abs(xi - ref)) <= 1e-10 * np.max(np.abs(ref))
+    fit = np.polynomial.Polynomial.fit(np.log(Ns), np.log(errs), 1)
+    assert fit.coef[1] <= -2
+    assert fit.convert().coef[1] <= -1.9

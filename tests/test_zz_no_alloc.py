@@ -1,8 +1,8 @@
 """The allocation-free sensitivity entry point against the context-based one.
 
 topo_sensitivity_rhs_noalloc serves callers that cannot allocate device
-memory (for example code recording a stream into a CUDA graph, or hosts with
-a fixed memory pool): it takes no context and uses a fixed scratch array
+memory (for example hosts with a fixed memory pool, or loops that must not pay
+cudaMalloc's device-wide synchronisation): it takes no context and uses a fixed scratch array
 inside the library.  It must reproduce topo_sensitivity_rhs of a mixed
 precision context on the same inputs, on consecutive calls (the shared
 scratch keeps the previous call's contents), and refuse meshes larger than

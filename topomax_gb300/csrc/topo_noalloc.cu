@@ -1,9 +1,9 @@
 // Sensitivity right-hand side for callers that must not allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code running while a stream is being
-// captured into a CUDA graph (an allocation there invalidates the capture),
-// hosts that hand out device memory only through their own fixed pool, and
-// embedded callers that run inside a caller-owned memory budget.  For them
+// Some callers cannot call cudaMalloc: hosts that hand out device memory only
+// through their own fixed pool, callers that run inside a fixed memory budget,
+// and loops that must not pay an allocation's device-wide synchronisation
+// (cudaMalloc and cudaFree can wait for all work on the device).  For them
 // this entry point needs no context and allocates nothing: the per-triangle
 // scratch lives in a fixed, file-scope device array that every GPU loading
 // this library holds until the process exits.
@@ -39,12 +39,18 @@ extern "C" int topo_sensitivity_rhs_noalloc(const topo_grid_desc* grid, double y
     return TOPO_ERR_ARG;
   const long long ntri = 2LL * grid->nx * grid->ny;
   if (ntri > TOPO_NOALLOC_MAX_TRIANGLES) return TOPO_ERR_ARG;  // scratch holds at most this many triangles
+  // an error already pending on this thread belongs to an earlier call: leave it in
+  // place for its owner and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return TOPO_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TOPO_ERR_CUDA;
   float* scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
   if (!scratch) {
     // once per device, with that device current (the first call on a device
-    // does this look-up: make it before any stream capture on that device)
+    // does this look-up: make it before any stream capture on that device).
+    // The address is kept for the life of the process: after a cudaDeviceReset
+    // the array may be reloaded elsewhere, so the entry point must not be used
+    // across a reset.
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_sens_scratch) != cudaSuccess || !p) return TOPO_ERR_CUDA;
     scratch = static_cast<float*>(p);
@@ -63,5 +69,6 @@ extern "C" int topo_sensitivity_rhs_noalloc(const topo_grid_desc* grid, double y
       nx, ny, 1.0 / hx, 1.0 / hy, float(lmbda), float(mu), float(area), make_penal<float>(penalization, penal_min),
       u, xi, scratch);
   k_vertex_gather3<float><<<vec_grid(nv, sms), kVecThreads, 0, s>>>(nx, ny, scratch, b);
+  // launch errors of this call only (nothing was pending before the launches)
   return cudaGetLastError() == cudaSuccess ? TOPO_OK : TOPO_ERR_CUDA;
 }
