@@ -80,6 +80,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps (the same design steps)")
     ap.add_argument("--c2-steps", type=int, default=50,
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
+    ap.add_argument("--kernel-steps", type=int, default=2,
+                    help="host-driven design iterations on the 2000x1000 grid timed kernel by kernel "
+                         "(HBM GB/s per kernel family); 0 skips them")
     ap.add_argument("--ref-grid", default="160x80",
                     help="grid of the CPU oracle legs (cpu_baseline, --impl reference) and of the GPU same-grid leg")
     ap.add_argument("--cpu-steps", type=int, default=5, help="timed oracle design iterations of cpu_baseline")
@@ -316,11 +319,12 @@ def main():
         prob._ctx._lib.topo_launch_count(prob._ctx.ptr, ctypes.byref(n))
         return n.value
 
-    def device_loop(prob, steps, warmup, time_operator=False, profile=False, space=None, start=None):
+    def device_loop(prob, steps, warmup, time_operator=False, profile=False, space=None, start=None, on_start=None):
         """Design-resident loop; returns per-step ms (CUDA events), objectives, launches, operator ms.
 
         With profile=True the timed steps are bracketed by cudaProfilerStart/Stop, so that a
-        profiler run with --profile-from-start off records exactly those launches."""
+        profiler run with --profile-from-start off records exactly those launches.  on_start()
+        runs once, after the warm-up steps."""
         lib = prob._ctx._lib
         rho = F.Function(space or V, (start if start is not None else rho0).cuda())
         psi = torch.log(rho.tensor / (1 - rho.tensor))
@@ -331,6 +335,8 @@ def main():
             if k == warmup:
                 barrier()
                 l0 = launches(prob)
+                if on_start is not None:
+                    on_start()
                 if profile:
                     torch.cuda.profiler.start()
             flush.zero_()
@@ -431,6 +437,9 @@ def main():
               "operator_launch_ms": float(np.mean(op2)), "operator_gbs": alg2 / (float(np.mean(op2)) * 1e-3) / 1e9}
         del prob2
         torch.cuda.empty_cache()
+        if args.kernel_steps > 0:
+            c2["kernels"] = kernel_table(tg, mesh2, V2, dom, par, rho02, device_loop, args, measured_peak()[0])
+            torch.cuda.empty_cache()
 
     # --- the CPU oracle legs' grid on the GPU: a same-grid comparison with cpu_baseline and --impl reference
     rnx, rny = _grid(args.ref_grid)
@@ -495,6 +504,49 @@ def main():
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def kernel_table(tg, mesh, V, dom, par, rho0, device_loop, args, peak):
+    """HBM GB/s per kernel family: a context with host-driven solves (TOPO_GRAPHS=0, the
+    same kernels as the recorded graphs) runs args.kernel_steps design iterations after one
+    warm-up with the library's kernel clock on, which brackets every annotated launch with
+    CUDA events and sums the algorithmic bytes of its family (no L2 flush between
+    launches: the vectors of the two finest levels exceed L2, the small levels stay
+    L2-resident as they do in the solve)."""
+    import ctypes
+    from topomax_gb300 import _capi
+    lib = _capi.load_library()
+    old = os.environ.get("TOPO_GRAPHS")
+    os.environ["TOPO_GRAPHS"] = "0"
+    try:
+        prob = tg.ElasticityProblem(mesh, V, dom, par, precision="mixed", rtol=args.rtol)
+        prob.set_penalization(PENALTY)
+        device_loop(prob, args.kernel_steps, 1, space=V, start=rho0, on_start=lambda: lib.topo_kernel_clock(1))
+        lib.topo_kernel_clock(0)
+        need = lib.topo_kernel_clock_report(None, 0)
+        buf = ctypes.create_string_buffer(int(need))
+        lib.topo_kernel_clock_report(buf, need)
+        del prob
+    finally:
+        if old is None:
+            os.environ.pop("TOPO_GRAPHS", None)
+        else:
+            os.environ["TOPO_GRAPHS"] = old
+    rows = []
+    for line in buf.value.decode().splitlines():
+        fam, level, n, ms, nbytes = line.split("\t")
+        n, ms, nbytes = int(n), float(ms), float(nbytes)
+        row = {"family": fam, "level": int(level), "launches_per_step": n / args.kernel_steps,
+               "us_per_launch": 1000.0 * ms / n, "ms_per_step": ms / args.kernel_steps}
+        if nbytes > 0:
+            row["bytes_per_launch"] = nbytes / n
+            row["gbs"] = nbytes / (ms * 1e-3) / 1e9
+            row["frac_of_peak"] = row["gbs"] / peak
+        rows.append(row)
+    rows.sort(key=lambda r: -r["ms_per_step"])
+    return {"method": "host-driven launches (TOPO_GRAPHS=0), each bracketed by CUDA events; algorithmic "
+                      "bytes per family as the library counts them; per design iteration over "
+                      f"{args.kernel_steps} iterations after 1 warm-up", "families": rows}
 
 
 class _E2ESolver:

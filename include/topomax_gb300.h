@@ -172,6 +172,19 @@ int topo_time_operator(topo_ctx* ctx, double* ms, topo_stream_t stream);
  * (kernels executed inside CUDA graphs are counted per execution). */
 int topo_launch_count(const topo_ctx* ctx, int64_t* launches);
 
+/* Measurement hook (no counterpart in the reference), process-wide and off by default:
+ * enable = 1 clears the totals and starts the kernel clock, 0 stops it.  While it runs, the
+ * solver's main kernels launched from the host (contexts created with TOPO_GRAPHS=0; launches
+ * on a capturing stream are never timed) are each bracketed by CUDA events and summed per
+ * family and level with their algorithmic bytes.  Not thread-safe: one measuring thread. */
+int topo_kernel_clock(int enable);
+
+/* Writes the kernel clock's totals as text, one line per family and level:
+ * "family<TAB>level<TAB>launches<TAB>milliseconds<TAB>algorithmic bytes<LF>", into buf when len
+ * is large enough (waits for the timed launches).  Returns the length needed including the
+ * terminating NUL, or TOPO_ERR_CUDA. */
+int64_t topo_kernel_clock_report(char* buf, int64_t len);
+
 /* y = M1 x with M1 the consistent CG1 mass matrix (the assembled (x, v) form, as the filter's
  * right-hand side FEM_src/filter.py:30-37 assembles it), FP64.  No counterpart as a function in
  * the reference: the Euclidean gradient of the compliance with respect to the nodal design is

@@ -339,3 +339,54 @@ def test_filter_manufactured_solution_converges(precision):
     fit = np.polynomial.Polynomial.fit(np.log(Ns), np.log(errs), 1)
     assert fit.coef[1] <= -2
     assert fit.convert().coef[1] <= -1.9
+
+
+def test_kernel_clock_times_host_driven_launches(monkeypatch):
+    """The kernel clock (topo_kernel_clock / topo_kernel_clock_report) times host-driven
+    launches only: a state solve of a context created with TOPO_GRAPHS=0 is itemised per
+    family with its algorithmic bytes (the P2 Apply launch moves 2 * dofs + vertices FP32
+    values), a context whose solves are recorded as graphs adds no P2 smoothing launches,
+    and the clock off records nothing."""
+    import ctypes
+    import torch
+    from topomax_gb300 import _capi
+    from topomax_gb300 import fem as F
+    lib = _capi.load_library()
+
+    def report():
+        need = lib.topo_kernel_clock_report(None, 0)
+        buf = ctypes.create_string_buffer(int(need))
+        assert lib.topo_kernel_clock_report(buf, need) == need
+        rows = {}
+        for line in buf.value.decode().splitlines():
+            fam, level, n, ms, nbytes = line.split("\t")
+            rows[(fam, int(level))] = (int(n), float(ms), float(nbytes))
+        return rows
+
+    d = _design()
+    nx, ny = 120, 60
+    xi = torch.full(((nx + 1) * (ny + 1),), 0.5, dtype=torch.float64, device="cuda")
+    monkeypatch.setenv("TOPO_GRAPHS", "0")
+    prob, V = _gpu_problem(d, nx, ny, rtol=1e-8)
+    prob.set_penalization(3.0)
+    lib.topo_kernel_clock(1)
+    prob.forward(F.Function(V, xi))
+    lib.topo_kernel_clock(0)
+    rows = report()
+    n, ms, nbytes = rows[("P2 march FP32 Apply", 0)]
+    assert n >= 1 and ms > 0
+    assert nbytes / n == (2 * 2 * (2 * nx + 1) * (2 * ny + 1) + (nx + 1) * (ny + 1)) * 4
+    assert ("P2 march FP32 Post2", 0) in rows and ("restriction", 0) in rows
+    # graph-recorded solves: the V-cycle launches run inside graphs and are not timed
+    monkeypatch.setenv("TOPO_GRAPHS", "1")
+    prob2, V2 = _gpu_problem(d, nx, ny, rtol=1e-8)
+    prob2.set_penalization(3.0)
+    prob2.forward(F.Function(V2, xi))          # records the graphs
+    lib.topo_kernel_clock(1)
+    prob2.forward(F.Function(V2, xi))
+    lib.topo_kernel_clock(0)
+    assert ("P2 march FP32 Post2", 0) not in report()
+    lib.topo_kernel_clock(1)                   # clears the totals
+    lib.topo_kernel_clock(0)
+    prob.forward(F.Function(V, xi))            # host-driven, clock off
+    assert report() == {}

@@ -923,6 +923,8 @@ int topo_sensitivity_rhs(topo_ctx* ctx, const double* u, const double* xi, doubl
     const size_t nt = size_t(2) * ctx->nx * ctx->ny;
     const double area = 0.5 * ctx->hx * ctx->hy;
     ctx->launches += 2;
+    // both kernels: u (FP64) and the design read, the CG1 right-hand side written
+    KClock kc(s, "sensitivity (moments + vertex gather)", 0, (2.0 * ctx->nn2 + 2.0 * ctx->nv) * 8.0);
     if (ctx->precision == TOPO_PREC_MIXED) {
       float* tri = static_cast<float*>(ctx->sens_tri);
       k_sens_tri<float><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
@@ -967,9 +969,17 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
     for (int launched = 0; launched < maxit;) {
       const int chunk = std::min(8, maxit - launched);
       ctx->launches += chunk;
-      for (int k = 0; k < chunk; ++k)
-        k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
-                                                          ctx->red.partials, ctx->red.counter, ctx->nstate);
+      for (int k = 0; k < chunk; ++k) {
+        if (launched == 0 && k == 0) {
+          // the clock times the first evaluation (later launches of a chunk may find Newton done)
+          KClock kc(s, "Newton evaluation (volume and its derivative)", 0, 2.0 * n * 8.0);
+          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
+                                                            ctx->red.partials, ctx->red.counter, ctx->nstate);
+        } else {
+          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
+                                                            ctx->red.partials, ctx->red.counter, ctx->nstate);
+        }
+      }
       launched += chunk;
       cudaMemcpyAsync(&hs, ctx->nstate, sizeof(hs), cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return ctx->cuda_check("projection");

@@ -11,6 +11,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "topo_kclock.h"
 #include "topo_mg.h"
 #include "topo_p1.cuh"
 #include "topo_p1march.cuh"
@@ -665,10 +666,49 @@ inline void prime_march_occupancy() {
   (void)p1_march_bps<T, 2, kP2Post2>();
 }
 
+// Kernel-clock names and algorithmic bytes of one launch (topo_kclock.h).  A mode
+// reads and writes whole level vectors: `vecs` of them, each of n values.
+inline const char* mode_name(int mode) {
+  switch (mode) {
+    case kP2Apply: return "Apply";
+    case kP2Diag: return "Diag";
+    case kP2Pre: return "Pre";
+    case kP2Res: return "Res";
+    case kP2First: return "First";
+    default: return "Post2";
+  }
+}
+template <class T>
+inline const char* p2_family(int mode) {
+  static const char* f32[6] = {"P2 march FP32 Apply", "P2 march FP32 Diag", "P2 march FP32 Pre",
+                               "P2 march FP32 Res", "P2 march FP32 First", "P2 march FP32 Post2"};
+  static const char* f64[6] = {"P2 march FP64 Apply", "P2 march FP64 Diag", "P2 march FP64 Pre",
+                               "P2 march FP64 Res", "P2 march FP64 First", "P2 march FP64 Post2"};
+  return (sizeof(T) == 4 ? f32 : f64)[mode];
+}
+// vectors of the level a smoothing or operator mode moves: operand(s) read, results written
+// (P2: Pre reads b, D^-1 and writes x; First also writes w; Post2 reads d, w, D^-1 (+ b when
+// it reduces r.r, r.z); P1 modes keep r between steps)
+inline int mode_vectors(int mode, bool p2, bool fused_rz) {
+  switch (mode) {
+    case kP2Apply: return 2;
+    case kP2Diag: return 1;
+    case kP2Pre: return 3;
+    case kP2Res: return 3;
+    case kP2First: return 5;
+    default: return p2 ? (fused_rz ? 5 : 4) : 5;
+  }
+}
+
 template <class T, int MODE>
 inline void launch_p2_mode(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
   int seg = 0;
   const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<T, MODE>(), seg);
+  const double n = 2.0 * (2 * P.nx + 1) * (2 * P.ny + 1), nv = double(P.nx + 1) * (P.ny + 1);
+  // the design (one value per vertex) plus, for First, the coarse correction (2 per vertex)
+  const double bytes = (mode_vectors(MODE, true, io.fuse == kFuseRZ) * n + nv + (MODE == kP2First ? 2 * nv : 0)) *
+                       sizeof(T);
+  KClock kc(s, p2_family<T>(MODE), 0, bytes);
   launch_pdl(k_p2_march<T, MODE>, g, P2M_THREADS, 0, s, P, xi, io, seg);
 }
 
@@ -688,6 +728,11 @@ template <class T, int NC, int MODE>
 inline void launch_p1_mode(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
   int seg = 0;
   const dim3 g = march_grid(P.nx, P.ny, p1_march_bps<T, NC, MODE>(), seg);
+  static const char* fam[6] = {"P1 march Apply", "P1 march Diag", "P1 march Pre", "P1 march Res", "P1 march First",
+                               "P1 march Post2"};
+  const double n = double(NC) * (P.nx + 1) * (P.ny + 1), ntri = 2.0 * P.nx * P.ny;
+  const double bytes = (mode_vectors(MODE, false, false) * n + ntri * ((P.kK ? 1 : 0) + (P.kM ? 1 : 0))) * sizeof(T);
+  KClock kc(s, fam[MODE], 1, bytes);
   launch_pdl(k_p1_march<T, NC, MODE>, g, P2M_THREADS, 0, s, P, io, seg);
 }
 
@@ -1062,6 +1107,11 @@ void MG<T>::apply(int l, const T* x, T* y, cudaStream_t s, bool op) {
   }
   const dim3 g = row_grid(L.NX, L.NY);
   const Lev& v = lv_[l];
+  // stencil operator: x read, y written, the stencil rows (unless one row is shared)
+  const double abytes = 2.0 * L.ndof() * sizeof(T) +
+                        (v.inner ? 0.0 : double((7 * L.NC * L.NC * sizeof(T) + 15) / 16 * 16) * L.nn());
+  KClock kc(s, (v.st && stencils_ready_) ? "P1 stencil Apply" : "P1 march Apply (operator)", l,
+            (v.st && stencils_ready_) ? abytes : 0.0);
   if (L.NC == 2) {
     if (v.st && stencils_ready_) {
       launch_pdl(k_p1_apply<T, 2, P1Stencil<T, 2>>, g, kRowThreads, 0, s, P1Stencil<T, 2>{L.nx, L.ny, L.dir, v.st, v.inner}, x, y);
@@ -1313,11 +1363,13 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   const int L = levels();
   const LevelSpec& S = specs_[l];
   if (l == cheb_coarse_ && cc_desc_) {
+    KClock kc(s, "coarse Chebyshev (one CTA)", l, 0.0);
     launch_pdl(k_coarse_cheb<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
     ++launches;
     return;
   }
   if (l == tail_ && tail_desc_ && use_tail) {
+    KClock kc(s, "tail V-cycle (one CTA)", l, 0.0);
     if (S.NC == 2)
       launch_pdl(k_tail_vcycle<T, 2>, 1, kTailThreads, tail_smem_, s, static_cast<const TailDesc<T, 2>*>(tail_desc_), b, x);
     else
@@ -1343,7 +1395,10 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Res;
     launch_p2_tile<T>(p2_, xi_, io, s);
-    launch_pdl(k_restrict<T, 2>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    {
+      KClock kc(s, "restriction", l, 2.0 * (double(S.nn()) + double(X.NXc) * X.NYc) * sizeof(T));
+      launch_pdl(k_restrict<T, 2>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    }
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
     io.mode = kP2First;  // adds the prolonged coarse correction to its operand on the fly
@@ -1363,17 +1418,34 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     return;
   }
   // the level's operator: assembled stencil when there is one, else on the fly
+  // algorithmic bytes of the transfers and of a smoothing step on a stencil level
+  const double nf = double(S.nn()) * S.NC, ncrs = double(X.NXc) * X.NYc * S.NC;
+  const double rbytes = (nf + ncrs) * sizeof(T), pbytes = (2 * nf + ncrs) * sizeof(T);
+  auto sbytes = [&](int mode) {
+    // the assembled stencil row of every node (7 NC x NC blocks, padded to 16 bytes), unless
+    // the level shares one interior row
+    const double row = double((7 * S.NC * S.NC * sizeof(T) + 15) / 16 * 16);
+    return mode_vectors(mode, false, false) * nf * sizeof(T) + (v.inner ? 0.0 : row * double(S.nn()));
+  };
   auto run = [&](auto nc_tag, const auto& P) {
     constexpr int NC = decltype(nc_tag)::value;
     using PP = std::decay_t<decltype(P)>;
-    launch_pdl(k_p1_smooth<T, NC, kP2Pre, PP>, gf, kRowThreads, 0, s, P, B);
-    launch_pdl(k_p1_smooth<T, NC, kP2Res, PP>, gf, kRowThreads, 0, s, P, B);
-    launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    constexpr bool ST = std::is_same<PP, P1Stencil<T, NC>>::value;
+    const char* fam_pre = ST ? "P1 stencil Pre" : "P1 node Pre";
+    const char* fam_res = ST ? "P1 stencil Res" : "P1 node Res";
+    const char* fam_first = ST ? "P1 stencil First" : "P1 node First";
+    const char* fam_post = ST ? "P1 stencil Post2" : "P1 node Post2";
+    { KClock kc(s, fam_pre, l, sbytes(kP2Pre)); launch_pdl(k_p1_smooth<T, NC, kP2Pre, PP>, gf, kRowThreads, 0, s, P, B); }
+    { KClock kc(s, fam_res, l, sbytes(kP2Res)); launch_pdl(k_p1_smooth<T, NC, kP2Res, PP>, gf, kRowThreads, 0, s, P, B); }
+    {
+      KClock kc(s, "restriction", l, rbytes);
+      launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    }
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x);
-    launch_pdl(k_p1_smooth<T, NC, kP2First, PP>, gf, kRowThreads, 0, s, P, B);
-    launch_pdl(k_p1_smooth<T, NC, kP2Post2, PP>, gf, kRowThreads, 0, s, P, B);
+    { KClock kc(s, "prolongation", l, pbytes); launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x); }
+    { KClock kc(s, fam_first, l, sbytes(kP2First)); launch_pdl(k_p1_smooth<T, NC, kP2First, PP>, gf, kRowThreads, 0, s, P, B); }
+    { KClock kc(s, fam_post, l, sbytes(kP2Post2)); launch_pdl(k_p1_smooth<T, NC, kP2Post2, PP>, gf, kRowThreads, 0, s, P, B); }
     launches += 3;
   };
   // large levels without a stencil: the column march (element products per cell)
@@ -1387,10 +1459,13 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     launch_p1_march<T, NC>(P, io, s);
     io.mode = kP2Res;
     launch_p1_march<T, NC>(P, io, s);
-    launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    {
+      KClock kc(s, "restriction", l, rbytes);
+      launch_pdl(k_restrict<T, NC>, gc, kRowThreads, 0, s, X, static_cast<const T*>(v.r), c.b, static_cast<const T*>(nullptr));
+    }
     launches += 3;
     vcycle_level(l + 1, c.b, c.x, s);
-    launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x);
+    { KClock kc(s, "prolongation", l, pbytes); launch_pdl(k_prolong_add<T, NC>, gf, kRowThreads, 0, s, X, static_cast<const T*>(c.x), x); }
     io.mode = kP2First;
     launch_p1_march<T, NC>(P, io, s);
     io.mode = kP2Post2;
@@ -1451,6 +1526,7 @@ template <class T>
 void MG<T>::pcg_xr(int g, cudaStream_t s) {
   const size_t n = specs_[0].ndof();
   T *r = pcg_[0], *q = pcg_[3];
+  KClock kc(s, "CG r -= alpha q", 0, 3.0 * n * sizeof(T));
   launch_pdl(k_pcg_r<T>, g, kVecThreads, 0, s, r, static_cast<const T*>(q), dev_, n);
 }
 
@@ -1459,6 +1535,8 @@ void MG<T>::pcg_p(int g, cudaStream_t s) {
   const size_t n = specs_[0].ndof();
   T *z = pcg_[1], *p = pcg_[2], *xi = pcg_[6];
   const PcgDev* dv = dev_;
+  // p read and written, z read, x (FP64 when accumulated so) read and written
+  KClock kc(s, "CG x += alpha p, p = z + beta p", 0, n * (3.0 * sizeof(T) + 2.0 * (xacc_ ? 8 : sizeof(T))));
   if (xacc_) launch_pdl(k_pcg_p<T, double>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), xacc_, dv, n);
   else launch_pdl(k_pcg_p<T, T>, g, kVecThreads, 0, s, p, static_cast<const T*>(z), xi, dv, n);
 }
@@ -1497,12 +1575,18 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
     return;
   }
   apply(0, p, q, s, true);
-  launch_pdl(k_dot<T, T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(p), static_cast<const T*>(q), n,
-             red_->partials, red_->counter, &dev_->pq);
+  {
+    KClock kc(s, "CG dot p.q", 0, 2.0 * n * sizeof(T));
+    launch_pdl(k_dot<T, T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(p), static_cast<const T*>(q), n,
+               red_->partials, red_->counter, &dev_->pq);
+  }
   pcg_xr(g, s);
   vcycle(r, z, s);
-  launch_pdl(k_dot2<T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(r), static_cast<const T*>(r),
-             static_cast<const T*>(r), static_cast<const T*>(z), n, red_->partials, red_->counter, &dev_->rr);
+  {
+    KClock kc(s, "CG dots r.r, r.z", 0, 2.0 * n * sizeof(T));
+    launch_pdl(k_dot2<T>, red_->blocks, kVecThreads, 0, s, static_cast<const T*>(r), static_cast<const T*>(r),
+               static_cast<const T*>(r), static_cast<const T*>(z), n, red_->partials, red_->counter, &dev_->rr);
+  }
   launch_pdl(k_pcg_check, 1, 1, 0, s, dev_, h, use_cond);
   pcg_p(g, s);
   launches += 5;
