@@ -80,6 +80,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps (the same design steps)")
     ap.add_argument("--c2-steps", type=int, default=50,
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
+    ap.add_argument("--c4-designs", type=int, default=64,
+                    help="designs of the ragged batch (domain 2x1, N in {100..300}); 0 skips the batch leg")
+    ap.add_argument("--c4-iterations", type=int, default=5, help="design iterations per design in the batch leg")
+    ap.add_argument("--c4-workers", type=int, default=8, help="concurrent workers (streams) of the batched run")
     ap.add_argument("--kernel-steps", type=int, default=2,
                     help="host-driven design iterations on the 2000x1000 grid timed kernel by kernel "
                          "(HBM GB/s per kernel family); 0 skips them")
@@ -441,6 +445,9 @@ def main():
             c2["kernels"] = kernel_table(tg, mesh2, V2, dom, par, rho02, device_loop, args, measured_peak()[0])
             torch.cuda.empty_cache()
 
+    # --- the ragged 64-design batch: batched (concurrent workers) against the un-batched loop
+    c4 = c4_batch(args) if args.c4_designs > 0 else None
+
     # --- the CPU oracle legs' grid on the GPU: a same-grid comparison with cpu_baseline and --impl reference
     rnx, rny = _grid(args.ref_grid)
     meshr = tg.RectangleMesh(2.0, 1.0, rnx, rny)
@@ -498,12 +505,50 @@ def main():
         "same_grid": same_grid,
         "gpu_launches": int(nlaunch),
         "c2_2000x1000": c2,
+        "c4_batch": c4,
         "clocks": ck,
         "solver_iterations": stats,
     }
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def c4_batch(args):
+    """The ragged design batch: args.c4_designs designs of the step-size sweep (domain 2x1,
+    N drawn from {100, 150, 200, 250, 300}, clamped bottom corners, circular body force,
+    p in {3, 4, 5}, random volume fraction and step size; seed 3), each run for
+    args.c4_iterations design iterations, once one design after another (the un-batched
+    loop) and once by args.c4_workers concurrent workers on their own streams.  Wall time
+    of each whole run, context set-up included; one design of every size runs first so
+    that both timed runs find the march tiles tuned."""
+    import torch
+    from topomax_gb300.batch import BatchItem, config4_designs, run_batch
+    items = config4_designs(args.c4_designs, seed=3)
+    seen = {}
+    for it in items:
+        seen.setdefault(it.N, it)
+    run_batch([BatchItem(it.N, it.design, it.name) for it in seen.values()], 1, workers=1, rtol=args.rtol)
+    out = {}
+    for leg, workers in (("sequential", 1), ("batched", args.c4_workers)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = run_batch(items, args.c4_iterations, workers=workers, rtol=args.rtol)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        iters = sum(h["iterations"] for r in res for h in r.history.values())
+        out[leg] = {"workers": workers, "s": dt, "design_iterations": iters,
+                    "design_iters_per_s": iters / dt, "errors": sum(1 for r in res if r.error)}
+        out[leg + "_histories"] = res
+    a, b = out.pop("sequential_histories"), out.pop("batched_histories")
+    keys = ("objectives", "deltas", "exit_condition", "iterations")  # not the wall times
+    same = all({p: {k: h[k] for k in keys} for p, h in x.history.items()}
+               == {p: {k: h[k] for k in keys} for p, h in y.history.items()} for x, y in zip(a, b))
+    sizes = sorted({it.N for it in items})
+    return {"workload": f"{len(items)} designs, domain 2x1, N in {sizes} (nx = 2N), "
+                        f"{args.c4_iterations} design iterations each, mixed precision, rtol {args.rtol}",
+            **out, "batched_over_sequential": out["sequential"]["s"] / out["batched"]["s"],
+            "histories_bitwise_equal": same}
 
 
 def kernel_table(tg, mesh, V, dom, par, rho0, device_loop, args, peak):

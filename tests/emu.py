@@ -22,6 +22,7 @@ def lib():
         E = load()
         E.emu_dir_ints.restype = C_I
         E.emu_lean_warps.restype = ctypes.c_long
+        E.emu_set_segment.argtypes = [C_I]
         E.emu_p2_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, C_D, C_D, P_I, P_D, P_D, P_D, C_I]
         E.emu_p1_apply.argtypes = [C_I, C_I, C_I, C_D, C_D, C_D, C_D, P_I, P_D, P_D, C_D, C_D, P_D, P_D, C_I]
         E.emu_transfer.argtypes = [C_I, C_I, C_I, P_I, C_I, C_I, P_I, P_D, P_D, C_I]
@@ -74,6 +75,11 @@ def p2_apply(nx, ny, hx, hy, lam, mu, p, dirv, xi, u, prec=0, mode=0, pmin=1e-6)
     uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
     lib().emu_p2_apply(prec, nx, ny, hx, hy, lam, mu, p, pmin, ip(dirv), dp(xi), dp(uu), dp(y), mode)
     return y
+
+
+def set_segment(seg: int) -> None:
+    """Cell rows per warp segment of the emulated P2 marches (0: the one-wave rule)."""
+    lib().emu_set_segment(int(seg))
 
 
 def lean_warps() -> int:

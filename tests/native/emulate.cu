@@ -47,6 +47,8 @@ void dir_to(const Dir& r, int* d) {
 
 // Warps of the last emulated P2 march that took the lean phases.
 static long lean_warps = 0;
+// Segment length of the emulated P2 marches (0: the kernel's one-wave rule).
+static int seg_override = 0;
 
 // Runs the column-march P2 kernel on the CPU: the 32 lanes of a warp execute
 // each phase in turn and the shuffles become copies between lane states.
@@ -54,7 +56,7 @@ template <class T>
 void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
   P2March<T>::prepare(io);
   lean_warps = 0;
-  if (seg <= 0) seg = p2_march_segment(P.nx, P.ny, 4, 5);
+  if (seg <= 0) seg = seg_override > 0 ? std::min(seg_override, P.ny) : p2_march_segment(P.nx, P.ny, 4, 5);
   const int nxw = (P.nx + 1 + P2M_OWN - 1) / P2M_OWN;
   const bool operand = io.mode != kP2Diag;
   std::vector<P2Lane<T>> L(32);
@@ -210,6 +212,7 @@ P2Params<T> p2params(int nx, int ny, double hx, double hy, double lam, double mu
 extern "C" {
 
 long emu_lean_warps() { return lean_warps; }
+void emu_set_segment(int seg) { seg_override = seg; }
 
 int emu_dir_ints() { return kDirInts; }
 

@@ -68,6 +68,25 @@ def test_p2_lean_warps_match_oracle(case):
         assert np.max(np.abs(y - ref)) <= tol * np.max(np.abs(ref))
 
 
+def test_p2_march_result_does_not_depend_on_the_segment():
+    """The march tile (cell rows per warp segment) is tuned at run time; every node value
+    must come out bit for bit the same for any segment length (a segment recomputes the
+    cell row below it, so each node sums the same contributions in the same order)."""
+    case = CASES[3]
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    try:
+        for prec in (0, 1):
+            ys = []
+            for seg in (0, 1, 2, 3, 5, 8, ny):
+                emu.set_segment(seg)
+                ys.append(emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=prec))
+            assert all(np.array_equal(ys[0], y) for y in ys[1:])
+    finally:
+        emu.set_segment(0)
+
+
 @pytest.mark.parametrize("case", CASES[:3])
 def test_p2_apply_fp32_matches_oracle(case):
     W, H, nx, ny, sides, p = case

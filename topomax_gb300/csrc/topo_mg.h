@@ -190,6 +190,9 @@ class MG {
   // execution order, last entry = launches; empty without a tail
   void tail_profile(std::vector<long long>& cycles) const;
   int tail_level() const { return tail_; }
+  // tune the segment length of this hierarchy's march kernels (level 0 if P2, the P1
+  // levels without a stencil) once per family and grid; needs set-up data in place
+  bool autotune = true;
 
  private:
   struct Lev {
@@ -204,6 +207,7 @@ class MG {
     bool bound = false;  // lmax is a guaranteed upper bound (no safety factor)
   };
   void vcycle_level(int l, const T* b, T* x, cudaStream_t s);
+  void tune_marches(cudaStream_t s);
   void vcycle_level_body(int l, const T* b, T* x, cudaStream_t s);
   int prof_depth_ = 0;
   int capture_pcg(bool warm);
@@ -268,6 +272,16 @@ class MG {
   Reducer* red_ = nullptr;
   int sms_ = 148;
 };
+
+// Segment lengths of the column-march kernels chosen by the autotuner
+// (MG::setup, once per kernel family and grid in a process): 0 when not tuned
+// (the one-wave rule of p2_march_segment applies).  TOPO_AUTOTUNE=0 turns the
+// tuner off.
+int tuned_segment(int family, int nx, int ny);
+void set_tuned_segment(int family, int nx, int ny, int seg);
+bool autotune_enabled();
+// march kernel family of the segment table: P2 or P1 march, precision, components
+constexpr int march_family(bool p2, int value_bytes, int nc) { return (p2 ? 0 : 8) + (value_bytes == 8 ? 4 : 0) + nc; }
 
 // y = A x for the FP64 P2 operator (used for refinement residuals)
 void p2_apply_f64(const P2Params<double>& p, const double* xi, const double* x, double* y,

@@ -639,8 +639,11 @@ inline int p1_march_bps() {
   return b;
 }
 
-inline dim3 march_grid(int nx, int ny, int blocks_per_sm, int& seg) {
-  seg = p2_march_segment(nx, ny, device_sms(), blocks_per_sm);
+// seg_force > 0: that segment length; else the tuned one for `family` (when tuned), else
+// the one-wave rule
+inline dim3 march_grid(int nx, int ny, int blocks_per_sm, int& seg, int family = -1, int seg_force = 0) {
+  const int tuned = seg_force > 0 ? seg_force : (family >= 0 ? tuned_segment(family, nx, ny) : 0);
+  seg = tuned > 0 ? std::min(tuned, ny) : p2_march_segment(nx, ny, device_sms(), blocks_per_sm);
   const int nseg = (ny + seg - 1) / seg;
   return dim3((nx + 1 + P2M_OWN - 1) / P2M_OWN, (nseg + P2M_WARPS - 1) / P2M_WARPS);
 }
@@ -701,9 +704,9 @@ inline int mode_vectors(int mode, bool p2, bool fused_rz) {
 }
 
 template <class T, int MODE>
-inline void launch_p2_mode(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s) {
+inline void launch_p2_mode(const P2Params<T>& P, const T* xi, const P2Io<T>& io, cudaStream_t s, int seg_force = 0) {
   int seg = 0;
-  const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<T, MODE>(), seg);
+  const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<T, MODE>(), seg, march_family(true, sizeof(T), 2), seg_force);
   const double n = 2.0 * (2 * P.nx + 1) * (2 * P.ny + 1), nv = double(P.nx + 1) * (P.ny + 1);
   // the design (one value per vertex) plus, for First, the coarse correction (2 per vertex)
   const double bytes = (mode_vectors(MODE, true, io.fuse == kFuseRZ) * n + nv + (MODE == kP2First ? 2 * nv : 0)) *
@@ -725,9 +728,9 @@ inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io,
 }
 
 template <class T, int NC, int MODE>
-inline void launch_p1_mode(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s) {
+inline void launch_p1_mode(const P1Params<T, NC>& P, const P1Io<T>& io, cudaStream_t s, int seg_force = 0) {
   int seg = 0;
-  const dim3 g = march_grid(P.nx, P.ny, p1_march_bps<T, NC, MODE>(), seg);
+  const dim3 g = march_grid(P.nx, P.ny, p1_march_bps<T, NC, MODE>(), seg, march_family(false, sizeof(T), NC), seg_force);
   static const char* fam[6] = {"P1 march Apply", "P1 march Diag", "P1 march Pre", "P1 march Res", "P1 march First",
                                "P1 march Post2"};
   const double n = double(NC) * (P.nx + 1) * (P.ny + 1), ntri = 2.0 * P.nx * P.ny;
@@ -1307,7 +1310,9 @@ int MG<T>::setup(cudaStream_t s) {
   cudaError_t e = cudaStreamSynchronize(s);
   mark("coarse inverse");
   if (e != cudaSuccess) return -5;
-  return st ? -2 : 0;
+  if (st) return -2;
+  tune_marches(s);
+  return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -5;
 }
 
 // One V-cycle from level l down: fused degree-2 Chebyshev pre-smoothing from
@@ -1491,6 +1496,104 @@ void MG<T>::vcycle(const T* b, T* x, cudaStream_t s) {
   vcycle_level(0, b, x, s);
 }
 
+// Autotuner of the column-march kernels' tile, the cell rows one warp marches:
+// candidate segment lengths are timed on the Apply mode with CUDA events (R
+// launches back to back per sample, best of two samples: the events resolve
+// about 2 us) and the one-wave rule of p2_march_segment is kept unless a
+// candidate is more than 5 % faster.  Once per kernel family and grid in the
+// process, after set-up and before the first graph recording (graphs keep the
+// segment they were recorded with).  Every segment length gives the same node
+// values; only the grid, and with it the fused reductions' block partials, changes,
+// so two processes may round a CG scalar differently (TOPO_AUTOTUNE=0 keeps the
+// one-wave rule and with it bitwise reproducible runs).
+template <class T>
+void MG<T>::tune_marches(cudaStream_t s) {
+  if (!autotune || !autotune_enabled()) return;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess) return;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return;
+  }
+  constexpr int R = 6;
+  auto time_it = [&](const auto& launch) -> float {
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      launch();  // warm
+      cudaEventRecord(e0, s);
+      for (int k = 0; k < R; ++k) launch();
+      cudaEventRecord(e1, s);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return 1e30f;
+      best = std::min(best, ms / R);
+    }
+    return best;
+  };
+  // max_blocks > 0: a candidate whose grid exceeds it is skipped
+  auto choose = [&](int family, int nx, int ny, int blocks_per_sm, size_t max_blocks, const auto& launch_with) {
+    if (tuned_segment(family, nx, ny) > 0) return;
+    // one tuner per key: a context set up concurrently for the same grid waits here and
+    // then uses the same segment, so all contexts of a grid in the process agree
+    std::lock_guard<std::recursive_mutex> lock(device_lock());
+    if (tuned_segment(family, nx, ny) > 0) return;
+    const int heur = p2_march_segment(nx, ny, device_sms(), blocks_per_sm);
+    const float t_heur = time_it([&] { launch_with(heur); });
+    int best = heur;
+    float t_best = t_heur;
+    for (int c : {1, 2, 3, 4, 6, 8, 12}) {
+      if (c == heur || c > ny) continue;
+      int sg = 0;
+      const dim3 g = march_grid(nx, ny, blocks_per_sm, sg, -1, c);
+      if (max_blocks && size_t(g.x) * g.y > max_blocks) continue;
+      const float t = time_it([&] { launch_with(c); });
+      if (t < t_best) {
+        t_best = t;
+        best = c;
+      }
+    }
+    set_tuned_segment(family, nx, ny, t_best < 0.95f * t_heur ? best : heur);
+  };
+  const int L = levels();
+  for (int l = 0; l < L; ++l) {
+    const LevelSpec& S = specs_[l];
+    Lev& v = lv_[l];
+    if (l == tail_ && tail_desc_ && use_tail) break;  // the tail runs the rest
+    if (l == cheb_coarse_ && cc_desc_) break;
+    if (S.p2) {
+      const size_t n = S.ndof();
+      T *x = pcg_[8], *y = pcg_[9];
+      cudaMemsetAsync(x, 0, n * sizeof(T), s);
+      P2Io<T> io;
+      std::memset(&io, 0, sizeof(io));
+      io.mode = kP2Apply;
+      io.u = x;
+      io.y = y;
+      // the fused CG reductions keep 2 partials per block in red_->blocks * 16 slots
+      const size_t max_blocks = red_ ? size_t(red_->blocks) * 8 : 0;
+      choose(march_family(true, sizeof(T), 2), S.nx, S.ny, p2_march_bps<T, kP2Apply>(), max_blocks,
+             [&](int seg) { launch_p2_mode<T, kP2Apply>(p2_op_, xi_, io, s, seg); });
+    } else if (!v.st && use_p1_march && l + 1 < L) {
+      cudaMemsetAsync(v.x, 0, S.ndof() * sizeof(T), s);
+      P1Io<T> io;
+      std::memset(&io, 0, sizeof(io));
+      io.mode = kP2Apply;
+      io.u = v.x;
+      io.y = v.t;
+      if (S.NC == 2) {
+        const auto P = make_p1<T, 2>(S, refs_[l], v.kK, nullptr);
+        choose(march_family(false, sizeof(T), 2), S.nx, S.ny, p1_march_bps<T, 2, kP2Apply>(), 0,
+               [&](int seg) { launch_p1_mode<T, 2, kP2Apply>(P, io, s, seg); });
+      } else {
+        const auto P = make_p1<T, 1>(S, refs_[l], v.kK, v.kM);
+        choose(march_family(false, sizeof(T), 1), S.nx, S.ny, p1_march_bps<T, 1, kP2Apply>(), 0,
+               [&](int seg) { launch_p1_mode<T, 1, kP2Apply>(P, io, s, seg); });
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
 // Records the CG solve into a graph: a prologue (initial residual, first
 // preconditioned direction, start test) followed by a WHILE conditional node
 // whose body is one CG iteration; the body's last kernel decides whether the
@@ -1548,8 +1651,9 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   T *r = pcg_[0], *z = pcg_[1], *p = pcg_[2], *q = pcg_[3];
   // both fused launches (operator and last post-smoothing) must fit the partial slots
   int seg = 0;
-  const dim3 ga = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Apply>(), seg);
-  const dim3 gp = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Post2>(), seg);
+  const int fam = march_family(true, sizeof(T), 2);
+  const dim3 ga = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Apply>(), seg, fam);
+  const dim3 gp = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Post2>(), seg, fam);
   const size_t mblocks = std::max(size_t(ga.x) * ga.y, size_t(gp.x) * gp.y);
   if (specs_[0].p2 && mblocks * 2 <= size_t(red_->blocks) * 16) {
     // P2 level 0: p.q is reduced inside the operator launch, r.r / r.z and the
