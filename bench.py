@@ -84,6 +84,9 @@ def parse():
                     help="designs of the ragged batch (domain 2x1, N in {100..300}); 0 skips the batch leg")
     ap.add_argument("--c4-iterations", type=int, default=5, help="design iterations per design in the batch leg")
     ap.add_argument("--c4-workers", type=int, default=8, help="concurrent workers (streams) of the batched run")
+    ap.add_argument("--fluid-n", type=int, default=40,
+                    help="cells per unit length of the fluid (Stokes-Brinkman diffuser) leg; 0 skips it")
+    ap.add_argument("--fluid-iterations", type=int, default=3, help="design iterations of the fluid leg")
     ap.add_argument("--kernel-steps", type=int, default=2,
                     help="host-driven design iterations on the 2000x1000 grid timed kernel by kernel "
                          "(HBM GB/s per kernel family); 0 skips them")
@@ -445,6 +448,9 @@ def main():
             c2["kernels"] = kernel_table(tg, mesh2, V2, dom, par, rho02, device_loop, args, measured_peak()[0])
             torch.cuda.empty_cache()
 
+    # --- the fluid problem: its GPU design loop beside the fluid oracle on the host
+    fluid = fluid_leg(args) if args.fluid_n > 0 and world == 1 else None
+
     # --- the ragged 64-design batch: batched (concurrent workers) against the un-batched loop
     c4 = c4_batch(args) if args.c4_designs > 0 else None
 
@@ -506,12 +512,53 @@ def main():
         "gpu_launches": int(nlaunch),
         "c2_2000x1000": c2,
         "c4_batch": c4,
+        "fluid": fluid,
         "clocks": ck,
         "solver_iterations": stats,
     }
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+FLUID = {"Fluid": {
+    "domain_parameters": dict(width=1.0, height=1.0, fem_step_size=0.0011, dem_step_size=0.0002, penalties=[0.1],
+                              volume_fraction=0.5),
+    "problem_parameters": dict(flows=[dict(side="Left", center=0.5, length=1.0, rate=1.0),
+                                      dict(side="Right", center=0.5, length=1.0 / 3.0, rate=-3.0)],
+                               viscosity=1.0)}}
+
+
+def fluid_leg(args):
+    """The Stokes-Brinkman diffuser (unit square, parabolic inflow on the left side, a three
+    times faster outflow a third as wide on the right, penalty 0.1) at args.fluid_n cells per
+    unit length: args.fluid_iterations design iterations of the GPU loop (FP64, rtol 1e-10)
+    and of the FP64 fluid oracle (sparse LU, the reference algorithm) on the host, each
+    from the uniform start, timed around solve() (set-up excluded; one GPU warm-up run)."""
+    import torch
+    from oracle.fluid import FluidDesign, FluidOracleSolver
+    from topomax_gb300.solver import FEMSolver
+    n, k = args.fluid_n, args.fluid_iterations
+    FEMSolver(n, dict(FLUID, name="diffuser"), precision="fp64", rtol=1e-10, verbose=False, save=False,
+              max_iterations=1).solve()
+    s = FEMSolver(n, dict(FLUID, name="diffuser"), precision="fp64", rtol=1e-10, verbose=False, save=False,
+                  max_iterations=k)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h = s.solve()[0.1]
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    o = FluidOracleSolver(n, FluidDesign.from_dict(FLUID), max_iterations=k, pressure="mean")
+    t0 = time.perf_counter()
+    run = o.solve()[0]
+    t_cpu = time.perf_counter() - t0
+    return {"workload": f"diffuser 1x1, {n}x{n} squares, Taylor-Hood, penalty 0.1, {k} design iterations",
+            "gpu": {"design_iters_per_s": h["iterations"] / t_gpu, "s": t_gpu, "iterations": h["iterations"],
+                    "objective": h["objectives"][-1],
+                    "krylov_iterations_per_solve": s.problem.stats["state_iterations"] / len(h["objectives"])},
+            "cpu_oracle": {"design_iters_per_s": run.iterations / t_cpu, "s": t_cpu, "iterations": run.iterations,
+                           "objective": run.objectives[-1], "cores": 1},
+            "objective_rel_diff": abs(h["objectives"][-1] - run.objectives[-1]) / abs(run.objectives[-1])}
 
 
 def c4_batch(args):
