@@ -106,6 +106,14 @@ int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs);
 /* Replaces Problem.set_penalization (src/problem.py:13, src/penalizers.py:14-20). */
 int topo_set_penalization(topo_ctx* ctx, double p);
 
+/* Warm starts of the filter solves (enable = 1; off by default, 0 turns them off and forgets the
+ * stored solutions): topo_filter_apply starts from the solution of the previous
+ * topo_filter_apply on this context, topo_sensitivity from the previous topo_sensitivity's; a
+ * failed solve is not reused.  Between design iterations both right-hand sides change little,
+ * so a solve to the same rtol takes fewer iterations.  No counterpart in the reference, whose
+ * HelmholtzFilter (FEM_src/filter.py:40-41) factorises and solves directly. */
+int topo_set_filter_warm_start(topo_ctx* ctx, int enable);
+
 /* Cap on the Krylov iterations of one filter or state solve (0 restores the defaults: 200
  * for the filter, 500 for the state; in mixed precision the cap counts the FP32 inner
  * iterations over all refinement steps of the solve).  A solve that reaches the cap

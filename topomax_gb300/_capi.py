@@ -27,7 +27,7 @@ SOLVE_WARM = 1
 
 EXPORTED = [
     "topo_create", "topo_create_filter", "topo_destroy", "topo_last_error", "topo_sizes",
-    "topo_set_penalization", "topo_set_iteration_limit", "topo_filter_apply", "topo_filter_solve", "topo_state_solve",
+    "topo_set_penalization", "topo_set_iteration_limit", "topo_set_filter_warm_start", "topo_filter_apply", "topo_filter_solve", "topo_state_solve",
     "topo_compliance", "topo_sensitivity_rhs", "topo_sensitivity", "topo_emd_step",
     "topo_emd_finish", "topo_integrate", "topo_apply_state", "topo_load_vector", "topo_time_operator",
     "topo_launch_count", "topo_kernel_clock", "topo_kernel_clock_report", "topo_sensitivity_rhs_noalloc", "topo_mass_apply",
@@ -109,6 +109,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     lib.topo_set_penalization.argtypes = [P, D]
     lib.topo_set_iteration_limit.argtypes = [P, I]
+    lib.topo_set_filter_warm_start.argtypes = [P, I]
     lib.topo_filter_apply.argtypes = [P, P, P, D, PI, P]
     lib.topo_filter_solve.argtypes = [P, P, P, D, PI, P]
     lib.topo_state_solve.argtypes = [P, P, P, D, I, PI, P]

@@ -222,6 +222,12 @@ struct topo_ctx {
   MG<float> fmg32;
   MG<double> fmg64;
   double* fb64 = nullptr;
+  // warm starts of the filter solves (topo_set_filter_warm_start): the last solution of
+  // the design filter (channel 0, topo_filter_apply) and of the sensitivity filter
+  // (channel 1, topo_sensitivity), each the next solve's initial guess on its channel
+  bool filter_warm = false;
+  double* fwarm[2] = {nullptr, nullptr};
+  bool fwarm_ok[2] = {false, false};
   double* fr64 = nullptr;
   double* fy64 = nullptr;
   float* fd32 = nullptr;
@@ -384,6 +390,8 @@ int init_filter(topo_ctx* C, double eps) {
   C->fb64 = C->arena.alloc_n<double>(C->nv);
   C->fr64 = C->arena.alloc_n<double>(C->nv);
   C->fy64 = C->arena.alloc_n<double>(C->nv);
+  C->fwarm[0] = C->arena.alloc_n<double>(C->nv);
+  C->fwarm[1] = C->arena.alloc_n<double>(C->nv);
   int st;
   if (C->precision == TOPO_PREC_MIXED) {
     C->fmg32.use_graphs = graphs_enabled();
@@ -594,21 +602,31 @@ int fgmres_ir(topo_ctx* C, MG<float>& mg, Apply64 apply64, const double* b, doub
                  rtol, st.relres, st.iterations);
 }
 
-int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int* iters, cudaStream_t s) {
+// channel: 0 design filter, 1 sensitivity filter (warm-started from the channel's last
+// solution when topo_set_filter_warm_start is on), -1 no warm start
+int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int* iters, cudaStream_t s,
+                      int channel = -1) {
   SolveStats st;
   int rc;
+  const bool warm = C->filter_warm && channel >= 0 && C->fwarm_ok[channel];
+  if (warm) cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (channel >= 0) C->fwarm_ok[channel] = false;  // until this solve succeeds
   if (C->precision == TOPO_PREC_MIXED) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
-    rc = fgmres_ir(C, C->fmg32, ap, b, xi, false, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
+    rc = fgmres_ir(C, C->fmg32, ap, b, xi, warm, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
                    C->inner_floor_filter, st, s);
   } else {
-    rc = C->fmg64.pcg(b, xi, false, rtol, C->max_iterations(kFilterMaxIt), st, s);
+    rc = C->fmg64.pcg(b, xi, warm, rtol, C->max_iterations(kFilterMaxIt), st, s);
     if (rc == -4) rc = C->fail(TOPO_ERR_NAN, "non-finite value in the filter solve");
     else if (rc == -5) rc = C->fail(TOPO_ERR_CUDA, "filter solve: CUDA graph recording or launch failed");
     else if (rc) rc = C->fail(TOPO_ERR_NOT_CONVERGED, "filter CG did not converge (relres %.3g)", st.relres);
   }
   if (iters) *iters = st.iterations;
   if (rc) return rc;
+  if (C->filter_warm && channel >= 0) {
+    cudaMemcpyAsync(C->fwarm[channel], xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    C->fwarm_ok[channel] = true;
+  }
   return C->cuda_check("filter solve");
 }
 
@@ -815,6 +833,14 @@ int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs) {
   return TOPO_OK;
 }
 
+int topo_set_filter_warm_start(topo_ctx* ctx, int enable) {
+  return guarded(ctx, [&]() {
+    ctx->filter_warm = enable != 0;
+    ctx->fwarm_ok[0] = ctx->fwarm_ok[1] = false;
+    return TOPO_OK;
+  });
+}
+
 int topo_set_iteration_limit(topo_ctx* ctx, int max_iterations) {
   return guarded(ctx, [&]() {
     if (max_iterations < 0) return ctx->fail(TOPO_ERR_ARG, "negative iteration limit");
@@ -839,7 +865,7 @@ int topo_filter_apply(topo_ctx* ctx, const double* f, double* xi, double rtol, i
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     filter_apply64(ctx, f, ctx->fb64, false, s);
     ctx->launches += 1;
-    return filter_solve_impl(ctx, ctx->fb64, xi, rtol, iters, s);
+    return filter_solve_impl(ctx, ctx->fb64, xi, rtol, iters, s, 0);
   });
 }
 
@@ -948,7 +974,7 @@ int topo_sensitivity(topo_ctx* ctx, const double* u, const double* xi, double* g
   if (rc) return rc;
   return guarded(ctx, [&]() {
     if (!g || !(rtol > 0)) return ctx->fail(TOPO_ERR_ARG, "invalid sensitivity arguments");
-    return filter_solve_impl(ctx, ctx->fb64, g, rtol, iters, reinterpret_cast<cudaStream_t>(stream));
+    return filter_solve_impl(ctx, ctx->fb64, g, rtol, iters, reinterpret_cast<cudaStream_t>(stream), 1);
   });
 }
 

@@ -371,7 +371,8 @@ class ElasticityProblem(Problem):
     Same constructor and methods as the reference.  Keyword-only extras:
     ``precision`` ("mixed": FP32 multigrid CG inside FP64 refinement, or
     "fp64"), ``rtol`` (relative residual of every linear solve) and
-    ``warm_start`` (start the state solve from the previous displacement).
+    ``warm_start`` (start the state solve from the previous displacement, and the
+    design and sensitivity filter solves from their previous solutions).
     """
 
     def __init__(self, mesh: RectangleMesh, control_space: FunctionSpace, domain_parameters: DomainParameters,
@@ -389,6 +390,7 @@ class ElasticityProblem(Problem):
         self.rtol = float(rtol)
         self.warm_start = warm_start
         self._ctx = self._create_context()
+        self._ctx.check(self._ctx._lib.topo_set_filter_warm_start(self._ctx.ptr, int(bool(warm_start))))
         self.filter = HelmholtzFilter(self.parameters.filter_radius, control_space, rtol=self.rtol,
                                       _ctx=self._ctx)
         self.Young_modulus = self.parameters.young_modulus
