@@ -29,7 +29,7 @@ template <class T, int NC>
 struct P1Lane {
   int i;            // cell column
   bool edge;        // last lane of the warp: loads its column 1 itself
-  T U[2][2][NC];    // operand at nodes (i+c, j+r), zero at clamped nodes
+  T U[2][2][NC];    // operand at nodes (i+c, j+r), zero outside the lattice (raw at clamped nodes)
   T A[2][2][NC];    // element results at the same nodes
   T kk[2], km[2];   // the cell's triangle coefficients
 };
@@ -60,11 +60,16 @@ struct P1March {
     }
   }
 
-  // operand at node (a,b); zero outside the lattice and at clamped nodes
+  // operand at node (a,b), zero outside the lattice.  At a clamped node it is the
+  // raw operand: the element phase zeroes it (tri) and the finish phase uses it as the
+  // identity row's value without loading it again.
   TOPO_HD static void fetch(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, T (&v)[NC]) {
     for (int c = 0; c < NC; ++c) v[c] = T(0);
-    if (a >= 0 && a <= P.nx && b >= 0 && b <= P.ny && (surely_free(P.dir, a, b) || !is_clamped(P.dir, a, b)))
-      operand(io, size_t(b) * (P.nx + 1) + a, v);
+    if (a >= 0 && a <= P.nx && b >= 0 && b <= P.ny) operand(io, size_t(b) * (P.nx + 1) + a, v);
+  }
+
+  TOPO_HD static bool clamped(const P1Params<T, NC>& P, int a, int b) {
+    return !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
   }
 
   template <int R0>
@@ -105,13 +110,15 @@ struct P1March {
     }
   }
 
+  // Z: the cell's clamped nodes (their operand enters the element product as zero)
   template <int O>
-  TOPO_HD static void tri(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int) {
+  TOPO_HD static void tri(const P1Params<T, NC>& P, P1Lane<T, NC>& L, const bool (&Z)[2][2]) {
     const T kk = L.kk[O];
     const T km = L.km[O];
     T u[3][NC];
-#define TOPO_LD(LV) \
-  for (int d = 0; d < NC; ++d) u[LV][d] = L.U[P1Off<O, LV>::b][P1Off<O, LV>::a][d];
+#define TOPO_LD(LV)                                                                          \
+  for (int d = 0; d < NC; ++d)                                                               \
+    u[LV][d] = Z[P1Off<O, LV>::b][P1Off<O, LV>::a] ? T(0) : L.U[P1Off<O, LV>::b][P1Off<O, LV>::a][d];
     TOPO_LD(0) TOPO_LD(1) TOPO_LD(2)
 #undef TOPO_LD
 #define TOPO_ST(LV)                                                                 \
@@ -133,8 +140,11 @@ struct P1March {
 
   TOPO_HD static void compute(const P1Params<T, NC>& P, P1Lane<T, NC>& L, int j) {
     if (L.i < 0 || L.i >= P.nx || j < 0 || j >= P.ny) return;
-    tri<0>(P, L, j);
-    tri<1>(P, L, j);
+    bool Z[2][2];
+    for (int r = 0; r < 2; ++r)
+      for (int c = 0; c < 2; ++c) Z[r][c] = clamped(P, L.i + c, j + r);
+    tri<0>(P, L, Z);
+    tri<1>(P, L, Z);
   }
 
   // The finish phase's per-node vectors of the lane's row-0 node at step j,
@@ -170,15 +180,11 @@ struct P1March {
   TOPO_HD static void finish_node(const P1Params<T, NC>& P, const P1Io<T>& io, int a, int b, const T (&sum)[NC],
                                   const T (&u)[NC], const Fin& F) {
     const size_t n = size_t(b) * (P.nx + 1) + a;
-    const bool cl = !surely_free(P.dir, a, b) && is_clamped(P.dir, a, b);
+    const bool cl = clamped(P, a, b);
     T un[NC], t[NC];
     for (int c = 0; c < NC; ++c) {
-      un[c] = u[c];
-      t[c] = sum[c];
-    }
-    if (cl) {
-      operand(io, n, un);  // the loaded copy is zero at clamped nodes
-      for (int c = 0; c < NC; ++c) t[c] = un[c];
+      un[c] = u[c];  // the operand as fetched: raw at a clamped node
+      t[c] = cl ? un[c] : sum[c];
     }
     const SmoothBufs<T>& B = io.B;
     for (int c = 0; c < NC; ++c) {
