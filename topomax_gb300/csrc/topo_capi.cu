@@ -226,6 +226,9 @@ struct topo_ctx {
   // the design filter (channel 0, topo_filter_apply) and of the sensitivity filter
   // (channel 1, topo_sensitivity), each the next solve's initial guess on its channel
   bool filter_warm = false;
+  // the filter solves of a mixed-precision context: FP32 multigrid CG inside FP64 FGMRES
+  // (true) or FP64 multigrid CG (false, TOPO_FILTER_FP64=1); FP64 contexts always use FP64
+  bool filter_mixed = false;
   double* fwarm[2] = {nullptr, nullptr};
   bool fwarm_ok[2] = {false, false};
   double* fr64 = nullptr;
@@ -393,7 +396,8 @@ int init_filter(topo_ctx* C, double eps) {
   C->fwarm[0] = C->arena.alloc_n<double>(C->nv);
   C->fwarm[1] = C->arena.alloc_n<double>(C->nv);
   int st;
-  if (C->precision == TOPO_PREC_MIXED) {
+  C->filter_mixed = C->precision == TOPO_PREC_MIXED && !env_flag("TOPO_FILTER_FP64", false);
+  if (C->filter_mixed) {
     C->fmg32.use_graphs = graphs_enabled();
     C->fmg32.fp64_solution = true;  // FGMRES directions keep the inner solutions in FP64
     C->fmg32.cheb_lo_frac = C->cheb_lo_filter;
@@ -417,8 +421,8 @@ int init_filter(topo_ctx* C, double eps) {
   }
   if (st) return C->fail(st == -5 ? TOPO_ERR_CUDA : TOPO_ERR_NOT_CONVERGED, "filter multigrid set-up failed (%d)", st);
   if (C->trace_solves) {
-    const int lc = C->precision == TOPO_PREC_MIXED ? C->fmg32.coarse_cheb_level() : C->fmg64.coarse_cheb_level();
-    const int dg = C->precision == TOPO_PREC_MIXED ? C->fmg32.coarse_cheb_deg : C->fmg64.coarse_cheb_deg;
+    const int lc = C->filter_mixed ? C->fmg32.coarse_cheb_level() : C->fmg64.coarse_cheb_level();
+    const int dg = C->filter_mixed ? C->fmg32.coarse_cheb_deg : C->fmg64.coarse_cheb_deg;
     std::fprintf(stderr, "[topo setup] filter hierarchy: %zu levels, coarse Chebyshev at level %d (degree %d)\n",
                  C->fspec.size(), lc, dg);
   }
@@ -611,7 +615,7 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   const bool warm = C->filter_warm && channel >= 0 && C->fwarm_ok[channel];
   if (warm) cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (channel >= 0) C->fwarm_ok[channel] = false;  // until this solve succeeds
-  if (C->precision == TOPO_PREC_MIXED) {
+  if (C->filter_mixed) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
     rc = fgmres_ir(C, C->fmg32, ap, b, xi, warm, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
                    C->inner_floor_filter, st, s);
