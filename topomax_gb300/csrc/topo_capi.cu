@@ -231,6 +231,11 @@ struct topo_ctx {
   bool filter_mixed = false;
   double* fwarm[2] = {nullptr, nullptr};
   bool fwarm_ok[2] = {false, false};
+  // the solution before the last one: with both, the next guess is 2 last - previous
+  // (the linear extrapolation in the design iteration; TOPO_EXTRAPOLATE=0 keeps the last)
+  double* fwarm_prev[2] = {nullptr, nullptr};
+  bool fwarm_prev_ok[2] = {false, false};
+  bool extrapolate = true;
   double* fr64 = nullptr;
   double* fy64 = nullptr;
   float* fd32 = nullptr;
@@ -395,6 +400,9 @@ int init_filter(topo_ctx* C, double eps) {
   C->fy64 = C->arena.alloc_n<double>(C->nv);
   C->fwarm[0] = C->arena.alloc_n<double>(C->nv);
   C->fwarm[1] = C->arena.alloc_n<double>(C->nv);
+  C->fwarm_prev[0] = C->arena.alloc_n<double>(C->nv);
+  C->fwarm_prev[1] = C->arena.alloc_n<double>(C->nv);
+  C->extrapolate = env_flag("TOPO_EXTRAPOLATE", true);
   int st;
   C->filter_mixed = C->precision == TOPO_PREC_MIXED && !env_flag("TOPO_FILTER_FP64", false);
   if (C->filter_mixed) {
@@ -613,8 +621,18 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   SolveStats st;
   int rc;
   const bool warm = C->filter_warm && channel >= 0 && C->fwarm_ok[channel];
-  if (warm) cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  if (channel >= 0) C->fwarm_ok[channel] = false;  // until this solve succeeds
+  if (warm) {
+    if (C->extrapolate && C->fwarm_prev_ok[channel]) {
+      const int g = C->grid(C->nv);
+      k_sub<double><<<g, kVecThreads, 0, s>>>(xi, C->fwarm[channel], C->fwarm_prev[channel], C->nv);
+      k_axpy<double><<<g, kVecThreads, 0, s>>>(xi, 1.0, C->fwarm[channel], C->nv);
+      C->launches += 2;
+    } else {
+      cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    }
+  }
+  const bool had_last = channel >= 0 && C->fwarm_ok[channel];
+  if (channel >= 0) C->fwarm_ok[channel] = C->fwarm_prev_ok[channel] = false;  // until this solve succeeds
   if (C->filter_mixed) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
     rc = fgmres_ir(C, C->fmg32, ap, b, xi, warm, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
@@ -628,6 +646,8 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   if (iters) *iters = st.iterations;
   if (rc) return rc;
   if (C->filter_warm && channel >= 0) {
+    if (had_last) std::swap(C->fwarm[channel], C->fwarm_prev[channel]);
+    C->fwarm_prev_ok[channel] = had_last;
     cudaMemcpyAsync(C->fwarm[channel], xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
     C->fwarm_ok[channel] = true;
   }
@@ -841,6 +861,7 @@ int topo_set_filter_warm_start(topo_ctx* ctx, int enable) {
   return guarded(ctx, [&]() {
     ctx->filter_warm = enable != 0;
     ctx->fwarm_ok[0] = ctx->fwarm_ok[1] = false;
+    ctx->fwarm_prev_ok[0] = ctx->fwarm_prev_ok[1] = false;
     return TOPO_OK;
   });
 }

@@ -25,6 +25,7 @@ reads them; "lattice" is the device order.
 from __future__ import annotations
 
 import ctypes
+import os
 import pickle
 
 import numpy as np
@@ -399,6 +400,8 @@ class ElasticityProblem(Problem):
         self.lamé_mu = self.Young_modulus / (2 * (1 + self.Poisson_ratio))
         self.lamé_lda = self.lamé_mu * self.Poisson_ratio / (0.5 - self.Poisson_ratio)
         self.u: Function | None = None
+        self._u_prev: Function | None = None
+        self.extrapolate = os.environ.get("TOPO_EXTRAPOLATE", "1") != "0"
         self.filtered_rho: Function | None = None
         self.stats = {"state_iterations": 0, "filter_iterations": 0}
         self._scalar = torch.zeros(1, dtype=torch.float64, device=_device())
@@ -476,11 +479,15 @@ class ElasticityProblem(Problem):
         flags = 0
         if self.warm_start and self.u is not None:
             u.tensor.copy_(self.u.tensor)
+            if self.extrapolate and self._u_prev is not None:
+                # the design moves a little each iteration: 2 u_k - u_(k-1) starts the solve closer
+                u.tensor.mul_(2.0).sub_(self._u_prev.tensor)
             flags = _capi.SOLVE_WARM
         it = ctypes.c_int(0)
         self._ctx.check(self._ctx._lib.topo_state_solve(self._ctx.ptr, _ptr(xi), _ptr(u.tensor), self.rtol, flags,
                                                         ctypes.byref(it), _stream()))
         self.stats["state_iterations"] += it.value
+        self._u_prev = self.u
         return u
 
     # -- extras ---------------------------------------------------------------
