@@ -109,9 +109,9 @@ int topo_set_penalization(topo_ctx* ctx, double p);
 /* Warm starts of the filter solves (enable = 1; off by default, 0 turns them off and forgets the
  * stored solutions): topo_filter_apply starts from the solution of the previous
  * topo_filter_apply on this context, topo_sensitivity from the previous topo_sensitivity's
- * (from 2 x_last - x_before once two solutions exist: the linear extrapolation over the design
- * iterations; environment TOPO_EXTRAPOLATE=0 at context creation keeps x_last); a failed solve
- * is not reused.  Between design iterations both right-hand sides change little,
+ * (extrapolated over the design iterations once more solutions exist: 2 x1 - x2 from two,
+ * 3 x1 - 3 x2 + x3 from three; environment TOPO_EXTRAPOLATE at context creation: 0 keeps x1,
+ * 1 linear, 2 quadratic, the default); a failed solve is not reused.  Between design iterations both right-hand sides change little,
  * so a solve to the same rtol takes fewer iterations.  No counterpart in the reference, whose
  * HelmholtzFilter (FEM_src/filter.py:40-41) factorises and solves directly. */
 int topo_set_filter_warm_start(topo_ctx* ctx, int enable);

@@ -90,6 +90,13 @@ __global__ void k_emd_half(const double* __restrict__ psi_prev, const double* __
 
 // One Newton step of  F(c) = int expit(half + c) - volume = 0  (src/solver.py:149-186,
 // scipy newton semantics: stop when |c_new - c| < tol).
+// warm-start guess from a solution history x1 (last), x2, x3: order 1 the linear
+// extrapolation 2 x1 - x2, order 2 the quadratic 3 (x1 - x2) + x3
+__global__ void k_extrapolate(double* __restrict__ y, const double* __restrict__ x1, const double* __restrict__ x2,
+                              const double* __restrict__ x3, size_t n, int order) {
+  TOPO_GRID_STRIDE(i, n) y[i] = order == 1 ? 2.0 * x1[i] - x2[i] : 3.0 * (x1[i] - x2[i]) + x3[i];
+}
+
 __global__ void k_newton(const double* __restrict__ half, const double* __restrict__ w, size_t n, double volume,
                          double tol, int maxit, double* partials, unsigned* counter, NewtonState* st) {
   if (st->done) return;
@@ -230,12 +237,13 @@ struct topo_ctx {
   // (true) or FP64 multigrid CG (false, TOPO_FILTER_FP64=1); FP64 contexts always use FP64
   bool filter_mixed = false;
   double* fwarm[2] = {nullptr, nullptr};
-  bool fwarm_ok[2] = {false, false};
-  // the solution before the last one: with both, the next guess is 2 last - previous
-  // (the linear extrapolation in the design iteration; TOPO_EXTRAPOLATE=0 keeps the last)
+  // the two solutions before the last one: with them the next guess is the linear
+  // (2 x1 - x2) or quadratic (3 x1 - 3 x2 + x3) extrapolation over the design iterations
+  // (TOPO_EXTRAPOLATE: 0 keeps the last, 1 linear, 2 quadratic, the default)
   double* fwarm_prev[2] = {nullptr, nullptr};
-  bool fwarm_prev_ok[2] = {false, false};
-  bool extrapolate = true;
+  double* fwarm_prev2[2] = {nullptr, nullptr};
+  int fwarm_hist[2] = {0, 0};  // solutions held: last, previous, the one before (0..3)
+  int extrapolate = 2;
   double* fr64 = nullptr;
   double* fy64 = nullptr;
   float* fd32 = nullptr;
@@ -400,9 +408,11 @@ int init_filter(topo_ctx* C, double eps) {
   C->fy64 = C->arena.alloc_n<double>(C->nv);
   C->fwarm[0] = C->arena.alloc_n<double>(C->nv);
   C->fwarm[1] = C->arena.alloc_n<double>(C->nv);
-  C->fwarm_prev[0] = C->arena.alloc_n<double>(C->nv);
-  C->fwarm_prev[1] = C->arena.alloc_n<double>(C->nv);
-  C->extrapolate = env_flag("TOPO_EXTRAPOLATE", true);
+  for (int k = 0; k < 2; ++k) {
+    C->fwarm_prev[k] = C->arena.alloc_n<double>(C->nv);
+    C->fwarm_prev2[k] = C->arena.alloc_n<double>(C->nv);
+  }
+  if (const char* e = std::getenv("TOPO_EXTRAPOLATE")) C->extrapolate = std::max(0, std::min(2, std::atoi(e)));
   int st;
   C->filter_mixed = C->precision == TOPO_PREC_MIXED && !env_flag("TOPO_FILTER_FP64", false);
   if (C->filter_mixed) {
@@ -620,19 +630,19 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
                       int channel = -1) {
   SolveStats st;
   int rc;
-  const bool warm = C->filter_warm && channel >= 0 && C->fwarm_ok[channel];
+  const int hist = (C->filter_warm && channel >= 0) ? C->fwarm_hist[channel] : 0;
+  const bool warm = hist > 0;
   if (warm) {
-    if (C->extrapolate && C->fwarm_prev_ok[channel]) {
-      const int g = C->grid(C->nv);
-      k_sub<double><<<g, kVecThreads, 0, s>>>(xi, C->fwarm[channel], C->fwarm_prev[channel], C->nv);
-      k_axpy<double><<<g, kVecThreads, 0, s>>>(xi, 1.0, C->fwarm[channel], C->nv);
-      C->launches += 2;
+    const int order = std::min(C->extrapolate, hist - 1);
+    if (order > 0) {
+      k_extrapolate<<<C->grid(C->nv), kVecThreads, 0, s>>>(xi, C->fwarm[channel], C->fwarm_prev[channel],
+                                                          C->fwarm_prev2[channel], C->nv, order);
+      C->launches += 1;
     } else {
       cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
     }
   }
-  const bool had_last = channel >= 0 && C->fwarm_ok[channel];
-  if (channel >= 0) C->fwarm_ok[channel] = C->fwarm_prev_ok[channel] = false;  // until this solve succeeds
+  if (channel >= 0) C->fwarm_hist[channel] = 0;  // until this solve succeeds
   if (C->filter_mixed) {
     auto ap = [C](const double* x, double* y, cudaStream_t ss) { filter_apply64(C, x, y, true, ss); };
     rc = fgmres_ir(C, C->fmg32, ap, b, xi, warm, C->nv, rtol, C->fgm, C->max_iterations(kFilterMaxIt),
@@ -646,10 +656,11 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   if (iters) *iters = st.iterations;
   if (rc) return rc;
   if (C->filter_warm && channel >= 0) {
-    if (had_last) std::swap(C->fwarm[channel], C->fwarm_prev[channel]);
-    C->fwarm_prev_ok[channel] = had_last;
+    // shift the history: the one before <- previous <- last <- this solution
+    std::swap(C->fwarm_prev2[channel], C->fwarm_prev[channel]);
+    std::swap(C->fwarm_prev[channel], C->fwarm[channel]);
     cudaMemcpyAsync(C->fwarm[channel], xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    C->fwarm_ok[channel] = true;
+    C->fwarm_hist[channel] = std::min(3, hist + 1);
   }
   return C->cuda_check("filter solve");
 }
@@ -860,8 +871,7 @@ int topo_sizes(const topo_ctx* ctx, int64_t* n_vertices, int64_t* n_dofs) {
 int topo_set_filter_warm_start(topo_ctx* ctx, int enable) {
   return guarded(ctx, [&]() {
     ctx->filter_warm = enable != 0;
-    ctx->fwarm_ok[0] = ctx->fwarm_ok[1] = false;
-    ctx->fwarm_prev_ok[0] = ctx->fwarm_prev_ok[1] = false;
+    ctx->fwarm_hist[0] = ctx->fwarm_hist[1] = 0;
     return TOPO_OK;
   });
 }

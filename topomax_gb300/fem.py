@@ -401,7 +401,11 @@ class ElasticityProblem(Problem):
         self.lamé_lda = self.lamé_mu * self.Poisson_ratio / (0.5 - self.Poisson_ratio)
         self.u: Function | None = None
         self._u_prev: Function | None = None
-        self.extrapolate = os.environ.get("TOPO_EXTRAPOLATE", "1") != "0"
+        self._u_prev2: Function | None = None
+        # warm-start guess from the last solutions: 0 the last one, 1 linear, 2 quadratic
+        # extrapolation over the design iterations (TOPO_EXTRAPOLATE; the default is 2)
+        self.extrapolate_order = int(os.environ.get("TOPO_EXTRAPOLATE", "2"))
+        self.extrapolate = self.extrapolate_order > 0
         self.filtered_rho: Function | None = None
         self.stats = {"state_iterations": 0, "filter_iterations": 0}
         self._scalar = torch.zeros(1, dtype=torch.float64, device=_device())
@@ -480,13 +484,18 @@ class ElasticityProblem(Problem):
         if self.warm_start and self.u is not None:
             u.tensor.copy_(self.u.tensor)
             if self.extrapolate and self._u_prev is not None:
-                # the design moves a little each iteration: 2 u_k - u_(k-1) starts the solve closer
-                u.tensor.mul_(2.0).sub_(self._u_prev.tensor)
+                if self.extrapolate_order == 2 and self._u_prev2 is not None:
+                    # 3 u_k - 3 u_(k-1) + u_(k-2)
+                    u.tensor.sub_(self._u_prev.tensor).mul_(3.0).add_(self._u_prev2.tensor)
+                else:
+                    # the design moves a little each iteration: 2 u_k - u_(k-1) starts the solve closer
+                    u.tensor.mul_(2.0).sub_(self._u_prev.tensor)
             flags = _capi.SOLVE_WARM
         it = ctypes.c_int(0)
         self._ctx.check(self._ctx._lib.topo_state_solve(self._ctx.ptr, _ptr(xi), _ptr(u.tensor), self.rtol, flags,
                                                         ctypes.byref(it), _stream()))
         self.stats["state_iterations"] += it.value
+        self._u_prev2 = self._u_prev
         self._u_prev = self.u
         return u
 
