@@ -65,3 +65,32 @@ def test_compliance_gradient_matches_central_differences():
         fd[n] = (vals[0] - vals[1]) / (2 * h)
     assert np.all(np.isfinite(fd))
     assert np.linalg.norm(fd - grad[idx]) <= 1e-3 * np.linalg.norm(grad[idx])
+
+
+def test_compliance_gradient_matches_the_oracles_analytic_sensitivity():
+    """The same 400 x 200 workload against the FP64 oracle's analytic sensitivity (the
+    reference's FEM_src/elasisity_problem.py:134-150 restated: the filtered -r'(xi)(...)
+    Riesz representative g, times the CG1 mass matrix M1 for the Euclidean gradient),
+    and the compliance against the oracle's sparse-LU value."""
+    import torch
+    from oracle.fem import Design, FEMOracle, Lattice
+    from topomax_gb300.autograd import compliance
+    prob, V = _problem("mixed", 1e-10)
+    g1 = torch.Generator().manual_seed(1)
+    rho0 = (torch.rand(V.dim(), generator=g1, dtype=torch.float64) * 0.95 + 0.05).cuda()
+    rho = rho0.clone().requires_grad_(True)
+    c = compliance(prob, rho)
+    c.backward()
+    grad = rho.grad.cpu().numpy()
+    d = Design(width=2.0, height=1.0, fem_step_size=0.002, penalties=[3.0], volume_fraction=0.5,
+               fixed_sides=["Left"], body_force=None,
+               tractions=[dict(side="Right", center=0.5, length=0.2, value=[0.0, -1.0])],
+               filter_radius=0.05, young_modulus=1.0, poisson_ratio=0.3)
+    o = FEMOracle(Lattice(2.0, 1.0, 400, 200), d)
+    o.set_penalization(3.0)
+    r = rho0.cpu().numpy()
+    xi = o.filter_apply(r)
+    u = o.state_solve(xi)
+    assert abs(float(c.detach()) - o.compliance(u)) <= 1e-9 * abs(o.compliance(u))
+    ref = o.M1 @ o.gradient(u, xi)
+    assert np.max(np.abs(grad - ref)) <= 1e-6 * np.max(np.abs(ref))
