@@ -82,7 +82,7 @@ def parse():
                     help="timed design iterations on the 2000x1000 grid (16,012,002 dofs); 0 skips it")
     ap.add_argument("--c4-designs", type=int, default=64,
                     help="designs of the ragged batch (domain 2x1, N in {100..300}); 0 skips the batch leg")
-    ap.add_argument("--c4-iterations", type=int, default=5, help="design iterations per design in the batch leg")
+    ap.add_argument("--c4-iterations", type=int, default=20, help="design iterations per design in the batch leg")
     ap.add_argument("--c4-workers", type=int, default=8, help="concurrent workers (streams) of the batched run")
     ap.add_argument("--fluid-n", type=int, default=40,
                     help="cells per unit length of the fluid (Stokes-Brinkman diffuser) leg; 0 skips it")
@@ -567,8 +567,10 @@ def c4_batch(args):
     p in {3, 4, 5}, random volume fraction and step size; seed 3), each run for
     args.c4_iterations design iterations, once one design after another (the un-batched
     loop) and once by args.c4_workers concurrent workers on their own streams.  Wall time
-    of each whole run, context set-up included; one design of every size runs first so
-    that both timed runs find the march tiles tuned."""
+    of each whole run, context set-up included (its per-design sums are reported beside:
+    set-up allocates device memory under the library's device lock, so it does not overlap
+    between workers); one design of every size runs first so that both timed runs find the
+    march tiles tuned."""
     import torch
     from topomax_gb300.batch import BatchItem, config4_designs, run_batch
     items = config4_designs(args.c4_designs, seed=3)
@@ -585,7 +587,9 @@ def c4_batch(args):
         dt = time.perf_counter() - t0
         iters = sum(h["iterations"] for r in res for h in r.history.values())
         out[leg] = {"workers": workers, "s": dt, "design_iterations": iters,
-                    "design_iters_per_s": iters / dt, "errors": sum(1 for r in res if r.error)}
+                    "design_iters_per_s": iters / dt, "errors": sum(1 for r in res if r.error),
+                    "setup_s_sum": sum(r.setup_s for r in res), "loop_s_sum": sum(r.solve_s for r in res),
+                    "loop_ms_per_design_iteration": 1000.0 * sum(r.solve_s for r in res) / max(1, iters)}
         out[leg + "_histories"] = res
     a, b = out.pop("sequential_histories"), out.pop("batched_histories")
     keys = ("objectives", "deltas", "exit_condition", "iterations")  # not the wall times

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import queue
 import threading
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -39,6 +40,8 @@ class BatchResult:
     history: dict = field(default_factory=dict)
     rho: np.ndarray | None = None
     error: str = ""
+    setup_s: float = 0.0   # wall time of the design's set-up (contexts, load vectors, filter)
+    solve_s: float = 0.0   # wall time of its design loop
 
 
 def config4_designs(count: int = 64, seed: int = 3) -> list[BatchItem]:
@@ -67,9 +70,13 @@ def config4_designs(count: int = 64, seed: int = 3) -> list[BatchItem]:
 def _run_one(item: BatchItem, iterations: int, precision: str, rtol: float) -> BatchResult:
     res = BatchResult(item.name, item.N)
     try:
+        t0 = time.perf_counter()
         solver = FEMSolver(item.N, dict(item.design, name=item.name), precision=precision, rtol=rtol,
                            verbose=False, save=False, max_iterations=iterations)
+        t1 = time.perf_counter()
         res.history = solver.solve()
+        torch.cuda.current_stream().synchronize()
+        res.setup_s, res.solve_s = t1 - t0, time.perf_counter() - t1
         res.rho = solver.to_array(solver.rho)
     except (ValueError, RuntimeError) as e:
         res.error = str(e)
