@@ -512,6 +512,7 @@ def main():
         "gpu_launches": int(nlaunch),
         "c2_2000x1000": c2,
         "c4_batch": c4,
+        "march_tiles": march_tiles(),
         "fluid": fluid,
         "clocks": ck,
         "solver_iterations": stats,
@@ -519,6 +520,21 @@ def main():
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def march_tiles():
+    """The autotuner's choices in this run: (kernel family, grid) -> cell rows per warp segment."""
+    import ctypes
+    from topomax_gb300 import _capi
+    lib = _capi.load_library()
+    need = lib.topo_march_tiles_report(None, 0)
+    buf = ctypes.create_string_buffer(int(need))
+    lib.topo_march_tiles_report(buf, need)
+    out = []
+    for line in buf.value.decode().splitlines():
+        fam, nx, ny, seg = line.split("\t")
+        out.append({"family": fam, "grid": f"{nx}x{ny}", "segment": int(seg)})
+    return out
 
 
 FLUID = {"Fluid": {

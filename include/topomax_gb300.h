@@ -195,6 +195,12 @@ int topo_kernel_clock(int enable);
  * terminating NUL, or TOPO_ERR_CUDA. */
 int64_t topo_kernel_clock_report(char* buf, int64_t len);
 
+/* Measurement hook (no counterpart in the reference): the tiles the march-kernel autotuner
+ * chose in this process (cell rows per warp segment), as text, one line per kernel family and
+ * grid: "family<TAB>nx<TAB>ny<TAB>segment<LF>", into buf when len is large enough.  Returns the
+ * length needed including the terminating NUL. */
+int64_t topo_march_tiles_report(char* buf, int64_t len);
+
 /* y = M1 x with M1 the consistent CG1 mass matrix (the assembled (x, v) form, as the filter's
  * right-hand side FEM_src/filter.py:30-37 assembles it), FP64.  No counterpart as a function in
  * the reference: the Euclidean gradient of the compliance with respect to the nodal design is

@@ -30,7 +30,7 @@ EXPORTED = [
     "topo_set_penalization", "topo_set_iteration_limit", "topo_set_filter_warm_start", "topo_filter_apply", "topo_filter_solve", "topo_state_solve",
     "topo_compliance", "topo_sensitivity_rhs", "topo_sensitivity", "topo_emd_step",
     "topo_emd_finish", "topo_integrate", "topo_apply_state", "topo_load_vector", "topo_time_operator",
-    "topo_launch_count", "topo_kernel_clock", "topo_kernel_clock_report", "topo_sensitivity_rhs_noalloc", "topo_mass_apply",
+    "topo_launch_count", "topo_kernel_clock", "topo_kernel_clock_report", "topo_march_tiles_report", "topo_sensitivity_rhs_noalloc", "topo_mass_apply",
     "topo_dem_create", "topo_dem_destroy", "topo_dem_last_error", "topo_dem_set_penalization",
     "topo_dem_set_external", "topo_dem_set_mask", "topo_dem_enforce", "topo_dem_energy",
     "topo_dem_energy_backward", "topo_dem_objective_gradient",
@@ -127,6 +127,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_kernel_clock.argtypes = [I]
     lib.topo_kernel_clock_report.restype = ctypes.c_int64
     lib.topo_kernel_clock_report.argtypes = [ctypes.c_char_p, ctypes.c_int64]
+    lib.topo_march_tiles_report.restype = ctypes.c_int64
+    lib.topo_march_tiles_report.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     lib.topo_sensitivity_rhs_noalloc.argtypes = [ctypes.POINTER(GridDesc), D, D, D, D, P, P, P, P]
     lib.topo_dem_create.restype = P
     lib.topo_dem_create.argtypes = [ctypes.POINTER(DemDesc), PI]
