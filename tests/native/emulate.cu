@@ -438,10 +438,16 @@ int emu_sensitivity(int prec, int nx, int ny, double hx, double hy, double lam, 
       float xe[3], c[3];
       for (int k = 0; k < 3; ++k) xe[k] = float(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
       const auto pen = make_penal<float>(p, pmin);
+      // the kernel's difference form: u - u_A in FP64, gradients and quadrature in FP32
+      float ud[6][2];
+      for (int k = 0; k < 6; ++k)
+        for (int d = 0; d < 2; ++d) ud[k][d] = k == 0 ? 0.0f : float(ue[k][d] - ue[0][d]);
       if (o == 0)
-        tri_sensitivity<0, double, float>(ue, xe, 1.0 / hx, 1.0 / hy, float(lam), float(mu), float(area), pen, c);
+        tri_sensitivity<0, float, float>(ud, xe, float(1.0 / hx), float(1.0 / hy), float(lam), float(mu), float(area),
+                                         pen, c);
       else
-        tri_sensitivity<1, double, float>(ue, xe, 1.0 / hx, 1.0 / hy, float(lam), float(mu), float(area), pen, c);
+        tri_sensitivity<1, float, float>(ud, xe, float(1.0 / hx), float(1.0 / hy), float(lam), float(mu), float(area),
+                                         pen, c);
       for (int k = 0; k < 3; ++k) tri[3 * t + k] = c[k];
     }
   }

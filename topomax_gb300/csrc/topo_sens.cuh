@@ -27,8 +27,19 @@ __global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu
     TQ xe[3];
     for (int k = 0; k < 3; ++k) xe[k] = TQ(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
     TQ c[3];
-    if (o == 0) tri_sensitivity<0, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
-    else tri_sensitivity<1, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+    if constexpr (sizeof(TQ) == 4) {
+      // difference form: the gradient ignores a translation, so the node values enter as
+      // u - u_A, subtracted in FP64 (exact for a smooth field) and rounded to FP32, where
+      // the gradients and the quadrature run (FP64 arithmetic is scarce on this GPU)
+      TQ ud[6][2];
+      for (int k = 0; k < 6; ++k)
+        for (int d = 0; d < 2; ++d) ud[k][d] = k == 0 ? TQ(0) : TQ(ue[k][d] - ue[0][d]);
+      if (o == 0) tri_sensitivity<0, TQ, TQ>(ud, xe, TQ(ihx), TQ(ihy), lam, mu, area, pen, c);
+      else tri_sensitivity<1, TQ, TQ>(ud, xe, TQ(ihx), TQ(ihy), lam, mu, area, pen, c);
+    } else {
+      if (o == 0) tri_sensitivity<0, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+      else tri_sensitivity<1, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+    }
     out[3 * t] = c[0];
     out[3 * t + 1] = c[1];
     out[3 * t + 2] = c[2];
