@@ -444,7 +444,7 @@ def main():
               "operator_launch_ms": float(np.mean(op2)), "operator_gbs": alg2 / (float(np.mean(op2)) * 1e-3) / 1e9}
         del prob2
         torch.cuda.empty_cache()
-        if args.kernel_steps > 0:
+        if args.kernel_steps > 0 and world == 1:
             c2["kernels"] = kernel_table(tg, mesh2, V2, dom, par, rho02, device_loop, args, measured_peak()[0])
             torch.cuda.empty_cache()
 
@@ -452,7 +452,7 @@ def main():
     fluid = fluid_leg(args) if args.fluid_n > 0 and world == 1 else None
 
     # --- the ragged 64-design batch: batched (concurrent workers) against the un-batched loop
-    c4 = c4_batch(args) if args.c4_designs > 0 else None
+    c4 = c4_batch(args) if args.c4_designs > 0 and world == 1 else None
 
     # --- the CPU oracle legs' grid on the GPU: a same-grid comparison with cpu_baseline and --impl reference
     rnx, rny = _grid(args.ref_grid)
