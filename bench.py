@@ -23,16 +23,23 @@ state solve + compliance).
   reference-facing API with host (pinned) arrays, as the reference's
   Solver.step/project/set_from_array drive it.
 * ``c2_2000x1000``: the same loop on the 2000x1000 grid of the throughput
-  configuration (16,012,002 dofs), with its operator's bandwidth.
+  configuration (16,012,002 dofs), with its operator's bandwidth; ``kernels``:
+  HBM GB/s per kernel family there (the library's kernel clock over host-driven
+  design iterations).
+* ``c4_batch``: the 64-design ragged batch (domain 2x1, N in {100..300}), run one
+  design after another and by concurrent workers; ``march_tiles``: the tiles the
+  march-kernel autotuner chose in this run.
+* ``fluid``: the Stokes-Brinkman diffuser's design loop on the GPU beside the fluid
+  oracle on the host.
 * ``roofline``: the dominant kernel (the FP32 matrix-free P2 operator),
   algorithmic bytes 2*V2u*4 + V1*4 per launch over its CUDA-event duration
   measured in this run, against the measured HBM copy bandwidth.
 * ``cpu_baseline`` / ``--impl reference``: the FP64 oracle (the reference
   algorithm: filter solves, sparse assembly + SuperLU, Newton projection) timed
   on this host's cores over real design iterations of the same loop, on the
-  --ref-grid cantilever (160x80 by default: one oracle iteration at 1000x500
-  takes tens of minutes).  ``same_grid``: the GPU loop on that grid, so that a
-  same-grid comparison exists beside the headline one.
+  --ref-grid cantilever (160x80 by default: SuperLU cannot factor the 1000x500
+  state matrix on a 62 GB host).  ``same_grid``: the GPU loop on that grid, so
+  that a same-grid comparison exists beside the headline one.
 """
 from __future__ import annotations
 
