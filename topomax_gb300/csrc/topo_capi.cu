@@ -988,13 +988,13 @@ int topo_sensitivity_rhs(topo_ctx* ctx, const double* u, const double* xi, doubl
     KClock kc(s, "sensitivity (moments + vertex gather)", 0, (2.0 * ctx->nn2 + 2.0 * ctx->nv) * 8.0);
     if (ctx->precision == TOPO_PREC_MIXED) {
       float* tri = static_cast<float*>(ctx->sens_tri);
-      k_sens_tri<float><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
+      k_sens_tri<float><<<ctx->grid(nt / 2), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
                                                                float(ctx->lmbda), float(ctx->mu), float(area),
                                                                make_penal<float>(ctx->p, ctx->pmin), u, xi, tri);
       k_vertex_gather3<float><<<ctx->grid(ctx->nv), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, tri, b);
     } else {
       double* tri = static_cast<double*>(ctx->sens_tri);
-      k_sens_tri<double><<<ctx->grid(nt), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
+      k_sens_tri<double><<<ctx->grid(nt / 2), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, 1.0 / ctx->hx, 1.0 / ctx->hy,
                                                                 ctx->lmbda, ctx->mu, area,
                                                                 make_penal<double>(ctx->p, ctx->pmin), u, xi, tri);
       k_vertex_gather3<double><<<ctx->grid(ctx->nv), kVecThreads, 0, s>>>(ctx->nx, ctx->ny, tri, b);

@@ -190,22 +190,13 @@ struct P1Off {
 };
 
 // Local P2 node offsets (da,db) inside a square, order [A,B,C,mid(BC),mid(AC),mid(AB)].
-TOPO_HD int p2_off_a(int o, int k) {
-  const int t[2][6] = {{0, 2, 2, 2, 1, 1}, {0, 0, 2, 1, 1, 0}};
-  return t[o][k];
-}
-TOPO_HD int p2_off_b(int o, int k) {
-  const int t[2][6] = {{0, 0, 2, 1, 1, 0}, {0, 2, 2, 2, 1, 1}};
-  return t[o][k];
-}
+// The tables are packed two bits per entry, entry (o, k) at bit 2 (6 o + k) (P1:
+// 2 (3 o + k)), so that a run-time orientation costs a shift instead of a table
+// built in local memory.
+TOPO_HD constexpr int p2_off_a(int o, int k) { return int((0x1605a8u >> (2 * (6 * o + k))) & 3u); }
+TOPO_HD constexpr int p2_off_b(int o, int k) { return int((0x5a8160u >> (2 * (6 * o + k))) & 3u); }
 // Local P1 vertex offsets, order [A,B,C].
-TOPO_HD int p1_off_a(int o, int k) {
-  const int t[2][3] = {{0, 1, 1}, {0, 0, 1}};
-  return t[o][k];
-}
-TOPO_HD int p1_off_b(int o, int k) {
-  const int t[2][3] = {{0, 0, 1}, {0, 1, 1}};
-  return t[o][k];
-}
+TOPO_HD constexpr int p1_off_a(int o, int k) { return int((0x414u >> (2 * (3 * o + k))) & 3u); }
+TOPO_HD constexpr int p1_off_b(int o, int k) { return int((0x510u >> (2 * (3 * o + k))) & 3u); }
 
 }  // namespace topo

@@ -28,10 +28,15 @@ struct P1Params {
 };
 
 // The six (cell offset, orientation, local vertex) incidences of vertex (a,b).
+// Packed five bits per incidence e (at bit 5 e): dci + 1, dcj + 1, o, loc (two bits):
+//   e = 0..5: (-1,-1,0,2) (-1,-1,1,2) (0,-1,1,1) (-1,0,0,1) (0,0,0,0) (0,0,1,0)
+TOPO_HD constexpr unsigned p1_incidence_bits(int e) { return (0xe353690u >> (5 * e)) & 31u; }
 TOPO_HD void p1_incidence(int e, int& dci, int& dcj, int& o, int& loc) {
-  const int t[6][4] = {{-1, -1, 0, 2}, {-1, -1, 1, 2}, {0, -1, 1, 1},
-                       {-1, 0, 0, 1},  {0, 0, 0, 0},   {0, 0, 1, 0}};
-  dci = t[e][0]; dcj = t[e][1]; o = t[e][2]; loc = t[e][3];
+  const unsigned f = p1_incidence_bits(e);
+  dci = int(f & 1u) - 1;
+  dcj = int((f >> 1) & 1u) - 1;
+  o = int((f >> 2) & 1u);
+  loc = int(f >> 3);
 }
 
 // Input of a node apply read directly from an array.
@@ -134,13 +139,14 @@ struct P1Kern {
 // on the fine level (fine cells beyond nxf x nyf contribute zero).
 template <class T>
 TOPO_HD T coarsen_kappa(const T* kf, int nxf, int nyf, int I, int J, int o) {
-  // children (dci, dcj, orientation)
-  const int ch[2][4][3] = {{{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 0}},
-                           {{0, 0, 1}, {0, 1, 1}, {0, 1, 0}, {1, 1, 1}}};
+  // children k = 0..3 of coarse triangle o: (dci, dcj, orientation) as bits 0, 1, 2
+  // of the 3-bit field 4 o + k:  o = 0: (0,0,0) (1,0,0) (1,0,1) (1,1,0);
+  //                              o = 1: (0,0,1) (0,1,1) (0,1,0) (1,1,1)
   T s = T(0);
   for (int k = 0; k < 4; ++k) {
-    const int i = 2 * I + ch[o][k][0], j = 2 * J + ch[o][k][1];
-    if (i < nxf && j < nyf) s += kf[(size_t(j) * nxf + i) * 2 + ch[o][k][2]];
+    const unsigned c = (0xeb4748u >> (3 * (4 * o + k))) & 7u;
+    const int i = 2 * I + int(c & 1u), j = 2 * J + int((c >> 1) & 1u);
+    if (i < nxf && j < nyf) s += kf[(size_t(j) * nxf + i) * 2 + int(c >> 2)];
   }
   return T(0.25) * s;
 }
@@ -242,7 +248,7 @@ struct StencilLayout {
 TOPO_HD constexpr int st_da(int k) { return k == 1 ? 1 : k == 2 ? -1 : k == 5 ? 1 : k == 6 ? -1 : 0; }
 TOPO_HD constexpr int st_db(int k) { return k == 3 ? 1 : k == 4 ? -1 : k == 5 ? 1 : k == 6 ? -1 : 0; }
 // block of offset (da, db): 0 self, 1 E, 2 W, 3 N, 4 S, 5 NE, 6 SW
-TOPO_HD int st_block(int da, int db) {
+TOPO_HD constexpr int st_block(int da, int db) {
   if (da == 0) return db == 0 ? 0 : db == 1 ? 3 : 4;
   if (db == 0) return da == 1 ? 1 : 2;
   return da == 1 ? 5 : 6;
@@ -279,6 +285,11 @@ TOPO_HD void p1_stencil_node(int a, int b, const P1Params<T, NC>& P, T* out) {
     for (int c = 0; c < NC; ++c) rs[c * NC + c] = 1.0;
   } else {
     const bool chk = P1Kern<T, NC>::near_clamped(P.dir, a, b);
+    // fully unrolled on the GPU: every block index is then a constant and the
+    // row stays in registers
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
     for (int e = 0; e < 6; ++e) {
       int dci, dcj, o, loc;
       p1_incidence(e, dci, dcj, o, loc);
@@ -287,11 +298,20 @@ TOPO_HD void p1_stencil_node(int a, int b, const P1Params<T, NC>& P, T* out) {
       const size_t t = (size_t(cj) * P.nx + ci) * 2 + o;
       const double kk = P.kK ? double(P.kK[t]) : double(P.kK_c);
       const double km = (NC == 1) ? (P.kM ? double(P.kM[t]) : double(P.kM_c)) : 0.0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
       for (int L = 0; L < 3; ++L) {
-        const int al = ci + p1_off_a(o, L), bl = cj + p1_off_b(o, L);
-        if (chk && is_clamped(P.dir, al, bl)) continue;
-        T* bk = blk + st_block(al - a, bl - b) * SB;
+        const int da = dci + p1_off_a(o, L), db = dcj + p1_off_b(o, L);
+        if (chk && is_clamped(P.dir, a + da, b + db)) continue;
+        T* bk = blk + st_block(da, db) * SB;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
         for (int c = 0; c < NC; ++c)
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
           for (int d = 0; d < NC; ++d) {
             double v = kk * double(P.K[o][loc * NC + c][L * NC + d]);
             if (NC == 1) v += km * double(P.Mm[o][loc][L]);

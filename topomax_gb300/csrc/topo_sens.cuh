@@ -8,41 +8,74 @@
 
 namespace topo {
 
-// out[3t+k] = int_T s phi_k for every triangle t (FEM_src/elasisity_problem.py:146-149)
+// moments of triangle O of a cell from the cell's node values U (3x3 nodes) and
+// vertex densities X (2x2), in the node orders of P2Off / P1Off
+template <int O, class TG, class TQ>
+__device__ __forceinline__ void sens_cell_tri(const TG (&U)[3][3][2], const TQ (&X)[2][2], TG ihx, TG ihy, TQ lam,
+                                              TQ mu, TQ area, const Penal<TQ>& pen, TQ (&c)[3]) {
+  TG ue[6][2];
+#define TOPO_UE(K)                                      \
+  ue[K][0] = U[P2Off<O, K>::b][P2Off<O, K>::a][0];      \
+  ue[K][1] = U[P2Off<O, K>::b][P2Off<O, K>::a][1];
+  TOPO_UE(0) TOPO_UE(1) TOPO_UE(2) TOPO_UE(3) TOPO_UE(4) TOPO_UE(5)
+#undef TOPO_UE
+  const TQ xe[3] = {X[P1Off<O, 0>::b][P1Off<O, 0>::a], X[P1Off<O, 1>::b][P1Off<O, 1>::a],
+                    X[P1Off<O, 2>::b][P1Off<O, 2>::a]};
+  tri_sensitivity<O, TG, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+}
+
+// out[3t+k] = int_T s phi_k for every triangle t (FEM_src/elasisity_problem.py:146-149).
+// One thread per cell: the cell's 3x3 P2 nodes and 2x2 vertices are loaded once
+// and both triangles are evaluated with compile-time node offsets, so the lanes
+// of a warp run the same instructions (a thread per triangle would alternate
+// orientations within the warp and run both code paths).  Output t = 2 cell + o:
+// six consecutive values per cell.
 template <class TQ>
 __global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu, TQ area, Penal<TQ> pen,
                            const double* __restrict__ u, const double* __restrict__ xi, TQ* __restrict__ out) {
-  const size_t nt = size_t(2) * nx * ny;
+  const size_t ncell = size_t(nx) * ny;
   const int VX = nx + 1, NX = 2 * nx + 1;
-  TOPO_GRID_STRIDE(t, nt) {
-    const int o = int(t & 1);
-    const size_t cell = t >> 1;
+  TOPO_GRID_STRIDE(cell, ncell) {
     const int i = int(cell % nx), j = int(cell / nx);
-    double ue[6][2];
-    for (int k = 0; k < 6; ++k) {
-      const size_t n = size_t(2 * j + p2_off_b(o, k)) * NX + 2 * i + p2_off_a(o, k);
-      ue[k][0] = u[2 * n];
-      ue[k][1] = u[2 * n + 1];
-    }
-    TQ xe[3];
-    for (int k = 0; k < 3; ++k) xe[k] = TQ(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
-    TQ c[3];
+    double un[3][3][2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t n = size_t(2 * j + r) * NX + 2 * i + c;
+        un[r][c][0] = u[2 * n];
+        un[r][c][1] = u[2 * n + 1];
+      }
+    TQ xv[2][2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) xv[r][c] = TQ(xi[size_t(j + r) * VX + i + c]);
+    TQ c0[3], c1[3];
     if constexpr (sizeof(TQ) == 4) {
       // difference form: the gradient ignores a translation, so the node values enter as
-      // u - u_A, subtracted in FP64 (exact for a smooth field) and rounded to FP32, where
-      // the gradients and the quadrature run (FP64 arithmetic is scarce on this GPU)
-      TQ ud[6][2];
-      for (int k = 0; k < 6; ++k)
-        for (int d = 0; d < 2; ++d) ud[k][d] = k == 0 ? TQ(0) : TQ(ue[k][d] - ue[0][d]);
-      if (o == 0) tri_sensitivity<0, TQ, TQ>(ud, xe, TQ(ihx), TQ(ihy), lam, mu, area, pen, c);
-      else tri_sensitivity<1, TQ, TQ>(ud, xe, TQ(ihx), TQ(ihy), lam, mu, area, pen, c);
+      // u - u_A (vertex A = node (0,0) of both triangles), subtracted in FP64 (exact for a
+      // smooth field) and rounded to FP32, where the gradients and the quadrature run (FP64
+      // arithmetic is scarce on this GPU)
+      TQ ud[3][3][2];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 2; ++d) ud[r][c][d] = (r | c) ? TQ(un[r][c][d] - un[0][0][d]) : TQ(0);
+      sens_cell_tri<0>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c0);
+      sens_cell_tri<1>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c1);
     } else {
-      if (o == 0) tri_sensitivity<0, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
-      else tri_sensitivity<1, double, TQ>(ue, xe, ihx, ihy, lam, mu, area, pen, c);
+      sens_cell_tri<0>(un, xv, ihx, ihy, lam, mu, area, pen, c0);
+      sens_cell_tri<1>(un, xv, ihx, ihy, lam, mu, area, pen, c1);
     }
-    out[3 * t] = c[0];
-    out[3 * t + 1] = c[1];
-    out[3 * t + 2] = c[2];
+    TQ* o = out + 6 * cell;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      o[k] = c0[k];
+      o[3 + k] = c1[k];
+    }
   }
 }
 
