@@ -2,6 +2,7 @@
 // iterative refinement, sensitivity and the entropic-mirror-descent update.
 #include <algorithm>
 #include <chrono>
+#include <cfloat>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -83,9 +84,14 @@ __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf,
   }
 }
 
+// half = psi_prev - alpha g, and ehalf = exp(-half) for the Newton evaluations
 __global__ void k_emd_half(const double* __restrict__ psi_prev, const double* __restrict__ g, double alpha,
-                           double* __restrict__ half, size_t n) {
-  TOPO_GRID_STRIDE(i, n) half[i] = psi_prev[i] - alpha * g[i];
+                           double* __restrict__ half, double* __restrict__ ehalf, size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    const double h = psi_prev[i] - alpha * g[i];
+    half[i] = h;
+    ehalf[i] = exp(-h);
+  }
 }
 
 // One Newton step of  F(c) = int expit(half + c) - volume = 0  (src/solver.py:149-186,
@@ -97,13 +103,21 @@ __global__ void k_extrapolate(double* __restrict__ y, const double* __restrict__
   TOPO_GRID_STRIDE(i, n) y[i] = order == 1 ? 2.0 * x1[i] - x2[i] : 3.0 * (x1[i] - x2[i]) + x3[i];
 }
 
-__global__ void k_newton(const double* __restrict__ half, const double* __restrict__ w, size_t n, double volume,
-                         double tol, int maxit, double* partials, unsigned* counter, NewtonState* st) {
+// expit(half + c) = 1 / (1 + exp(-half) exp(-c)): with exp(-half) evaluated once per
+// projection (ehalf), an evaluation costs one exponential per thread instead of one
+// per node (FP64 arithmetic is scarce on this GPU).  Where either factor is zero or
+// infinite the product could be 0 * inf; those nodes take the direct formula.
+__global__ void k_newton(const double* __restrict__ half, const double* __restrict__ ehalf,
+                         const double* __restrict__ w, size_t n, double volume, double tol, int maxit,
+                         double* partials, unsigned* counter, NewtonState* st) {
   if (st->done) return;
   const double c = st->c;
+  const double q = exp(-c);
+  const bool q_ok = q > 0.0 && q <= DBL_MAX;
   double v[2] = {0.0, 0.0};
   TOPO_GRID_STRIDE(i, n) {
-    const double e = expit_d(half[i] + c);
+    const double eh = ehalf[i];
+    const double e = (q_ok && eh > 0.0 && eh <= DBL_MAX) ? 1.0 / (1.0 + eh * q) : expit_d(half[i] + c);
     v[0] += w[i] * e;
     v[1] += w[i] * (e * (1.0 - e));
   }
@@ -251,6 +265,7 @@ struct topo_ctx {
   // sensitivity / design scratch
   void* sens_tri = nullptr;
   double* half = nullptr;
+  double* ehalf = nullptr;  // exp(-half)
   NewtonState* nstate = nullptr;
   double* cfix = nullptr;
 
@@ -374,6 +389,7 @@ int init_common(topo_ctx* C, const topo_grid_desc* g, int precision) {
   if (!C->vw) return C->fail(TOPO_ERR_CUDA, "out of device memory");
   cudaMemcpy(C->vw, w.data(), C->nv * sizeof(double), cudaMemcpyHostToDevice);
   C->half = C->arena.alloc_n<double>(C->nv);
+  C->ehalf = C->arena.alloc_n<double>(C->nv);
   C->nstate = C->arena.alloc_n<NewtonState>(1);
   C->cfix = C->arena.alloc_n<double>(1);
   return TOPO_OK;
@@ -1020,7 +1036,7 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
       return ctx->fail(TOPO_ERR_ARG, "invalid step arguments");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const size_t n = ctx->nv;
-    k_emd_half<<<ctx->grid(n), kVecThreads, 0, s>>>(psi_prev, g, alpha, ctx->half, n);
+    k_emd_half<<<ctx->grid(n), kVecThreads, 0, s>>>(psi_prev, g, alpha, ctx->half, ctx->ehalf, n);
     ctx->launches += 2;  // half step and the final update
     NewtonState init{};
     init.c = 0.0;
@@ -1034,10 +1050,10 @@ int topo_emd_step(topo_ctx* ctx, const double* psi_prev, const double* g, double
         if (launched == 0 && k == 0) {
           // the clock times the first evaluation (later launches of a chunk may find Newton done)
           KClock kc(s, "Newton evaluation (volume and its derivative)", 0, 2.0 * n * 8.0);
-          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
+          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->ehalf, ctx->vw, n, volume, 1e-12, maxit,
                                                             ctx->red.partials, ctx->red.counter, ctx->nstate);
         } else {
-          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->vw, n, volume, 1e-12, maxit,
+          k_newton<<<ctx->red.blocks, kVecThreads, 0, s>>>(ctx->half, ctx->ehalf, ctx->vw, n, volume, 1e-12, maxit,
                                                             ctx->red.partials, ctx->red.counter, ctx->nstate);
         }
       }
