@@ -216,13 +216,24 @@ void emu_set_segment(int seg) { seg_override = seg; }
 
 int emu_dir_ints() { return kDirInts; }
 
-// y = K(xi) u (mode 0) or diag K(xi) (mode 1); prec 0 = FP64, 1 = FP32
+// y = K(xi) u (mode 0) or diag K(xi) (mode 1); prec 0 = FP64, 1 = FP32, 2 = pair-of-FP32 (mode 0)
 int emu_p2_apply(int prec, int nx, int ny, double hx, double hy, double lam, double mu, double p, double pmin,
                  const int* dir, const double* xi, const double* u, double* y, int mode) {
   const size_t nv = size_t(nx + 1) * (ny + 1), nd = size_t(2) * (2 * nx + 1) * (2 * ny + 1);
   if (prec == 0) {
     auto P = p2params<double>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
     p2_run<double>(P, xi, u, y, mode);
+  } else if (prec == 2) {
+    // pair-of-FP32 operator (Apply only): mass matrices precomputed in FP64 and split
+    if (mode != 0 || !u) return -1;
+    auto P = p2params<dd>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
+    const Penal<double> pen = make_penal<double>(p, pmin, 0);
+    std::vector<dd> rm(size_t(12) * nx * ny);
+    std::vector<double> kK(size_t(2) * nx * ny);
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) cell_rmass_kappa<double, dd>(i, j, nx, ny, xi, pen, rm.data(), kK.data());
+    P.rmass = rm.data();
+    p2_run<dd>(P, nullptr, reinterpret_cast<const dd*>(u), reinterpret_cast<dd*>(y), 0);
   } else {
     auto P = p2params<float>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
     std::vector<float> xf(xi, xi + nv), uf(nd, 0.f), yf(nd, 0.f);

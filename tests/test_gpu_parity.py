@@ -262,6 +262,31 @@ def test_tail_matches_level_kernels(precision, monkeypatch):
     assert np.max(np.abs(results[0][1] - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+def test_pair_fp32_residual_operator_matches_fp64(monkeypatch):
+    """Mixed precision computes its refinement residuals b - K u with the pair-of-FP32
+    operator (FP32-pipe arithmetic, differences of the FP64 operand taken in FP64);
+    TOPO_RESIDUAL_FP64=1 selects the FP64 operator.  On a high-contrast design both
+    reach the true FP64 residual the solve asks for (1e-10, checked with the FP64
+    operator) and their solutions agree to that tolerance."""
+    import torch
+    from topomax_gb300 import fem as F
+    d = _design()
+    results = []
+    for flag in ("0", "1"):
+        monkeypatch.setenv("TOPO_RESIDUAL_FP64", flag)
+        prob, V = _gpu_problem(d, 200, 100, rtol=1e-10)
+        prob.set_penalization(3.0)
+        g = torch.Generator().manual_seed(5)
+        xi = F.Function(V, (torch.rand(V.dim(), generator=g, dtype=torch.float64) * 0.99 + 0.01).cuda())
+        u = prob.forward(xi).tensor.clone()
+        b = prob.load_vector()
+        r = b - prob.apply_operator(xi.tensor, u)
+        assert (r.norm() / b.norm()).item() <= 1e-10
+        results.append(u.cpu().numpy())
+        del prob
+    assert np.linalg.norm(results[0] - results[1]) <= 1e-9 * np.linalg.norm(results[1])
+
+
 def test_contexts_of_different_sizes_interleave():
     """Kernel attributes are process-wide: a context created later (here a smaller
     mesh) must not break the launches of an earlier one."""

@@ -87,6 +87,65 @@ def test_p2_march_result_does_not_depend_on_the_segment():
         emu.set_segment(0)
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_p2_apply_pair_fp32_matches_oracle(case):
+    """The refinement residual's operator in pair-of-FP32 arithmetic (dd, about 48
+    significant bits on the FP32 pipe) against the oracle's assembled FP64 matrix, at
+    the FP64 march's tolerance."""
+    W, H, nx, ny, sides, p = case
+    d, L, o, xi, u, dirv = _problem(*case)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    y = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=2)
+    ref = o.apply_state(xi, u)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_p2_pair_fp32_residual_accuracy_at_a_smooth_field():
+    """A refinement residual b - K u cancels K u against b to many digits, so the
+    operator's rounding must stay small against |K| |u|, not against |K u|: at a smooth
+    field riding on a large translation (K u is 1e-5 of |K| |u| here) the pair-of-FP32
+    apply agrees with the FP64 one to 1e-13 of |K| |u|."""
+    W, H, nx, ny, sides, p = CASES[3]   # no clamped nodes (their identity rows return u itself)
+    d, L, o, xi, u, dirv = _problem(*CASES[3])
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    xs = np.arange(2 * nx + 1) * (L.hx / 2)
+    ys = np.arange(2 * ny + 1) * (L.hy / 2)
+    X, Y = np.meshgrid(xs, ys)
+    us = np.empty(2 * L.n_p2)
+    us[0::2] = (250.0 + 0.01 * X * X + 0.003 * X * Y).ravel()
+    us[1::2] = (-75.0 + 0.02 * np.sin(3.0 * X) * Y).ravel()
+    y64 = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, us)
+    ydd = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, us, prec=2)
+    # |K| |u| scale: the operator's row magnitudes times the field's size
+    scale = np.max(np.abs(emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u))) / np.max(np.abs(u)) * \
+        np.max(np.abs(us))
+    assert np.max(np.abs(y64)) < 1e-3 * scale   # the cancellation this test is about
+    assert np.max(np.abs(ydd - y64)) <= 1e-13 * scale
+
+
+def test_p2_pair_fp32_residual_at_a_solved_state():
+    """At the oracle's solved displacement of a high-contrast design (xi ~ U(0.01, 1),
+    p = 3) the pair-of-FP32 operator reproduces K u as closely as the FP64 march does:
+    both differ from the oracle's assembled product by ~3e-11 of |b| (the attainable
+    residual of this problem in FP64), and from each other by less."""
+    W, H, nx, ny, sides, p = 2.0, 1.0, 80, 40, ["Left"], 3.0
+    d = make_design(width=W, height=H, fixed_sides=sides)
+    L = Lattice(W, H, nx, ny)
+    o = FEMOracle(L, d)
+    o.set_penalization(p)
+    xi = np.random.default_rng(1).uniform(0.01, 1.0, L.n_vertices)
+    u = o.state_solve(xi)
+    b = o.apply_state(xi, u)
+    dirv = emu.make_dir(nx, ny, L.hx, L.hy, sides)
+    lam, mu = lame(d.young_modulus, d.poisson_ratio)
+    y64 = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u)
+    ydd = emu.p2_apply(nx, ny, L.hx, L.hy, lam, mu, p, dirv, xi, u, prec=2)
+    nb = np.linalg.norm(b)
+    assert np.linalg.norm(y64 - b) <= 1e-10 * nb
+    assert np.linalg.norm(ydd - b) <= 1e-10 * nb
+    assert np.linalg.norm(ydd - y64) <= 2e-11 * nb
+
+
 @pytest.mark.parametrize("case", CASES[:3])
 def test_p2_apply_fp32_matches_oracle(case):
     W, H, nx, ny, sides, p = case

@@ -67,11 +67,13 @@ __global__ void k_cell_rmass32(int nx, int ny, Penal<float> pen, const float* __
   TOPO_GRID_STRIDE(c, nc) cell_rmass<float>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
 }
 
-// kappa of state level 1 and the FP64 operator's mass matrices, one pass
+// kappa of state level 1 and the residual operator's mass matrices (RM: FP64, or
+// (hi, lo) pairs for the pair-of-FP32 operator), one pass
+template <class RM>
 __global__ void k_cell_rmass_kappa(int nx, int ny, Penal<double> pen, const double* __restrict__ xi,
-                                   double* __restrict__ rm, double* __restrict__ kK) {
+                                   RM* __restrict__ rm, double* __restrict__ kK) {
   const size_t nc = size_t(nx) * ny;
-  TOPO_GRID_STRIDE(c, nc) cell_rmass_kappa<double>(int(c % nx), int(c / nx), nx, ny, xi, pen, rm, kK);
+  TOPO_GRID_STRIDE(c, nc) cell_rmass_kappa<double, RM>(int(c % nx), int(c / nx), nx, ny, xi, pen, rm, kK);
 }
 
 __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
@@ -217,7 +219,10 @@ struct topo_ctx {
   float* xi32 = nullptr;
   double* xi64 = nullptr;  // FP64 mode: the design copied to a fixed buffer (graphs keep their parameters)
   // per-triangle r-weighted mass matrices of the current design, [o][k][cell]
-  double* rm_op64 = nullptr;  // true penalisation (FP64 operator)
+  double* rm_op64 = nullptr;  // true penalisation (residual operator): FP64, or (hi, lo) pairs when op_dd
+  // mixed precision: the refinement residuals use the pair-of-FP32 operator
+  // (TOPO_RESIDUAL_FP64=1: the FP64 one)
+  bool op_dd = false;
   double* rm_pc64 = nullptr;  // clamped (FP64 preconditioner, FP64 mode)
   bool trace_solves = false;  // TOPO_TRACE_SOLVES=1: one line per refinement step and inner solve
   bool verify_residual = false;  // TOPO_VERIFY_RESIDUAL=1: confirm FGMRES convergence with a true residual
@@ -686,7 +691,12 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   Penal<double> pen = make_penal<double>(C->p, C->pmin, 1);
   const size_t ncell = size_t(C->nx) * C->ny;
   const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
-  k_cell_rmass_kappa<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64, C->skK[1]);
+  if (C->op_dd)
+    k_cell_rmass_kappa<dd><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi,
+                                                                  reinterpret_cast<dd*>(C->rm_op64), C->skK[1]);
+  else
+    k_cell_rmass_kappa<double><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi, C->rm_op64,
+                                                                      C->skK[1]);
   C->launches += 1 + (L - 2);
   for (int l = 2; l < L; ++l) {
     const LevelSpec &F = C->sspec[l - 1], &Cc = C->sspec[l];
@@ -809,6 +819,8 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       C->r64 = C->arena.alloc_n<double>(n);
       C->y64 = C->arena.alloc_n<double>(n);
       if (precision == TOPO_PREC_MIXED) {
+        C->op_dd = !env_flag("TOPO_RESIDUAL_FP64", false);
+        if (C->op_dd) p2_dd_prime();
         C->smg32.use_graphs = graphs_enabled();
         C->smg32.fp64_solution = true;
         C->smg32.cheb_lo_frac = C->cheb_lo_state;
@@ -957,10 +969,17 @@ int topo_state_solve(topo_ctx* ctx, const double* xi, double* u, double rtol, in
     const bool warm = (flags & TOPO_SOLVE_WARM) != 0;
     SolveStats st;
     if (ctx->precision == TOPO_PREC_MIXED) {
-      P2Params<double> P64 = ctx->p2params<double>(0, ctx->rm_op64);
-      auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
-      rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm, ctx->max_iterations(kStateMaxIt),
-                     ctx->inner_floor_state, st, s);
+      if (ctx->op_dd) {
+        const P2Params<dd> Pdd = ctx->p2params<dd>(0, reinterpret_cast<const dd*>(ctx->rm_op64));
+        auto ap = [Pdd](const double* x, double* y, cudaStream_t ss) { p2_apply_dd(Pdd, x, y, ss); };
+        rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm,
+                       ctx->max_iterations(kStateMaxIt), ctx->inner_floor_state, st, s);
+      } else {
+        const P2Params<double> P64 = ctx->p2params<double>(0, ctx->rm_op64);
+        auto ap = [P64, xi](const double* x, double* y, cudaStream_t ss) { p2_apply_f64(P64, xi, x, y, ss); };
+        rc = fgmres_ir(ctx, ctx->smg32, ap, ctx->load, u, warm, n, rtol, ctx->sgm,
+                       ctx->max_iterations(kStateMaxIt), ctx->inner_floor_state, st, s);
+      }
     } else {
       rc = ctx->smg64.pcg(ctx->load, u, warm, rtol, ctx->max_iterations(kStateMaxIt), st, s);
       if (rc == -4) rc = ctx->fail(TOPO_ERR_NAN, "non-finite value in the state solve");

@@ -288,5 +288,9 @@ void p2_apply_f64(const P2Params<double>& p, const double* xi, const double* x, 
                   cudaStream_t s);
 void p2_apply_f32(const P2Params<float>& p, const float* xi, const float* x, float* y,
                   cudaStream_t s);
+// y = A x with pair-of-FP32 arithmetic (x, y FP64; p.rmass: per-cell mass matrices as
+// (hi, lo) pairs), and its one-time occupancy query (outside any stream capture)
+void p2_apply_dd(const P2Params<dd>& p, const double* x, double* y, cudaStream_t s);
+void p2_dd_prime();
 
 }  // namespace topo

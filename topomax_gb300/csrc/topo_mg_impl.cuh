@@ -43,6 +43,8 @@ template <class T>
 __device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 template <class T>
 __device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ dd shfl_down1(dd v) { return dd(shfl_down1(v.hi), shfl_down1(v.lo)); }
+__device__ __forceinline__ dd shfl_up1(dd v) { return dd(shfl_up1(v.hi), shfl_up1(v.lo)); }
 
 // column 2 of rows R0..2 (operand) and of density rows from lane L+1
 template <class T, int R0, bool OPERAND>
@@ -123,8 +125,14 @@ __device__ __forceinline__ void p2_march_run(const P2Params<T>& P, const T* __re
   }
 }
 
+// resident blocks the register budget is sized for: FP32 4, pair-of-FP32 3, FP64 2
+template <class T>
+constexpr int p2_march_min_blocks() {
+  return IsDD<T>::value ? 3 : sizeof(T) == 4 ? 4 : 2;
+}
+
 template <class T, int MODE>
-__global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(P2M_THREADS, p2_march_min_blocks<T>())
     k_p2_march(P2Params<T> P, const T* __restrict__ xi, P2Io<T> io, int seg) {
   TOPO_PDL_ENTRY();
   io.mode = MODE;  // compile-time mode: the per-node switches fold
@@ -140,7 +148,7 @@ __global__ void __launch_bounds__(P2M_THREADS, sizeof(T) == 4 ? 4 : 2)
     else
       p2_march_run<T, MODE, false>(P, xi, io, lane, js, je, acc);
   }
-  if constexpr (MODE == kP2Apply || MODE == kP2Post2) {
+  if constexpr ((MODE == kP2Apply || MODE == kP2Post2) && !IsDD<T>::value) {
     if (io.fuse != kFuseNone) {
       double tot[2];
       if (finish_reduction<2>(acc, io.partials, io.counter, tot)) {
@@ -758,6 +766,22 @@ inline void launch_p2_apply(const P2Params<T>& P, const T* xi, const T* x, T* y,
   io.u = x;
   io.y = y;
   launch_p2_tile<T>(P, xi, io, s);
+}
+
+// y = A x with the pair-of-FP32 operator: x, y FP64, P.rmass the mass matrices as
+// (hi, lo) pairs (the design is not read)
+inline void launch_p2_apply_dd(const P2Params<dd>& P, const double* x, double* y, cudaStream_t s) {
+  P2Io<dd> io;
+  std::memset(&io, 0, sizeof(io));
+  io.mode = kP2Apply;
+  io.u = reinterpret_cast<const dd*>(x);
+  io.y = reinterpret_cast<dd*>(y);
+  int seg = 0;
+  const dim3 g = march_grid(P.nx, P.ny, p2_march_bps<dd, kP2Apply>(), seg);
+  // x read and y written in FP64, the mass matrices (12 pairs per cell)
+  const double n = 2.0 * (2 * P.nx + 1) * (2 * P.ny + 1), nc = double(P.nx) * P.ny;
+  KClock kc(s, "P2 march pair-of-FP32 Apply", 0, 2.0 * n * 8.0 + 12.0 * nc * 8.0);
+  launch_pdl(k_p2_march<dd, kP2Apply>, g, P2M_THREADS, 0, s, P, static_cast<const dd*>(nullptr), io, seg);
 }
 
 template <class T, int NC>

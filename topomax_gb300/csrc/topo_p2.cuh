@@ -14,39 +14,65 @@
 #pragma once
 
 #include "topo_common.cuh"
+#include "topo_dd.cuh"
 #include "topo_p1.cuh"
 
 namespace topo {
 
 // The two displacement components of a node (and the smoothing vectors' pair
-// at a node) are adjacent: one 8-byte (FP32) or 16-byte (FP64) access.
+// at a node) are adjacent: one 8-byte (FP32) or 16-byte (FP64) access.  With the
+// pair-of-FP32 type (dd) the vectors are FP64 in memory: a load keeps the double's
+// bits (dd_pack_double; the element phase takes differences in FP64 and splits
+// them), a store rounds hi + lo to a double.
 template <class T>
 TOPO_HD void ld2(const T* p, T (&v)[2]) {
+  if constexpr (IsDD<T>::value) {
+    const double* q = reinterpret_cast<const double*>(p);
 #if defined(__CUDA_ARCH__)
-  if constexpr (sizeof(T) == 4) {
-    const float2 t = *reinterpret_cast<const float2*>(p);
-    v[0] = t.x;
-    v[1] = t.y;
-  } else {
-    const double2 t = *reinterpret_cast<const double2*>(p);
-    v[0] = t.x;
-    v[1] = t.y;
-  }
+    const double2 t = *reinterpret_cast<const double2*>(q);
+    v[0] = dd_pack_double(t.x);
+    v[1] = dd_pack_double(t.y);
 #else
-  v[0] = p[0];
-  v[1] = p[1];
+    v[0] = dd_pack_double(q[0]);
+    v[1] = dd_pack_double(q[1]);
 #endif
+  } else {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 4) {
+      const float2 t = *reinterpret_cast<const float2*>(p);
+      v[0] = t.x;
+      v[1] = t.y;
+    } else {
+      const double2 t = *reinterpret_cast<const double2*>(p);
+      v[0] = t.x;
+      v[1] = t.y;
+    }
+#else
+    v[0] = p[0];
+    v[1] = p[1];
+#endif
+  }
 }
 
 template <class T>
 TOPO_HD void st2(T* p, T a, T b) {
+  if constexpr (IsDD<T>::value) {
+    double* q = reinterpret_cast<double*>(p);
 #if defined(__CUDA_ARCH__)
-  if constexpr (sizeof(T) == 4) *reinterpret_cast<float2*>(p) = make_float2(a, b);
-  else *reinterpret_cast<double2*>(p) = make_double2(a, b);
+    *reinterpret_cast<double2*>(q) = make_double2(dd_to_double(a), dd_to_double(b));
 #else
-  p[0] = a;
-  p[1] = b;
+    q[0] = dd_to_double(a);
+    q[1] = dd_to_double(b);
 #endif
+  } else {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 4) *reinterpret_cast<float2*>(p) = make_float2(a, b);
+    else *reinterpret_cast<double2*>(p) = make_double2(a, b);
+#else
+    p[0] = a;
+    p[1] = b;
+#endif
+  }
 }
 
 template <class T>
@@ -386,6 +412,7 @@ struct P2March {
   // density at vertex (i + c, j) of the lane (rows j <= ny always)
   template <bool LEAN = false>
   TOPO_HD static T density(const P2Params<T>& P, const T* xi, const P2Mask& K, int c, int i, int j) {
+    if constexpr (IsDD<T>::value) return T(0);  // the pair-of-FP32 operator reads precomputed mass matrices
     if (!LEAN && !K.vcol[c]) return T(0);
     return xi[unsigned(j) * unsigned(P.nx + 1) + unsigned(i + c)];
   }
@@ -420,8 +447,9 @@ struct P2March {
     const T xe[3] = {L.X[P1Off<O, 0>::b][P1Off<O, 0>::a], L.X[P1Off<O, 1>::b][P1Off<O, 1>::a],
                      L.X[P1Off<O, 2>::b][P1Off<O, 2>::a]};
     T y[6][2];
+    if constexpr (IsDD<T>::value) mode = kP2Apply;  // Apply only (precomputed mass matrices)
     if (mode == kP2Diag) {
-      tri_diag(O, xe, P, y);
+      if constexpr (!IsDD<T>::value) tri_diag(O, xe, P, y);
     } else {
       T ue[6][2];
 #define TOPO_LD(K)                                                                                      \
@@ -439,16 +467,21 @@ struct P2March {
 #pragma unroll
 #endif
       for (int c = 0; c < 2; ++c) {
-        const T ua = ue[0][c];
-        for (int k = 1; k < 6; ++k) ue[k][c] -= ua;
+        if constexpr (IsDD<T>::value) {  // operand packed as doubles: FP64 differences, then split
+          const double ua = dd_unpack_double(ue[0][c]);
+          for (int k = 1; k < 6; ++k) ue[k][c] = dd_from_double(dd_unpack_double(ue[k][c]) - ua);
+        } else {
+          const T ua = ue[0][c];
+          for (int k = 1; k < 6; ++k) ue[k][c] -= ua;
+        }
         ue[0][c] = T(0);
       }
-      if (P.rmass) {
+      if (IsDD<T>::value || P.rmass) {
         T M[6];
         for (int k = 0; k < 6; ++k) M[k] = L.M[O * 6 + k];
         tri_apply_m<O>(ue, M, P, y);
       } else {
-        tri_apply<O>(ue, xe, P, y);
+        if constexpr (!IsDD<T>::value) tri_apply<O>(ue, xe, P, y);
       }
     }
 #define TOPO_ST(K)                                             \
@@ -468,7 +501,15 @@ struct P2March {
     }
     const T* src = P.rmass + (unsigned(j) * unsigned(P.nx) + unsigned(i)) * 12u;
 #if defined(__CUDA_ARCH__)
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (IsDD<T>::value) {  // (hi, lo) pairs: two per 16-byte load
+      const float4* q = reinterpret_cast<const float4*>(src);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float4 t = q[k];
+        M[2 * k] = dd(t.x, t.y);
+        M[2 * k + 1] = dd(t.z, t.w);
+      }
+    } else if constexpr (sizeof(T) == 4) {
       const float4* q = reinterpret_cast<const float4*>(src);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -600,13 +641,23 @@ struct P2March {
     const T un[2] = {u[0], u[1]};
     T r[2] = {sum[0], sum[1]};
     if (cl) {
-      r[0] = un[0];
-      r[1] = un[1];
+      if constexpr (!IsDD<T>::value) {  // (dd: the operand is packed as doubles; Apply stores it)
+        r[0] = un[0];
+        r[1] = un[1];
+      }
     }
     const SmoothBufs<T>& B = io.B;
     const T c0 = io.cf[0], c1 = io.cf[1], c2 = io.cf[2];
     switch (io.mode) {
       case kP2Apply:
+        if constexpr (IsDD<T>::value) {
+          if (cl) {  // identity row: the operand's double itself
+            double* q = reinterpret_cast<double*>(io.y + i);
+            q[0] = dd_unpack_double(un[0]);
+            q[1] = dd_unpack_double(un[1]);
+            break;
+          }
+        }
         st2(io.y + i, r[0], r[1]);
         if (io.fuse == kFusePQ) {
           acc[0] += un[0] * r[0];
@@ -765,8 +816,9 @@ TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<
 // quadrature points: the r-weighted mass matrices of the operator (r as given)
 // and kappa_T of the P1 levels (r clamped at pmin, the preconditioner's
 // coefficient).  Same arithmetic, term by term, as cell_rmass and tri_kappa.
-template <class T>
-TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const Penal<T>& pen, T* rm, T* kK) {
+// RM: the mass matrices' storage type (T, or dd pairs for the pair-of-FP32 operator)
+template <class T, class RM = T>
+TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const Penal<T>& pen, RM* rm, T* kK) {
   const size_t c = size_t(j) * nx + i;
   const int VX = nx + 1;
   for (int o = 0; o < 2; ++o) {
@@ -790,7 +842,10 @@ TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const P
       M[5] += wr * (l1 * l2);
       kap += T(Rule7::w(q)) * (r >= pen.pmin ? r : pen.pmin);
     }
-    for (int k = 0; k < 6; ++k) rm[c * 12 + o * 6 + k] = M[k];
+    for (int k = 0; k < 6; ++k) {
+      if constexpr (IsDD<RM>::value) rm[c * 12 + o * 6 + k] = dd_from_double(M[k]);
+      else rm[c * 12 + o * 6 + k] = M[k];
+    }
     kK[c * 2 + o] = kap;
   }
 }
