@@ -133,7 +133,8 @@ TOPO_HD dd dd_from_double(double x) {
     if (r != 0) {
       // |r| < 2^29 in units of 2^(e - 1075); the float conversion keeps 24 bits, and the
       // scale goes into the exponent field (the result stays a normal float in this range)
-      const float f = float(sign ? -r : r);
+      const int ri = int(r);  // |r| <= 2^28: a 32-bit conversion
+      const float f = float(sign ? -ri : ri);
       lo = __uint_as_float(__float_as_uint(f) + (unsigned(e - 1075) << 23));
     }
     return dd(__uint_as_float(fb), lo);
