@@ -98,6 +98,31 @@ TOPO_HD dd operator*(dd a, dd b) {
   e = ddop::fma(a.lo, b.hi, e);
   return fast_two_sum(p, e);
 }
+// K x for a small integer constant K, written so that the float and double
+// operators keep their exact arithmetic (T(K) * x) and the pair type takes the
+// cheap exact forms: a power of two scales both parts, 3 is one TwoProd.
+template <int K, class T>
+TOPO_HD T mul_small(T x) {
+  if constexpr (IsDD<T>::value) {
+    if constexpr ((K & (K - 1)) == 0) {
+      return T(ddop::mul(x.hi, float(K)), ddop::mul(x.lo, float(K)));
+    } else {
+      const float p = ddop::mul(x.hi, float(K));
+      float e = ddop::fma(x.hi, float(K), -p);
+      e = ddop::fma(x.lo, float(K), e);
+      return fast_two_sum(p, e);
+    }
+  } else {
+    return T(K) * x;
+  }
+}
+// x / 2 (exact in every type)
+template <class T>
+TOPO_HD T half_of(T x) {
+  if constexpr (IsDD<T>::value) return T(ddop::mul(x.hi, 0.5f), ddop::mul(x.lo, 0.5f));
+  else return T(0.5) * x;
+}
+
 // a - b with both parts' sums made exact (the IEEE-style addition): the error is
 // bounded relative to the result, so the difference of two nearby values (the
 // difference form's u_k - u_A) keeps about 48 bits of the difference itself

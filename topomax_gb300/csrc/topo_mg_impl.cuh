@@ -143,10 +143,15 @@ __global__ void __launch_bounds__(P2M_THREADS, p2_march_min_blocks<T>())
   if (js < P.ny) {  // whole warp: warps past the last segment only join the reduction
     const int je = min(js + seg, P.ny);
     // warp-uniform: the same cell columns and rows for all lanes
-    if (P2March<T>::lean_region(P, int(blockIdx.x) * P2M_OWN - 1, js > 0 ? js - 1 : 0, je))
-      p2_march_run<T, MODE, true>(P, xi, io, lane, js, je, acc);
-    else
+    if constexpr (IsDD<T>::value) {
+      // pair-of-FP32: issue-bound on a long element body; one copy of it (the masked
+      // phases) keeps the code within reach of the instruction caches
       p2_march_run<T, MODE, false>(P, xi, io, lane, js, je, acc);
+    } else if (P2March<T>::lean_region(P, int(blockIdx.x) * P2M_OWN - 1, js > 0 ? js - 1 : 0, je)) {
+      p2_march_run<T, MODE, true>(P, xi, io, lane, js, je, acc);
+    } else {
+      p2_march_run<T, MODE, false>(P, xi, io, lane, js, je, acc);
+    }
   }
   if constexpr ((MODE == kP2Apply || MODE == kP2Post2) && !IsDD<T>::value) {
     if (io.fuse != kFuseNone) {

@@ -131,9 +131,9 @@ TOPO_HD void p2_vertex_grads(const TU (&u)[6][2], T ihx, T ihy, T (&G)[3][2][2])
 #endif
   for (int c = 0; c < 2; ++c) {
     // W[k][i]: coefficient of g_i in grad(u)(v_k), component c
-    const TU w00 = TU(3) * u[0][c], w01 = TU(4) * u[5][c] - u[1][c], w02 = TU(4) * u[4][c] - u[2][c];
-    const TU w10 = TU(4) * u[5][c] - u[0][c], w11 = TU(3) * u[1][c], w12 = TU(4) * u[3][c] - u[2][c];
-    const TU w20 = TU(4) * u[4][c] - u[0][c], w21 = TU(4) * u[3][c] - u[1][c], w22 = TU(3) * u[2][c];
+    const TU w00 = mul_small<3>(u[0][c]), w01 = mul_small<4>(u[5][c]) - u[1][c], w02 = mul_small<4>(u[4][c]) - u[2][c];
+    const TU w10 = mul_small<4>(u[5][c]) - u[0][c], w11 = mul_small<3>(u[1][c]), w12 = mul_small<4>(u[3][c]) - u[2][c];
+    const TU w20 = mul_small<4>(u[4][c]) - u[0][c], w21 = mul_small<4>(u[3][c]) - u[1][c], w22 = mul_small<3>(u[2][c]);
     if constexpr (O == 0) {
       G[0][c][0] = T(w01 - w00) * ihx; G[0][c][1] = T(w02 - w01) * ihy;
       G[1][c][0] = T(w11 - w10) * ihx; G[1][c][1] = T(w12 - w11) * ihy;
@@ -151,7 +151,7 @@ template <int O, class T>
 TOPO_HD void tri_apply_m(const T (&u)[6][2], const T (&M)[6], const P2Params<T>& P, T (&y)[6][2]) {
   T G[3][2][2];
   p2_vertex_grads<O>(u, P.ihx, P.ihy, G);
-  const T muT = T(0.5) * P.mu2T;
+  const T muT = half_of(P.mu2T);
   T sig[3][3];
 #if defined(__CUDA_ARCH__)
 #pragma unroll
@@ -176,9 +176,9 @@ TOPO_HD void tri_apply_m(const T (&u)[6][2], const T (&M)[6], const P2Params<T>&
   T Q[3][3];
   for (int c = 0; c < 3; ++c) {
     const T tot = S[0][c] + S[1][c] + S[2][c];
-    Q[0][c] = T(4) * S[0][c] - tot;
-    Q[1][c] = T(4) * S[1][c] - tot;
-    Q[2][c] = T(4) * S[2][c] - tot;
+    Q[0][c] = mul_small<4>(S[0][c]) - tot;
+    Q[1][c] = mul_small<4>(S[1][c]) - tot;
+    Q[2][c] = mul_small<4>(S[2][c]) - tot;
   }
   sg<O, 0>(Q[0], P.ihx, P.ihy, y[0][0], y[0][1]);
   sg<O, 1>(Q[1], P.ihx, P.ihy, y[1][0], y[1][1]);
@@ -187,13 +187,13 @@ TOPO_HD void tri_apply_m(const T (&u)[6][2], const T (&M)[6], const P2Params<T>&
   T ax, ay, bx, by;
   sg<O, 2>(S[1], P.ihx, P.ihy, ax, ay);
   sg<O, 1>(S[2], P.ihx, P.ihy, bx, by);
-  y[3][0] = T(4) * (ax + bx); y[3][1] = T(4) * (ay + by);
+  y[3][0] = mul_small<4>(ax + bx); y[3][1] = mul_small<4>(ay + by);
   sg<O, 2>(S[0], P.ihx, P.ihy, ax, ay);
   sg<O, 0>(S[2], P.ihx, P.ihy, bx, by);
-  y[4][0] = T(4) * (ax + bx); y[4][1] = T(4) * (ay + by);
+  y[4][0] = mul_small<4>(ax + bx); y[4][1] = mul_small<4>(ay + by);
   sg<O, 1>(S[0], P.ihx, P.ihy, ax, ay);
   sg<O, 0>(S[1], P.ihx, P.ihy, bx, by);
-  y[5][0] = T(4) * (ax + bx); y[5][1] = T(4) * (ay + by);
+  y[5][0] = mul_small<4>(ax + bx); y[5][1] = mul_small<4>(ay + by);
 }
 
 // y = K_T u for one triangle of orientation O.
