@@ -10,7 +10,6 @@
 
 #include <cuda_runtime.h>
 #include <cstring>
-#include <memory>
 #include <string>
 #include <mutex>
 #include <vector>
@@ -87,22 +86,12 @@ struct Reducer {
   void init(Arena& a, int sms);
 };
 
-// Grid-wide barrier of the persistent V-cycle kernels (cooperative launches):
-// arrivals at the current barrier, barriers completed, and a status that a wait
-// sets when it runs out (the launch's results are then invalid; the solve
-// reports a CUDA error and the status is cleared for the next one).
-struct GridBar {
-  unsigned count, gen;
-  int status, pad;
-};
-
 // Device-resident scalars of one preconditioned-CG solve (read back once at the end).
 struct PcgDev {
   double bb, rz, pq, beta, tol2, relres;
   double rr, rz_new;  // adjacent: one two-value reduction writes both
   double alpha;       // the iteration's step as applied to r (rounded to the CG's precision; 0 on breakdown)
   int it, maxit, status, pad;  // status: 0 converged, 1 running, 2 iteration cap, 3 breakdown, 4 non-finite, 5 zero rhs
-  GridBar bar;        // the hierarchy's persistent V-cycle kernels
 };
 
 struct SolveStats {
@@ -146,10 +135,7 @@ class MG {
   // chosen from the coefficients at the first setup() (a filter's never
   // change); a caller whose scalar coefficients change between setups calls
   // this first so that the next setup() chooses them again.
-  void coefficients_changed() {
-    cc_selected_ = false;
-    pers_built_ = false;
-  }
+  void coefficients_changed() { cc_selected_ = false; }
   // y = A_l x; on level 0, op selects the Krylov operator instead of the
   // preconditioner's (they differ only where the penalisation is clamped)
   void apply(int l, const T* x, T* y, cudaStream_t s, bool op = false);
@@ -193,12 +179,6 @@ class MG {
   int coarse_cheb_level() const { return cheb_coarse_; }
   int coarse_cheb_deg = 0;
   bool use_p1_march = true;  // large P1 levels: column march (false: node-centric kernels)
-  // run the V-cycle's consecutive stencil levels above the coarse solve in two
-  // cooperative launches (down: pre-smoothing, residual, restriction per level;
-  // up: prolongation, post-smoothing), the phases separated by grid barriers,
-  // instead of six launches per level (TOPO_PERSIST=0: per-level launches)
-  bool use_persistent = true;
-  int persistent_levels() const { return pers_desc_ ? pers_last_ - pers_first_ : 0; }
   long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;
@@ -284,19 +264,6 @@ class MG {
   bool fuse_rz_ = false;
   unsigned long long fuse_cond_ = 0;
   int fuse_use_cond_ = 0;
-
-  // persistent V-cycle: levels [pers_first_, pers_last_) in PersistDesc<T, NC> (device);
-  // pers_last_ is the coarse solve's level (tail, coarse Chebyshev or dense inverse)
-  int pers_first_ = -1, pers_last_ = -1, pers_blocks_ = 0, pers_threads_ = 0;
-  bool pers_tail_ = false;  // the coarse solve is the tail kernel (use_tail at build time)
-  void* pers_desc_ = nullptr;
-  struct CudaFree {
-    void operator()(void* p) const { cudaFree(p); }
-  };
-  std::unique_ptr<void, CudaFree> pers_owned_;  // the descriptor's allocation
-  bool pers_built_ = false;
-  void build_persistent();
-  bool run_persistent(const T* b, T* x, cudaStream_t s);  // false: not taken (per-level path)
 
   T* pcg_[kScratch] = {};
   double* xacc_ = nullptr;  // FP64 solution of the CG loop (fp64_solution)

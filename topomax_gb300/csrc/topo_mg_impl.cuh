@@ -821,125 +821,6 @@ static inline Transfer make_transfer(const LevelSpec& f, const LevelSpec& c) {
 }
 
 // ---------------------------------------------------------------------------
-// persistent V-cycle over consecutive stencil levels
-// ---------------------------------------------------------------------------
-// The levels between the large ones and the coarse solve are launch-latency
-// bound: six launches per level and V-cycle, each a few microseconds of launch
-// and ramp for little data.  Two cooperative launches run them instead, one
-// block per SM, every phase a grid-stride loop over the level's nodes with the
-// same node functions as the per-level kernels, the phases separated by grid
-// barriers: down (per level: pre-smoothing, residual, restriction) and up (per
-// level, coarse to fine: prolongation, the two post-smoothing steps).  The
-// coarse solve between them is its own launch.
-constexpr int kPersistMaxLevels = 8;
-constexpr int kPersistThreads = 512;
-// a barrier wait gives up after this many polls (~100 ns each): the launch then
-// records the failure in GridBar::status and its remaining barriers return at once
-constexpr unsigned kBarSpinLimit = 1u << 20;
-
-template <class T, int NC>
-struct PersistLevel {
-  P1Stencil<T, NC> P;
-  SmoothBufs<T> B;  // the first level's b and x come from the launch
-  Transfer X;       // to the next level
-  T* cb;            // next level's right-hand side (restriction output)
-  T* cx;            // next level's solution (prolongation input)
-  int nn, nnc;      // nodes of this level and of the next
-};
-
-template <class T, int NC>
-struct PersistDesc {
-  int nlev;
-  PersistLevel<T, NC> lv[kPersistMaxLevels];
-};
-
-// Grid-wide barrier of a cooperative launch (every block resident): the
-// block's writes are released before it arrives and the others' acquired after
-// the last arrival moves the generation.  Bounded: a wait that runs out sets
-// the status, and once the status is set no barrier waits any more.
-__device__ __forceinline__ void grid_barrier(GridBar* g) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile GridBar* vg = g;
-    if (vg->status == 0) {
-      const unsigned gen = vg->gen;  // read before arriving: it cannot move until this block arrives
-      __threadfence();
-      if (atomicAdd(&g->count, 1u) == gridDim.x - 1) {
-        vg->count = 0u;  // every other block is waiting on gen: none touches count now
-        __threadfence();
-        atomicAdd(&g->gen, 1u);
-      } else {
-        unsigned spins = 0;
-        while (vg->gen == gen) {
-          if (vg->status != 0) break;
-          if (++spins > kBarSpinLimit) {
-            atomicExch(&g->status, 1);
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
-      __threadfence();
-    }
-  }
-  __syncthreads();
-}
-
-template <class T, int NC>
-__global__ void __launch_bounds__(kPersistThreads)
-    k_vcycle_down(const PersistDesc<T, NC>* __restrict__ D, const T* b0, T* x0, PcgDev* dv) {
-  GridBar* g = &dv->bar;
-  const int nlev = D->nlev;
-  const int tid = int(blockIdx.x * blockDim.x + threadIdx.x), stride = int(gridDim.x * blockDim.x);
-  for (int l = 0; l < nlev; ++l) {
-    const PersistLevel<T, NC>& L = D->lv[l];
-    SmoothBufs<T> B = L.B;
-    if (l == 0) {
-      B.b = b0;
-      B.x = x0;
-    }
-    // the stencil and transfer descriptions are read in place (they hold the
-    // Dirichlet lists: a private copy per thread would live in local memory)
-    const P1Stencil<T, NC>& P = L.P;
-    const int NX = P.nx + 1, nn = L.nn;
-    for (int n = tid; n < nn; n += stride) P1Smooth<T, NC>::pre(n % NX, n / NX, P, B);
-    grid_barrier(g);
-    for (int n = tid; n < nn; n += stride) P1Smooth<T, NC>::res(n % NX, n / NX, P, B);
-    grid_barrier(g);
-    const Transfer& X = L.X;
-    for (int n = tid; n < L.nnc; n += stride)
-      TransferKern<T, NC>::node_restrict(n % X.NXc, n / X.NXc, X, B.r, L.cb, static_cast<const T*>(nullptr));
-    if (l + 1 < nlev) grid_barrier(g);  // (the last restriction feeds the next launch)
-  }
-}
-
-template <class T, int NC>
-__global__ void __launch_bounds__(kPersistThreads)
-    k_vcycle_up(const PersistDesc<T, NC>* __restrict__ D, const T* b0, T* x0, PcgDev* dv) {
-  GridBar* g = &dv->bar;
-  const int nlev = D->nlev;
-  const int tid = int(blockIdx.x * blockDim.x + threadIdx.x), stride = int(gridDim.x * blockDim.x);
-  for (int l = nlev - 1; l >= 0; --l) {
-    const PersistLevel<T, NC>& L = D->lv[l];
-    SmoothBufs<T> B = L.B;
-    if (l == 0) {
-      B.b = b0;
-      B.x = x0;
-    }
-    const P1Stencil<T, NC>& P = L.P;
-    const Transfer& X = L.X;
-    const int NX = P.nx + 1, nn = L.nn;
-    for (int n = tid; n < nn; n += stride)
-      TransferKern<T, NC>::node_prolong_add(n % X.NXf, n / X.NXf, X, static_cast<const T*>(L.cx), B.x);
-    grid_barrier(g);
-    for (int n = tid; n < nn; n += stride) P1Smooth<T, NC>::first(n % NX, n / NX, P, B);
-    grid_barrier(g);
-    for (int n = tid; n < nn; n += stride) P1Smooth<T, NC>::post2(n % NX, n / NX, P, B);
-    if (l > 0) grid_barrier(g);  // the finer level's prolongation reads this x
-  }
-}
-
-// ---------------------------------------------------------------------------
 // graph-resident CG scalars
 // ---------------------------------------------------------------------------
 // x += alpha p ; r -= alpha q with alpha = rz / pq read from device memory
@@ -1460,122 +1341,7 @@ int MG<T>::setup(cudaStream_t s) {
   if (e != cudaSuccess) return -5;
   if (st) return -2;
   tune_marches(s);
-  if (!pers_built_) {
-    build_persistent();
-    graph_valid_ = false;  // the V-cycle's launches change with it
-  }
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -5;
-}
-
-// Chooses the persistent V-cycle's levels (the stencil levels directly above
-// the coarse solve, at least two) and writes their descriptor.  Called at the
-// end of the first set-up, when the stencils, the coarse solve and the shared
-// interior rows are known; the pointers it records stay fixed afterwards.
-template <class T>
-void MG<T>::build_persistent() {
-  std::lock_guard<std::recursive_mutex> lock(device_lock());  // allocates and copies
-  pers_built_ = true;
-  pers_first_ = pers_last_ = -1;
-  pers_desc_ = nullptr;
-  if (!use_persistent) return;
-  const int L = levels();
-  int coarse = L - 1;
-  pers_tail_ = false;
-  if (cheb_coarse_ >= 0) {
-    coarse = cheb_coarse_;
-  } else if (tail_ >= 0 && use_tail && tail_desc_) {
-    coarse = tail_;
-    pers_tail_ = true;
-  }
-  int first = coarse;
-  while (first > 0 && !specs_[first - 1].p2 && lv_[first - 1].st && specs_[first - 1].NC == specs_[coarse].NC)
-    --first;
-  if (coarse - first > kPersistMaxLevels) first = coarse - kPersistMaxLevels;
-  if (coarse - first < 2) return;
-  auto build = [&](auto nc_tag) {
-    constexpr int NC = decltype(nc_tag)::value;
-    int nb = 0, nb2 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_vcycle_down<T, NC>, kPersistThreads, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_vcycle_up<T, NC>, kPersistThreads, 0) != cudaSuccess ||
-        nb < 1 || nb2 < 1) {
-      cudaGetLastError();
-      return;
-    }
-    PersistDesc<T, NC> h;
-    std::memset(&h, 0, sizeof(h));
-    h.nlev = coarse - first;
-    for (int k = 0; k < h.nlev; ++k) {
-      const int l = first + k;
-      const LevelSpec& S = specs_[l];
-      Lev& v = lv_[l];
-      PersistLevel<T, NC>& q = h.lv[k];
-      q.P = P1Stencil<T, NC>{S.nx, S.ny, S.dir, v.st, v.inner};
-      q.B = SmoothBufs<T>{v.b, v.dinv, v.x, v.x2, v.r, v.d, cheb_ + 8 * l};
-      q.X = make_transfer(S, specs_[l + 1]);
-      q.cb = lv_[l + 1].b;
-      q.cx = lv_[l + 1].x;
-      q.nn = S.NX * S.NY;
-      q.nnc = q.X.NXc * q.X.NYc;
-    }
-    void* p = nullptr;
-    if (cudaMalloc(&p, sizeof(h)) != cudaSuccess) {
-      cudaGetLastError();
-      return;
-    }
-    pers_owned_.reset(p);
-    cudaMemcpy(p, &h, sizeof(h), cudaMemcpyHostToDevice);
-    cudaMemset(&dev_->bar, 0, sizeof(GridBar));
-    pers_desc_ = p;
-    pers_first_ = first;
-    pers_last_ = coarse;
-    pers_blocks_ = sms_;
-    pers_threads_ = kPersistThreads;
-  };
-  if (specs_[coarse].NC == 2) build(std::integral_constant<int, 2>{});
-  else build(std::integral_constant<int, 1>{});
-}
-
-// One V-cycle from level pers_first_ down (see k_vcycle_down / k_vcycle_up);
-// false when the persistent path is not available for this call.
-template <class T>
-bool MG<T>::run_persistent(const T* b, T* x, cudaStream_t s) {
-  if (!use_persistent || !pers_desc_ || (pers_tail_ && !use_tail)) return false;
-  const int NC = specs_[pers_first_].NC;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(pers_blocks_);
-  cfg.blockDim = dim3(pers_threads_);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaError_t e;
-  {
-    KClock kc(s, "persistent V-cycle, down", pers_first_, 0.0);
-    if (NC == 2)
-      e = cudaLaunchKernelEx(&cfg, k_vcycle_down<T, 2>, static_cast<const PersistDesc<T, 2>*>(pers_desc_), b, x, dev_);
-    else
-      e = cudaLaunchKernelEx(&cfg, k_vcycle_down<T, 1>, static_cast<const PersistDesc<T, 1>*>(pers_desc_), b, x, dev_);
-  }
-  if (e != cudaSuccess) {  // nothing was launched: this and later V-cycles take the per-level path
-    cudaGetLastError();
-    use_persistent = false;
-    return false;
-  }
-  ++launches;
-  vcycle_level(pers_last_, lv_[pers_last_].b, lv_[pers_last_].x, s);
-  {
-    KClock kc(s, "persistent V-cycle, up", pers_first_, 0.0);
-    if (NC == 2)
-      cudaLaunchKernelEx(&cfg, k_vcycle_up<T, 2>, static_cast<const PersistDesc<T, 2>*>(pers_desc_),
-                         static_cast<const T*>(b), x, dev_);
-    else
-      cudaLaunchKernelEx(&cfg, k_vcycle_up<T, 1>, static_cast<const PersistDesc<T, 1>*>(pers_desc_),
-                         static_cast<const T*>(b), x, dev_);
-  }
-  ++launches;
-  return true;
 }
 
 // One V-cycle from level l down: fused degree-2 Chebyshev pre-smoothing from
@@ -1650,7 +1416,6 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     ++launches;
     return;
   }
-  if (l == pers_first_ && run_persistent(b, x, s)) return;
   SmoothBufs<T> B{b, v.dinv, x, v.x2, v.r, v.d, cheb_ + 8 * l};
   const Transfer X = make_transfer(S, specs_[l + 1]);
   Lev& c = lv_[l + 1];
@@ -2096,15 +1861,6 @@ int MG<T>::graph_pcg(const T* b, T* x, double* x64, bool warm, double rtol, int 
   else cudaMemcpyAsync(x, xi, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(hdev_, dev_, sizeof(PcgDev), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) return -5;
-  if (hdev_->bar.status != 0) {
-    // a persistent V-cycle's barrier wait ran out: this solve's result is invalid;
-    // the hierarchy continues with per-level launches
-    cudaMemsetAsync(&dev_->bar, 0, sizeof(GridBar), s);
-    cudaStreamSynchronize(s);
-    use_persistent = false;
-    graph_valid_ = false;
-    return -5;
-  }
   st.iterations = hdev_->it;
   st.relres = hdev_->relres;
   if (graphs) launches += (long long)hdev_->it * G.body_nodes;
