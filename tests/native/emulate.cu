@@ -227,11 +227,17 @@ int emu_p2_apply(int prec, int nx, int ny, double hx, double hy, double lam, dou
     // pair-of-FP32 operator (Apply only): mass matrices precomputed in FP64 and split
     if (mode != 0 || !u) return -1;
     auto P = p2params<dd>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
+    // the library's set-up: pair-of-FP32 quadrature for an integer exponent, else FP64 split
     const Penal<double> pen = make_penal<double>(p, pmin, 0);
     std::vector<dd> rm(size_t(12) * nx * ny);
     std::vector<double> kK(size_t(2) * nx * ny);
     for (int j = 0; j < ny; ++j)
-      for (int i = 0; i < nx; ++i) cell_rmass_kappa<double, dd>(i, j, nx, ny, xi, pen, rm.data(), kK.data());
+      for (int i = 0; i < nx; ++i) {
+        if (pen.ip >= 1 && pen.ip <= 16)
+          cell_rmass_kappa_dd(i, j, nx, xi, pen.ip, dd(pmin), dd(1.0 - pmin), rm.data(), kK.data());
+        else
+          cell_rmass_kappa<double, dd>(i, j, nx, ny, xi, pen, rm.data(), kK.data());
+      }
     P.rmass = rm.data();
     p2_run<dd>(P, nullptr, reinterpret_cast<const dd*>(u), reinterpret_cast<dd*>(y), 0);
   } else {

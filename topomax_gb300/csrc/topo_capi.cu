@@ -76,6 +76,15 @@ __global__ void k_cell_rmass_kappa(int nx, int ny, Penal<double> pen, const doub
   TOPO_GRID_STRIDE(c, nc) cell_rmass_kappa<double, RM>(int(c % nx), int(c / nx), nx, ny, xi, pen, rm, kK);
 }
 
+// The same one pass in pair-of-FP32 arithmetic (cell_rmass_kappa_dd) for an
+// integer penalisation exponent: mass matrices as (hi, lo) pairs, kappa in FP64
+__global__ void k_cell_rmass_kappa_dd(int nx, int ny, int ip, dd pmin, dd one_m_pmin,
+                                      const double* __restrict__ xi, dd* __restrict__ rm,
+                                      double* __restrict__ kK) {
+  const size_t nc = size_t(nx) * ny;
+  TOPO_GRID_STRIDE(c, nc) cell_rmass_kappa_dd(int(c % nx), int(c / nx), nx, xi, ip, pmin, one_m_pmin, rm, kK);
+}
+
 __global__ void k_coarsen_kappa(const double* __restrict__ kf, int nxf, int nyf, double* __restrict__ kc,
                                 int nxc, int nyc) {
   const size_t nt = size_t(2) * nxc * nyc;
@@ -691,7 +700,11 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
   Penal<double> pen = make_penal<double>(C->p, C->pmin, 1);
   const size_t ncell = size_t(C->nx) * C->ny;
   const Penal<double> pen_op = make_penal<double>(C->p, C->pmin, 0);
-  if (C->op_dd)
+  if (C->op_dd && pen_op.ip >= 1 && pen_op.ip <= 16)
+    k_cell_rmass_kappa_dd<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op.ip, dd(C->pmin),
+                                                                 dd(1.0 - C->pmin), xi,
+                                                                 reinterpret_cast<dd*>(C->rm_op64), C->skK[1]);
+  else if (C->op_dd)
     k_cell_rmass_kappa<dd><<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, pen_op, xi,
                                                                   reinterpret_cast<dd*>(C->rm_op64), C->skK[1]);
   else

@@ -170,6 +170,26 @@ TOPO_HD dd dd_from_double(double x) {
   return dd(h, float(x - double(h)));
 }
 
+// A double rounded to the nearest float (ties to even), on the integer pipe on the
+// GPU for results in the normal float range and zero; the rest through a conversion.
+TOPO_HD float float_from_double(double x) {
+#if defined(__CUDA_ARCH__)
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned top = unsigned(b >> 32);
+  const int e = int((top >> 20) & 0x7ffu);
+  const unsigned sign = top & 0x80000000u;
+  if (e >= 897 && e < 1151) {
+    const unsigned long long m = b & 0xfffffffffffffull;
+    unsigned fb = sign | (unsigned(e - 896) << 23) | unsigned(m >> 29);
+    const unsigned r = unsigned(m & 0x1fffffffull);
+    if (r > 0x10000000u || (r == 0x10000000u && (fb & 1u))) fb += 1u;  // a carry moves the exponent
+    return __uint_as_float(fb);
+  }
+  if (e == 0) return __uint_as_float(sign);
+#endif
+  return float(x);
+}
+
 // Exact float -> double on the integer pipe for normal floats and zero.
 TOPO_HD double dd_widen(float f) {
 #if defined(__CUDA_ARCH__)

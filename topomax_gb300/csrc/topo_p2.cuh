@@ -850,6 +850,46 @@ TOPO_HD void cell_rmass_kappa(int i, int j, int nx, int ny, const T* xi, const P
   }
 }
 
+// cell_rmass_kappa in pair-of-FP32 arithmetic (FP32 pipe; FP64 arithmetic is scarce
+// on this GPU) for an integer penalisation exponent ip (1..16), r = pmin + xi^p
+// (1 - pmin): the same 7-point quadrature, with the constants' products formed in
+// FP64 at compile time.  Mass matrices as (hi, lo) pairs, kappa rounded to FP64.
+TOPO_HD bool dd_ge(dd a, dd b) { return a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo); }
+
+TOPO_HD void cell_rmass_kappa_dd(int i, int j, int nx, const double* xi, int ip, dd pmin, dd one_m_pmin, dd* rm,
+                                 double* kK) {
+  const size_t c = size_t(j) * nx + i;
+  const int VX = nx + 1;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int o = 0; o < 2; ++o) {
+    dd xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = dd_from_double(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
+    dd M[6] = {dd(0), dd(0), dd(0), dd(0), dd(0), dd(0)};
+    dd kap = dd(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int q = 0; q < Rule7::n; ++q) {
+      const double l0 = Rule7::lam(q, 0), l1 = Rule7::lam(q, 1), l2 = Rule7::lam(q, 2), w = Rule7::w(q);
+      const dd x = dd(l0) * xe[0] + dd(l1) * xe[1] + dd(l2) * xe[2];
+      dd xp = x;
+      for (int k = 1; k < ip; ++k) xp = xp * x;
+      const dd r = pmin + xp * one_m_pmin;
+      M[0] += r * dd(w * l0 * l0);
+      M[1] += r * dd(w * l1 * l1);
+      M[2] += r * dd(w * l2 * l2);
+      M[3] += r * dd(w * l0 * l1);
+      M[4] += r * dd(w * l0 * l2);
+      M[5] += r * dd(w * l1 * l2);
+      kap += dd(w) * (dd_ge(r, pmin) ? r : pmin);
+    }
+    for (int k = 0; k < 6; ++k) rm[c * 12 + o * 6 + k] = M[k];
+    kK[c * 2 + o] = dd_to_double(kap);
+  }
+}
+
 // kappa_T = (1/|T|) int_T r(xi) with the 7-point rule: the Galerkin P1
 // coefficient of the P2 operator (P1 strains are constant per triangle).
 template <class T>

@@ -50,7 +50,11 @@ __global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu
 #pragma unroll
     for (int r = 0; r < 2; ++r)
 #pragma unroll
-      for (int c = 0; c < 2; ++c) xv[r][c] = TQ(xi[size_t(j + r) * VX + i + c]);
+      for (int c = 0; c < 2; ++c) {
+        const double x = xi[size_t(j + r) * VX + i + c];
+        if constexpr (sizeof(TQ) == 4) xv[r][c] = float_from_double(x);  // (integer pipe)
+        else xv[r][c] = TQ(x);
+      }
     TQ c0[3], c1[3];
     if constexpr (sizeof(TQ) == 4) {
       // difference form: the gradient ignores a translation, so the node values enter as
@@ -63,7 +67,7 @@ __global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
-          for (int d = 0; d < 2; ++d) ud[r][c][d] = (r | c) ? TQ(un[r][c][d] - un[0][0][d]) : TQ(0);
+          for (int d = 0; d < 2; ++d) ud[r][c][d] = (r | c) ? float_from_double(un[r][c][d] - un[0][0][d]) : TQ(0);
       sens_cell_tri<0>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c0);
       sens_cell_tri<1>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c1);
     } else {
