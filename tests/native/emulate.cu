@@ -455,10 +455,14 @@ int emu_sensitivity(int prec, int nx, int ny, double hx, double hy, double lam, 
       float xe[3], c[3];
       for (int k = 0; k < 3; ++k) xe[k] = float(xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)]);
       const auto pen = make_penal<float>(p, pmin);
-      // the kernel's difference form: u - u_A in FP64, gradients and quadrature in FP32
+      // the kernel's difference form: u - u_A from the values' (hi, lo) splits in FP32,
+      // gradients and quadrature in FP32
       float ud[6][2];
       for (int k = 0; k < 6; ++k)
-        for (int d = 0; d < 2; ++d) ud[k][d] = k == 0 ? 0.0f : float(ue[k][d] - ue[0][d]);
+        for (int d = 0; d < 2; ++d) {
+          const dd a = dd_from_double(ue[k][d]), b = dd_from_double(ue[0][d]);
+          ud[k][d] = k == 0 ? 0.0f : (a.hi - b.hi) + (a.lo - b.lo);
+        }
       if (o == 0)
         tri_sensitivity<0, float, float>(ud, xe, float(1.0 / hx), float(1.0 / hy), float(lam), float(mu), float(area),
                                          pen, c);

@@ -58,16 +58,28 @@ __global__ void k_sens_tri(int nx, int ny, double ihx, double ihy, TQ lam, TQ mu
     TQ c0[3], c1[3];
     if constexpr (sizeof(TQ) == 4) {
       // difference form: the gradient ignores a translation, so the node values enter as
-      // u - u_A (vertex A = node (0,0) of both triangles), subtracted in FP64 (exact for a
-      // smooth field) and rounded to FP32, where the gradients and the quadrature run (FP64
-      // arithmetic is scarce on this GPU)
+      // u - u_A (vertex A = node (0,0) of both triangles), rounded to FP32, where the
+      // gradients and the quadrature run.  The difference is taken on the FP32 pipe from
+      // the values' (hi, lo) splits (FP64 arithmetic is scarce on this GPU): hi - hi is
+      // exact for nearby values, and lo - lo carries the rest, so the float result is
+      // within a rounding or two of the FP64 difference rounded to FP32.
+      dd us[3][3][2];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 2; ++d) us[r][c][d] = dd_from_double(un[r][c][d]);
       TQ ud[3][3][2];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
-          for (int d = 0; d < 2; ++d) ud[r][c][d] = (r | c) ? float_from_double(un[r][c][d] - un[0][0][d]) : TQ(0);
+          for (int d = 0; d < 2; ++d)
+            ud[r][c][d] = (r | c) ? ddop::add(ddop::sub(us[r][c][d].hi, us[0][0][d].hi),
+                                              ddop::sub(us[r][c][d].lo, us[0][0][d].lo))
+                                  : TQ(0);
       sens_cell_tri<0>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c0);
       sens_cell_tri<1>(ud, xv, TQ(ihx), TQ(ihy), lam, mu, area, pen, c1);
     } else {
