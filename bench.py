@@ -22,10 +22,12 @@ state solve + compliance).
 * ``e2e``: the same steps (same warm-up, same step sizes) through the
   reference-facing API with host (pinned) arrays, as the reference's
   Solver.step/project/set_from_array drive it.
+* ``kernels``: time and HBM GB/s per kernel family on the headline grid (the
+  library's kernel clock over host-driven design iterations; ``sum_ms_per_step``
+  against ``ms_per_step`` shows what launches and host round trips add).
 * ``c2_2000x1000``: the same loop on the 2000x1000 grid of the throughput
-  configuration (16,012,002 dofs), with its operator's bandwidth; ``kernels``:
-  HBM GB/s per kernel family there (the library's kernel clock over host-driven
-  design iterations).
+  configuration (16,012,002 dofs), with its operator's bandwidth, and the same
+  per-family table there (``kernels``).
 * ``c4_batch``: the 64-design ragged batch (domain 2x1, N in {100..300}), run one
   design after another and by concurrent workers; ``march_tiles``: the tiles the
   march-kernel autotuner chose in this run.
@@ -453,7 +455,16 @@ def main():
         torch.cuda.empty_cache()
         if args.kernel_steps > 0 and world == 1:
             c2["kernels"] = kernel_table(tg, mesh2, V2, dom, par, rho02, device_loop, args, measured_peak()[0])
+            c2["kernels"]["sum_ms_per_step"] = sum(r["ms_per_step"] for r in c2["kernels"]["families"])
             torch.cuda.empty_cache()
+
+    # --- the same per-family table on the headline grid; its sum against the recorded
+    # step shows what the host-driven launches and round trips add
+    kernels = None
+    if args.kernel_steps > 0 and world == 1:
+        kernels = kernel_table(tg, mesh, V, dom, par, rho0, device_loop, args, measured_peak()[0])
+        kernels["sum_ms_per_step"] = sum(r["ms_per_step"] for r in kernels["families"])
+        torch.cuda.empty_cache()
 
     # --- the fluid problem: its GPU design loop beside the fluid oracle on the host
     fluid = fluid_leg(args) if args.fluid_n > 0 and world == 1 else None
@@ -517,6 +528,7 @@ def main():
         "cpu_baseline": cpu,
         "same_grid": same_grid,
         "gpu_launches": int(nlaunch),
+        "kernels": kernels,
         "c2_2000x1000": c2,
         "c4_batch": c4,
         "march_tiles": march_tiles(),
