@@ -393,12 +393,26 @@ struct TailDesc {
   TailLevel<T, NC> lv[kTailMaxLevels];
 };
 
+// Copies n values global -> shared with 16-byte accesses (both addresses 16-byte
+// aligned), the remainder one by one: the tail's per-launch staging issues a few
+// wide loads per thread instead of a long chain of scalar ones.
+template <class T>
+__device__ __forceinline__ void stage16(T* __restrict__ dst, const T* __restrict__ src, int n, int tid, int nt) {
+  constexpr int V = 16 / sizeof(T);
+  const int nv = n / V;
+  const float4* s4 = reinterpret_cast<const float4*>(src);
+  float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll 4
+  for (int i = tid; i < nv; i += nt) d4[i] = s4[i];
+  for (int i = nv * V + tid; i < n; i += nt) dst[i] = src[i];
+}
+
 template <class T, int NC>
 __global__ void __launch_bounds__(kTailThreads)
     k_tail_vcycle(const TailDesc<T, NC>* __restrict__ D, const T* __restrict__ b_in, T* __restrict__ x_out) {
   TOPO_PDL_ENTRY();
   __shared__ TailLevel<T, NC> lv[kTailMaxLevels];
-  __shared__ T cinv[kCoarseMaxDofs * kCoarseMaxDofs];
+  __shared__ __align__(16) T cinv[kCoarseMaxDofs * kCoarseMaxDofs];
   extern __shared__ __align__(16) unsigned char tail_raw[];
   T* sm = reinterpret_cast<T*>(tail_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -410,17 +424,17 @@ __global__ void __launch_bounds__(kTailThreads)
     for (int i = tid; i < words; i += nt) dst[i] = src[i];
   }
   __syncthreads();
+  // (stencil and diagonal offsets are multiples of 16 bytes, every source a separate allocation)
   for (int l = 0; l < nlev; ++l) {
     const TailLevel<T, NC>& L = lv[l];
-    const int ns = StencilLayout<NC>::stride * L.nn;
-    for (int i = tid; i < ns; i += nt) sm[L.soff + i] = L.S.s[i];
-    for (int i = tid; i < NC * L.nn; i += nt) sm[L.doff + i] = L.dinv[i];
+    stage16(sm + L.soff, L.S.s, StencilLayout<NC>::stride * L.nn, tid, nt);
+    stage16(sm + L.doff, L.dinv, NC * L.nn, tid, nt);
   }
   {
     const int mc = NC * lv[nlev - 1].nn;
-    for (int i = tid; i < mc * mc; i += nt) cinv[i] = D->cinv[i];
+    stage16(cinv, D->cinv, mc * mc, tid, nt);
     const int m = NC * lv[0].nn;
-    T* b0 = sm + lv[0].off + m;
+    T* b0 = sm + lv[0].off + m;  // (inside the level's five vectors: not 16-byte aligned)
     for (int i = tid; i < m; i += nt) b0[i] = b_in[i];
   }
   __syncthreads();
@@ -1083,6 +1097,8 @@ void MG<T>::build_tail(Arena& arena) {
     h.nlev = L - first;
     h.cinv = cinv_;
     int off = 0;
+    constexpr int kAlign = 16 / int(sizeof(T));  // shared offsets in 16-byte units (stage16)
+    auto align = [&](int o) { return (o + kAlign - 1) / kAlign * kAlign; };
     for (int k = 0; k < h.nlev; ++k) {
       const int l = first + k;
       TailLevel<T, NC>& d = h.lv[k];
@@ -1097,9 +1113,9 @@ void MG<T>::build_tail(Arena& arena) {
     }
     for (int k = 0; k < h.nlev; ++k) {
       TailLevel<T, NC>& d = h.lv[k];
-      d.soff = off;
+      d.soff = off = align(off);
       off += StencilLayout<NC>::stride * d.nn;
-      d.doff = off;
+      d.doff = off = align(off);
       off += NC * d.nn;
     }
     h.smem_elems = off;
