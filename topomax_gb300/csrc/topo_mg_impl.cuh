@@ -373,7 +373,6 @@ __global__ void k_dense_matvec(const T* __restrict__ Ainv, const T* __restrict__
 constexpr int kTailThreads = 1024;
 constexpr int kTailMaxLevels = 10;
 constexpr size_t kTailSmemBudget = 196 * 1024;
-constexpr int kTailMaxNodes = 4096;  // largest level the one-CTA tail takes
 constexpr int kTailTraceSlots = 64;  // [0, 62]: SM cycles per phase, [63]: launches
 
 template <class T, int NC>
@@ -383,7 +382,7 @@ struct TailLevel {
   const T* dinv;
   const T* cheb;
   int NX, nn, off;  // off: first of this level's five shared vectors x, b, r, d, x2 (NC*nn each)
-  int soff, doff;   // shared copies of the stencil (stride*nn; -1: read in global memory) and of dinv (NC*nn)
+  int soff, doff;   // shared copies of the stencil (stride*nn) and of dinv (NC*nn)
 };
 
 template <class T, int NC>
@@ -428,7 +427,7 @@ __global__ void __launch_bounds__(kTailThreads)
   // (stencil and diagonal offsets are multiples of 16 bytes, every source a separate allocation)
   for (int l = 0; l < nlev; ++l) {
     const TailLevel<T, NC>& L = lv[l];
-    if (L.soff >= 0) stage16(sm + L.soff, L.S.s, StencilLayout<NC>::stride * L.nn, tid, nt);
+    stage16(sm + L.soff, L.S.s, StencilLayout<NC>::stride * L.nn, tid, nt);
     stage16(sm + L.doff, L.dinv, NC * L.nn, tid, nt);
   }
   {
@@ -441,7 +440,7 @@ __global__ void __launch_bounds__(kTailThreads)
   __syncthreads();
   if (tid == 0)
     for (int l = 0; l < nlev; ++l) {
-      if (lv[l].soff >= 0) lv[l].S.s = sm + lv[l].soff;
+      lv[l].S.s = sm + lv[l].soff;
       lv[l].dinv = sm + lv[l].doff;
     }
   __syncthreads();
@@ -1081,29 +1080,16 @@ void MG<T>::build_tail(Arena& arena) {
   tail_smem_ = 0;
   const int L = levels();
   const int stride = specs_[L - 1].NC == 2 ? StencilLayout<2>::stride : StencilLayout<1>::stride;
-  // The levels, from the coarsest up, whose five vectors and inverse diagonal fit the
-  // shared-memory budget (at most kTailMaxNodes nodes each: larger levels are served
-  // better by the whole GPU).  Their stencils are staged too, coarsest first, while
-  // there is room; a level whose stencil does not fit reads it from global memory
-  // (it stays L2-resident), which still saves its six launches per V-cycle.
   size_t bytes = 0;
   int first = L;
   for (int l = L - 1; l >= 1; --l) {
-    const size_t add = 6 * specs_[l].ndof() * sizeof(T) + 16;  // (+ 16-byte alignment of the diagonal)
-    if (specs_[l].p2 || !lv_[l].st || bytes + add > kTailSmemBudget || L - l > kTailMaxLevels ||
-        specs_[l].nn() > size_t(kTailMaxNodes))
-      break;
+    // five vectors, the inverse diagonal and the stencil
+    const size_t add = (6 * specs_[l].ndof() + size_t(stride) * specs_[l].nn()) * sizeof(T);
+    if (specs_[l].p2 || !lv_[l].st || bytes + add > kTailSmemBudget || L - l > kTailMaxLevels) break;
     bytes += add;
     first = l;
   }
   if (first >= L - 1) return;  // fewer than two levels: nothing to gain
-  std::vector<char> staged(L, 0);
-  for (int l = L - 1; l >= first; --l) {
-    const size_t add = size_t(stride) * specs_[l].nn() * sizeof(T) + 16;
-    if (bytes + add > kTailSmemBudget) break;
-    bytes += add;
-    staged[l] = 1;
-  }
   auto build = [&](auto nc_tag) {
     constexpr int NC = decltype(nc_tag)::value;
     TailDesc<T, NC> h;
@@ -1127,11 +1113,8 @@ void MG<T>::build_tail(Arena& arena) {
     }
     for (int k = 0; k < h.nlev; ++k) {
       TailLevel<T, NC>& d = h.lv[k];
-      d.soff = -1;  // stencil read from global memory
-      if (staged[first + k]) {
-        d.soff = off = align(off);
-        off += StencilLayout<NC>::stride * d.nn;
-      }
+      d.soff = off = align(off);
+      off += StencilLayout<NC>::stride * d.nn;
       d.doff = off = align(off);
       off += NC * d.nn;
     }
