@@ -156,9 +156,7 @@ def vertex_weights(nx, ny, hx, hy):
     return w
 
 
-# P2 degree-3 cycle: "pre3" / "post2_3" are Pre and Post2 writing to x2 and r, "mid" and
-# "post3" the third steps
-MODE = {"pre": 2, "res": 3, "first": 4, "post2": 5, "mid": 6, "post3": 7, "pre3": 8, "post2_3": 9}
+MODE = {"pre": 2, "res": 3, "first": 4, "post2": 5}
 
 
 def smooth(mode, p2, NC, nx, ny, hx, hy, lam, mu, p, dirv, xi, kK, bufs, cheb, NXc=1, NYc=1, dirc=None,

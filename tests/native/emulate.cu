@@ -310,8 +310,7 @@ int emu_transfer(int NC, int NXf, int NYf, const int* dirf, int NXc, int NYc, co
   return 0;
 }
 
-// fused smoothing steps (FP64).  bufs = {b, dinv, x, x2, r, d}; cheb = {c0, c1, c2}
-// ({c0, .., c4} for the degree-3 P2 modes: 6 Mid, 7 Post3, 8 Pre and 9 Post2 of that cycle);
+// fused smoothing steps (FP64).  bufs = {b, dinv, x, x2, r, d}; cheb = {c0, c1, c2};
 // level given by p2 (P2 lattice of nx x ny cells) or P1 (NC comps on nx x ny cells);
 // xc / dirc / NXc, NYc: the next coarser lattice (post1 source, resr target bc)
 int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, double lam, double mu, double p,
@@ -330,9 +329,7 @@ int emu_smooth(int p2, int NC, int mode, int nx, int ny, double hx, double hy, d
     auto P = p2params<double>(nx, ny, hx, hy, lam, mu, p, pmin, dir);
     P2Io<double> io;
     std::memset(&io, 0, sizeof(io));
-    // modes 8 and 9: Pre and Post2 of the degree-3 cycle (results to x2 and r)
-    io.deg3 = mode >= kP2Mid;
-    io.mode = mode == 8 ? kP2Pre : mode == 9 ? kP2Post2 : mode;
+    io.mode = mode;
     io.u = bufs[2];
     io.B = B;
     io.xc = mode == kP2First ? xc : nullptr;  // optional fused prolongation

@@ -457,54 +457,6 @@ def test_fused_smoothing_steps_match_composition(level):
         assert np.array_equal(bufs2["x"], x)
 
 
-@pytest.mark.parametrize("wide", [False, True])
-def test_p2_degree3_smoothing_steps_match_composition(wide):
-    """Degree-3 Chebyshev on the P2 level (TOPO_P2_DEGREE=3): PRE writes its two-step
-    result to x2, MID takes the third step x = x2 + c3 (x2 - x1) + c4 Dinv (b - A x2)
-    with x1 = c0 Dinv b; after the coarse correction FIRST is unchanged, POST2 writes its
-    result z to r, and POST3 takes x = z + c3 (z - (u + d0)) + c4 Dinv (b - A z).  Each
-    against the same steps composed from plain applies."""
-    nx, ny, hx, hy, p = (70, 17, 0.025, 0.05, 3.0) if wide else (34, 10, 0.05, 0.05, 3.0)
-    lam, mu = lame(1.0, 0.3)
-    rng = np.random.default_rng(23)
-    xi = rng.uniform(0.05, 1.0, (nx + 1) * (ny + 1))
-    dirv = emu.make_dir(nx, ny, hx, hy, ["Left"])
-    lv = emu.build_levels(True, nx, ny, hx, hy, dirv, 2)
-    f = lv[0]
-    A = lambda u: emu.p2_apply(nx, ny, hx, hy, lam, mu, p, dirv, xi, u)
-    n = 2 * f["NX"] * f["NY"]
-    free = _free_rows(f["dir"], f["NX"], f["NY"], 2)
-    b = rng.standard_normal(n) * free
-    x = rng.standard_normal(n) * free
-    dinv = rng.uniform(0.5, 2.0, n)
-    dinv[~free] = 1.0
-    cheb = np.array([0.7, 0.3, 0.9, 0.25, 0.8])
-    run = lambda mode, bufs: emu.smooth(mode, True, 2, nx, ny, hx, hy, lam, mu, p, dirv, xi, None, bufs, cheb)
-    tol = lambda ref: 1e-12 * np.max(np.abs(ref))
-    bufs = dict(b=b.copy(), dinv=dinv.copy(), x=np.zeros(n), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
-    run("pre3", bufs)
-    x1 = cheb[0] * dinv * b
-    x2 = x1 + cheb[1] * x1 + cheb[2] * dinv * (b - A(x1))
-    assert np.max(np.abs(bufs["x2"] - x2)) <= tol(x2)
-    assert not np.any(bufs["x"])
-    run("mid", bufs)
-    x3 = x2 + cheb[3] * (x2 - x1) + cheb[4] * dinv * (b - A(x2))
-    assert np.max(np.abs(bufs["x"] - x3)) <= tol(x3)
-    # post-smoothing from u (the coarse correction already added)
-    u = x.copy()
-    bufs = dict(b=b.copy(), dinv=dinv.copy(), x=u.copy(), x2=np.zeros(n), r=np.zeros(n), d=np.zeros(n))
-    run("first", bufs)
-    r0 = b - A(u)
-    d0 = cheb[0] * dinv * r0
-    run("post2_3", bufs)
-    z = u + d0 + cheb[1] * d0 + cheb[2] * dinv * (r0 - A(d0))
-    assert np.max(np.abs(bufs["r"] - z)) <= tol(z)
-    assert np.array_equal(bufs["x"], u)
-    run("post3", bufs)
-    ref = z + cheb[3] * (z - (u + d0)) + cheb[4] * dinv * (b - A(z))
-    assert np.max(np.abs(bufs["x"] - ref)) <= tol(ref)
-
-
 @pytest.mark.parametrize("nx,ny,radius", [(16, 8, 0.05), (24, 12, 0.05), (12, 6, 0.2)])
 def test_coarse_chebyshev_solve(nx, ny, radius):
     """Truncated filter hierarchy: the planned interval holds the spectrum of

@@ -839,7 +839,6 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg32.cheb_lo_frac = C->cheb_lo_state;
         C->smg32.trace_setup = C->trace_solves;
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
-        if (const char* e = std::getenv("TOPO_P2_DEGREE")) C->smg32.p2_degree = std::atoi(e) == 3 ? 3 : 2;
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg32.set_coefficients(kK, kM);
@@ -851,7 +850,6 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg64.use_graphs = graphs_enabled();
         C->smg64.cheb_lo_frac = C->cheb_lo_state;
         C->smg64.use_tail = env_flag("TOPO_TAIL", true);
-        if (const char* e = std::getenv("TOPO_P2_DEGREE")) C->smg64.p2_degree = std::atoi(e) == 3 ? 3 : 2;
         C->smg64.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg64.set_coefficients(kK, kM);

@@ -163,7 +163,6 @@ class MG {
   bool fp64_solution = false;
 
   int cheb_degree = 2;  // the fused smoothing kernels implement degree 2
-  int p2_degree = 2;    // the P2 level: 2, or 3 (two more fused steps, P2Mode)
   double cheb_lo_frac = 0.1;   // smoothing interval [lo_frac, 1.1] * lambda_max
   int power_iters = 10;
   int power_iters_warm = 4;  // level 0 of a P2 hierarchy, started from the previous set-up's vector

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(P2M_THREADS, p2_march_min_blocks<T>())
       p2_march_run<T, MODE, false>(P, xi, io, lane, js, je, acc);
     }
   }
-  if constexpr ((MODE == kP2Apply || MODE == kP2Post2 || MODE == kP2Post3) && !IsDD<T>::value) {
+  if constexpr ((MODE == kP2Apply || MODE == kP2Post2) && !IsDD<T>::value) {
     if (io.fuse != kFuseNone) {
       double tot[2];
       if (finish_reduction<2>(acc, io.partials, io.counter, tot)) {
@@ -684,8 +684,6 @@ inline void prime_march_occupancy() {
   (void)p2_march_bps<T, kP2Res>();
   (void)p2_march_bps<T, kP2First>();
   (void)p2_march_bps<T, kP2Post2>();
-  (void)p2_march_bps<T, kP2Mid>();
-  (void)p2_march_bps<T, kP2Post3>();
   (void)p1_march_bps<T, 1, kP2Apply>();
   (void)p1_march_bps<T, 1, kP2Pre>();
   (void)p1_march_bps<T, 1, kP2Res>();
@@ -707,19 +705,15 @@ inline const char* mode_name(int mode) {
     case kP2Pre: return "Pre";
     case kP2Res: return "Res";
     case kP2First: return "First";
-    case kP2Mid: return "Mid";
-    case kP2Post3: return "Post3";
     default: return "Post2";
   }
 }
 template <class T>
 inline const char* p2_family(int mode) {
-  static const char* f32[8] = {"P2 march FP32 Apply", "P2 march FP32 Diag", "P2 march FP32 Pre",
-                               "P2 march FP32 Res",   "P2 march FP32 First", "P2 march FP32 Post2",
-                               "P2 march FP32 Mid",   "P2 march FP32 Post3"};
-  static const char* f64[8] = {"P2 march FP64 Apply", "P2 march FP64 Diag", "P2 march FP64 Pre",
-                               "P2 march FP64 Res",   "P2 march FP64 First", "P2 march FP64 Post2",
-                               "P2 march FP64 Mid",   "P2 march FP64 Post3"};
+  static const char* f32[6] = {"P2 march FP32 Apply", "P2 march FP32 Diag", "P2 march FP32 Pre",
+                               "P2 march FP32 Res", "P2 march FP32 First", "P2 march FP32 Post2"};
+  static const char* f64[6] = {"P2 march FP64 Apply", "P2 march FP64 Diag", "P2 march FP64 Pre",
+                               "P2 march FP64 Res", "P2 march FP64 First", "P2 march FP64 Post2"};
   return (sizeof(T) == 4 ? f32 : f64)[mode];
 }
 // vectors of the level a smoothing or operator mode moves: operand(s) read, results written
@@ -732,8 +726,6 @@ inline int mode_vectors(int mode, bool p2, bool fused_rz) {
     case kP2Pre: return 3;
     case kP2Res: return 3;
     case kP2First: return 5;
-    case kP2Mid: return 4;    // x2, b, Dinv read; x written
-    case kP2Post3: return 6;  // r, b, Dinv, x, d read; x written
     default: return p2 ? (fused_rz ? 5 : 4) : 5;
   }
 }
@@ -758,8 +750,6 @@ inline void launch_p2_tile(const P2Params<T>& P, const T* xi, const P2Io<T>& io,
     case kP2Pre: launch_p2_mode<T, kP2Pre>(P, xi, io, s); break;
     case kP2Res: launch_p2_mode<T, kP2Res>(P, xi, io, s); break;
     case kP2First: launch_p2_mode<T, kP2First>(P, xi, io, s); break;
-    case kP2Mid: launch_p2_mode<T, kP2Mid>(P, xi, io, s); break;
-    case kP2Post3: launch_p2_mode<T, kP2Post3>(P, xi, io, s); break;
     default: launch_p2_mode<T, kP2Post2>(P, xi, io, s); break;
   }
 }
@@ -1337,8 +1327,7 @@ int MG<T>::setup(cudaStream_t s) {
     double* c = cc.data() + 8 * l;
     c[0] = 1.0 / theta;
     double rho_old = 1.0 / sigma;
-    const int deg = (l == 0 && S.p2) ? std::max(cheb_degree, p2_degree) : cheb_degree;
-    for (int k = 1; k < deg && k < 4; ++k) {
+    for (int k = 1; k < cheb_degree && k < 4; ++k) {
       const double rho_new = 1.0 / (2.0 * sigma - rho_old);
       c[2 * k - 1] = rho_new * rho_old;
       c[2 * k] = 2.0 * rho_new / delta;
@@ -1452,14 +1441,8 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     std::memset(&io, 0, sizeof(io));
     io.B = B;
     io.u = x;
-    io.deg3 = p2_degree == 3;
     io.mode = kP2Pre;
     launch_p2_tile<T>(p2_, xi_, io, s);
-    if (io.deg3) {
-      io.mode = kP2Mid;
-      launch_p2_tile<T>(p2_, xi_, io, s);
-      ++launches;
-    }
     io.mode = kP2Res;
     launch_p2_tile<T>(p2_, xi_, io, s);
     {
@@ -1472,11 +1455,6 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
     io.xc = c.x;
     launch_p2_tile<T>(p2_, xi_, io, s);
     io.mode = kP2Post2;
-    if (io.deg3) {
-      launch_p2_tile<T>(p2_, xi_, io, s);
-      io.mode = kP2Post3;
-      ++launches;
-    }
     if (l == 0 && fuse_rz_) {  // the CG's r.r, r.z and test (see pcg_body)
       io.fuse = kFuseRZ;
       io.partials = red_->partials;
@@ -1721,8 +1699,7 @@ void MG<T>::pcg_body(cudaStream_t s, cudaGraphConditionalHandle h, int use_cond)
   const int fam = march_family(true, sizeof(T), 2);
   const dim3 ga = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Apply>(), seg, fam);
   const dim3 gp = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Post2>(), seg, fam);
-  const dim3 gp3 = march_grid(specs_[0].nx, specs_[0].ny, p2_march_bps<T, kP2Post3>(), seg, fam);
-  const size_t mblocks = std::max({size_t(ga.x) * ga.y, size_t(gp.x) * gp.y, size_t(gp3.x) * gp3.y});
+  const size_t mblocks = std::max(size_t(ga.x) * ga.y, size_t(gp.x) * gp.y);
   if (specs_[0].p2 && mblocks * 2 <= size_t(red_->blocks) * 16) {
     // P2 level 0: p.q is reduced inside the operator launch, r.r / r.z and the
     // iteration's test inside the V-cycle's last post-smoothing launch

@@ -261,12 +261,7 @@ constexpr int P2M_WARPS = 4;                  // warps per block, one row segmen
 constexpr int P2M_THREADS = 32 * P2M_WARPS;
 
 // What one launch of the P2 kernel computes.
-enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2First = 4, kP2Post2 = 5, kP2Mid = 6, kP2Post3 = 7 };
-// Degree-3 Chebyshev smoothing (P2Io::deg3) adds one step on each side: Pre writes its
-// two-step result to x2 and kP2Mid takes the third step (operand x2, the first step
-// c0 Dinv b recomputed per node) into x; Post2 writes its result to r and kP2Post3
-// takes the third step (operand r, the previous iterate x + d0) into x.
-// Step 3 of the recurrence: x3 = x2 + c3 (x2 - x1) + c4 Dinv (b - A x2).
+enum P2Mode { kP2Apply = 0, kP2Diag = 1, kP2Pre = 2, kP2Res = 3, kP2First = 4, kP2Post2 = 5 };
 
 struct PcgDev;
 
@@ -292,8 +287,7 @@ struct P2Io {
   PcgDev* pcg;         // CG scalars
   unsigned long long cond;  // graph conditional handle of the CG loop
   int use_cond;
-  int deg3;            // degree-3 smoothing (see P2Mode)
-  T cf[5];             // B.cheb[0..4], copied in by P2March::prepare (registers, not re-read)
+  T cf[3];             // B.cheb[0..2], copied in by P2March::prepare (registers, not re-read)
 };
 
 // Which of a lane's cells and nodes exist and which nodes are clamped.  A lane
@@ -332,10 +326,8 @@ template <class T>
 struct P2March {
   // once per launch, before any phase: the smoothing coefficients by value
   TOPO_HD static void prepare(P2Io<T>& io) {
-    const bool smooth = io.mode == kP2Pre || io.mode == kP2First || io.mode == kP2Post2 || io.mode == kP2Mid ||
-                        io.mode == kP2Post3;
-    const int nc = (io.mode == kP2Mid || io.mode == kP2Post3) ? 5 : 3;
-    for (int k = 0; k < 5; ++k) io.cf[k] = (smooth && io.B.cheb && k < nc) ? io.B.cheb[k] : T(0);
+    const bool smooth = io.mode == kP2Pre || io.mode == kP2First || io.mode == kP2Post2;
+    for (int k = 0; k < 3; ++k) io.cf[k] = (smooth && io.B.cheb) ? io.B.cheb[k] : T(0);
   }
 
   // operand of the apply at node n for the launch's mode
@@ -352,12 +344,6 @@ struct P2March {
       }
       case kP2Post2:
         ld2(io.B.d + 2 * n, v);
-        break;
-      case kP2Mid:
-        ld2(io.B.x2 + 2 * n, v);
-        break;
-      case kP2Post3:
-        ld2(io.B.r + 2 * n, v);
         break;
       default:
         ld2(io.u + 2 * n, v);
@@ -594,7 +580,7 @@ struct P2March {
   // nodes), loaded before the step's arithmetic so that it hides their latency:
   //   Pre, First: b, Dinv   Res: b   Post2: w, Dinv (+ b for the fused r.r, r.z)
   struct Fin {
-    T v[4][4][2];
+    T v[4][3][2];
   };
   template <bool LEAN = false>
   TOPO_HD static void fin_load(const P2Params<T>& P, const P2Io<T>& io, const P2Lane<T>& L, int j, Fin& F) {
@@ -619,22 +605,12 @@ struct P2March {
           ld2(B.dinv + i, F.v[q][1]);
           if (io.fuse == kFuseRZ) ld2(B.b + i, F.v[q][2]);
           break;
-        case kP2Mid:
-          ld2(B.b + i, F.v[q][0]);
-          ld2(B.dinv + i, F.v[q][1]);
-          break;
-        case kP2Post3:
-          ld2(B.b + i, F.v[q][0]);
-          ld2(B.dinv + i, F.v[q][1]);
-          ld2(B.x + i, F.v[q][2]);
-          ld2(B.d + i, F.v[q][3]);
-          break;
         default: break;
       }
     }
   }
   // the same vectors for one node (row 2 of the last cell row)
-  TOPO_HD static void fin_load_node(const P2Io<T>& io, size_t i, T (&v)[4][2]) {
+  TOPO_HD static void fin_load_node(const P2Io<T>& io, size_t i, T (&v)[3][2]) {
     const SmoothBufs<T>& B = io.B;
     switch (io.mode) {
       case kP2Pre:
@@ -648,16 +624,6 @@ struct P2March {
         ld2(B.dinv + i, v[1]);
         if (io.fuse == kFuseRZ) ld2(B.b + i, v[2]);
         break;
-      case kP2Mid:
-        ld2(B.b + i, v[0]);
-        ld2(B.dinv + i, v[1]);
-        break;
-      case kP2Post3:
-        ld2(B.b + i, v[0]);
-        ld2(B.dinv + i, v[1]);
-        ld2(B.x + i, v[2]);
-        ld2(B.d + i, v[3]);
-        break;
       default: break;
     }
   }
@@ -665,7 +631,7 @@ struct P2March {
   // v: the node's finish vectors (Fin); cl: the node is clamped (an identity row);
   // u: the node's operand as fetched (raw at a clamped node)
   TOPO_HD static void finish_node(const P2Params<T>& P, const P2Io<T>& io, int a, int b, bool cl, const T (&sum)[2],
-                                  const T (&u)[2], const T (&v)[4][2], T (&acc)[2]) {
+                                  const T (&u)[2], const T (&v)[3][2], T (&acc)[2]) {
     const int NX = 2 * P.nx + 1;
     const size_t n = size_t(unsigned(b) * unsigned(NX) + unsigned(a)), i = 2 * n;
     if (io.mode == kP2Diag) {
@@ -702,28 +668,7 @@ struct P2March {
         const T(&bv)[2] = v[0];
         const T(&dv)[2] = v[1];
         const T r0 = bv[0] - r[0], r1 = bv[1] - r[1];
-        // (degree 3: the two-step result goes to x2, the operand of kP2Mid)
-        st2((io.deg3 ? B.x2 : B.x) + i, un[0] + c1 * un[0] + c2 * dv[0] * r0, un[1] + c1 * un[1] + c2 * dv[1] * r1);
-        break;
-      }
-      case kP2Mid:
-      case kP2Post3: {
-        // third step: x3 = x2 + c3 (x2 - x1) + c4 Dinv (b - A x2), x2 the operand; x1 = c0 Dinv b
-        // before the coarse solve, x + d0 after it
-        const T(&bv)[2] = v[0];
-        const T(&dv)[2] = v[1];
-        const T c3 = io.cf[3], c4 = io.cf[4];
-        T x1[2];
-        for (int k = 0; k < 2; ++k) x1[k] = io.mode == kP2Mid ? c0 * dv[k] * bv[k] : v[2][k] + v[3][k];
-        const T z0 = un[0] + c3 * (un[0] - x1[0]) + c4 * dv[0] * (bv[0] - r[0]);
-        const T z1 = un[1] + c3 * (un[1] - x1[1]) + c4 * dv[1] * (bv[1] - r[1]);
-        st2(B.x + i, z0, z1);
-        if (io.mode == kP2Post3 && io.fuse == kFuseRZ) {
-          acc[0] += bv[0] * bv[0];
-          acc[1] += bv[0] * z0;
-          acc[0] += bv[1] * bv[1];
-          acc[1] += bv[1] * z1;
-        }
+        st2(B.x + i, un[0] + c1 * un[0] + c2 * dv[0] * r0, un[1] + c1 * un[1] + c2 * dv[1] * r1);
         break;
       }
       case kP2Res: {
@@ -747,7 +692,7 @@ struct P2March {
         const T(&dv)[2] = v[1];
         const T z0 = wv[0] + c1 * un[0] - c2 * dv[0] * r[0];
         const T z1 = wv[1] + c1 * un[1] - c2 * dv[1] * r[1];
-        st2((io.deg3 ? B.r : B.x) + i, z0, z1);  // (degree 3: r is kP2Post3's operand)
+        st2(B.x + i, z0, z1);
         if (io.fuse == kFuseRZ) {
           const T(&bv)[2] = v[2];
           acc[0] += bv[0] * bv[0];
@@ -782,7 +727,7 @@ struct P2March {
         if (r < 2) {
           finish_node(P, io, a, b, cl, L.A[r][c], L.U[r][c], F.v[2 * r + c], acc);
         } else {  // row 2: only on the last cell row
-          T v[4][2] = {};
+          T v[3][2] = {};
           fin_load_node(io, 2 * (size_t(b) * NX + a), v);
           finish_node(P, io, a, b, cl, L.A[r][c], L.U[r][c], v, acc);
         }
