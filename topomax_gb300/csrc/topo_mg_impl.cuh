@@ -114,6 +114,8 @@ __device__ __forceinline__ void p2_march_run(const P2Params<T>& P, const T* __re
     const bool fin = owner && j >= js;
     typename P2March<T>::Fin F;
     if (MODE != kP2Apply && MODE != kP2Diag && fin) P2March<T>::template fin_load<LEAN>(P, io, L, j, F);
+    // the pair type keeps no prefetched mass matrices (registers): they are loaded here
+    if constexpr (IsDD<T>::value) P2March<T>::template load_mass<LEAN>(P, L.K, L.i, j, L.M);
     P2March<T>::template compute<LEAN>(P, L, j, MODE);
     p2m_exchange_up<T>(L, lane);
     if (fin) P2March<T>::template finish<LEAN>(P, io, L, j, j == P.ny - 1 ? 3 : 2, F, acc);

@@ -550,7 +550,7 @@ struct P2March {
     }
     N.X[0] = density<LEAN>(P, xi, L.K, 0, L.i, j + 1);
     if (L.edge) N.X[1] = density<LEAN>(P, xi, L.K, 1, L.i, j + 1);
-    load_mass<LEAN>(P, L.K, L.i, j, N.M);
+    if constexpr (!IsDD<T>::value) load_mass<LEAN>(P, L.K, L.i, j, N.M);  // (dd: loaded at compute time)
   }
 
   // after advance(): the prefetched loads become rows 1, 2 of the step
@@ -560,7 +560,8 @@ struct P2March {
         for (int d = 0; d < 2; ++d) L.U[r][c][d] = N.U[r - 1][c][d];
     L.X[1][0] = N.X[0];
     L.X[1][1] = N.X[1];
-    for (int k = 0; k < 12; ++k) L.M[k] = N.M[k];
+    if constexpr (!IsDD<T>::value)
+      for (int k = 0; k < 12; ++k) L.M[k] = N.M[k];
   }
 
   // element results of cell (L.i, j), both triangles (0 <= j < ny always)
