@@ -110,6 +110,10 @@ void p2_run_io(const P2Params<T>& P, const T* xi, P2Io<T> io, int seg = 0) {
               else P2March<T>::fin_load(P, io, L[l], j, F[l]);
             }
         for (int l = 0; l < 32; ++l) {
+          if constexpr (IsDD<T>::value) {  // the kernel's pair path loads the mass matrices here
+            if (lean) P2March<T>::template load_mass<true>(P, L[l].K, L[l].i, j, L[l].M);
+            else P2March<T>::load_mass(P, L[l].K, L[l].i, j, L[l].M);
+          }
           if (lean) P2March<T>::template compute<true>(P, L[l], j, io.mode);
           else P2March<T>::compute(P, L[l], j, io.mode);
         }
