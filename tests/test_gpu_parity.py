@@ -262,30 +262,6 @@ def test_tail_matches_level_kernels(precision, monkeypatch):
     assert np.max(np.abs(results[0][1] - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_cluster_vcycle_matches_level_kernels(precision, monkeypatch):
-    """The state V-cycle below the largest stencil level runs in one thread-block cluster
-    (TOPO_CLUSTER=1, the default) with the per-level kernels' node steps, phases separated
-    by the cluster barrier: the solves agree with the per-level launches (TOPO_CLUSTER=0)
-    to rounding of the final refinement and take the same number of iterations."""
-    import torch
-    from topomax_gb300 import fem as F
-    d = _design()
-    results = []
-    for flag in ("1", "0"):
-        monkeypatch.setenv("TOPO_CLUSTER", flag)
-        prob, V = _gpu_problem(d, 400, 200, precision=precision, rtol=1e-10)
-        prob.set_penalization(3.0)
-        g = torch.Generator().manual_seed(4)
-        xi = F.Function(V, (torch.rand(V.dim(), generator=g, dtype=torch.float64) * 0.99 + 0.01).cuda())
-        u = prob.forward(xi)
-        results.append((prob.stats["state_iterations"], u.tensor.cpu().numpy()))
-        del prob
-    assert results[0][0] == results[1][0], [r[0] for r in results]
-    ref = results[1][1]
-    assert np.max(np.abs(results[0][1] - ref)) <= 1e-13 * np.max(np.abs(ref))
-
-
 def test_pair_fp32_residual_operator_matches_fp64(monkeypatch):
     """Mixed precision computes its refinement residuals b - K u with the pair-of-FP32
     operator (FP32-pipe arithmetic, differences of the FP64 operand taken in FP64);

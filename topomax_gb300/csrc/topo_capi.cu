@@ -450,7 +450,6 @@ int init_filter(topo_ctx* C, double eps) {
     C->fmg32.fp64_solution = true;  // FGMRES directions keep the inner solutions in FP64
     C->fmg32.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg32.use_tail = env_flag("TOPO_TAIL", true);
-    C->fmg32.use_cluster = env_flag("TOPO_CLUSTER", true);
     C->fmg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg32.set_coefficients(kK, kM);
@@ -462,7 +461,6 @@ int init_filter(topo_ctx* C, double eps) {
     C->fmg64.use_graphs = graphs_enabled();
     C->fmg64.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg64.use_tail = env_flag("TOPO_TAIL", true);
-    C->fmg64.use_cluster = env_flag("TOPO_CLUSTER", true);
     C->fmg64.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg64.set_coefficients(kK, kM);
@@ -841,7 +839,6 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg32.cheb_lo_frac = C->cheb_lo_state;
         C->smg32.trace_setup = C->trace_solves;
         C->smg32.use_tail = env_flag("TOPO_TAIL", true);
-        C->smg32.use_cluster = env_flag("TOPO_CLUSTER", true);
         C->smg32.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg32.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg32.set_coefficients(kK, kM);
@@ -853,7 +850,6 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
         C->smg64.use_graphs = graphs_enabled();
         C->smg64.cheb_lo_frac = C->cheb_lo_state;
         C->smg64.use_tail = env_flag("TOPO_TAIL", true);
-        C->smg64.use_cluster = env_flag("TOPO_CLUSTER", true);
         C->smg64.profile_levels = env_flag("TOPO_PROFILE", false);
         C->smg64.init(C->sspec, C->srefs.data(), C->lmbda, C->mu, C->arena, &C->red);
         C->smg64.set_coefficients(kK, kM);

@@ -10,7 +10,6 @@
 
 #include <cuda_runtime.h>
 #include <cstring>
-#include <memory>
 #include <string>
 #include <mutex>
 #include <vector>
@@ -136,10 +135,7 @@ class MG {
   // chosen from the coefficients at the first setup() (a filter's never
   // change); a caller whose scalar coefficients change between setups calls
   // this first so that the next setup() chooses them again.
-  void coefficients_changed() {
-    cc_selected_ = false;
-    cl_built_ = false;
-  }
+  void coefficients_changed() { cc_selected_ = false; }
   // y = A_l x; on level 0, op selects the Krylov operator instead of the
   // preconditioner's (they differ only where the penalisation is clamped)
   void apply(int l, const T* x, T* y, cudaStream_t s, bool op = false);
@@ -183,11 +179,6 @@ class MG {
   int coarse_cheb_level() const { return cheb_coarse_; }
   int coarse_cheb_deg = 0;
   bool use_p1_march = true;  // large P1 levels: column march (false: node-centric kernels)
-  // run the V-cycle of the levels with at most kClusterMaxNodes nodes (down to the
-  // coarsest) in one thread-block cluster, phases separated by the hardware cluster
-  // barrier, instead of six launches per level and the tail (TOPO_CLUSTER=0: off)
-  bool use_cluster = true;
-  int cluster_level() const { return cl_desc_ ? cl_first_ : -1; }
   long long capture_failures = 0;  // recordings that failed (those solves ran host-driven)
   // opt-in level timing (host-driven mode only): inclusive ms per level, summed
   bool profile_levels = false;
@@ -273,17 +264,6 @@ class MG {
   bool fuse_rz_ = false;
   unsigned long long fuse_cond_ = 0;
   int fuse_use_cond_ = 0;
-
-  // cluster V-cycle: levels [cl_first_, coarsest] in ClusterDesc<T, NC> (device)
-  int cl_first_ = -1;
-  void* cl_desc_ = nullptr;
-  struct CudaFree {
-    void operator()(void* p) const { cudaFree(p); }
-  };
-  std::unique_ptr<void, CudaFree> cl_owned_;  // the description's allocation
-  bool cl_built_ = false;
-  void build_cluster();
-  bool run_cluster(const T* b, T* x, cudaStream_t s);  // false: not taken (per-level path)
 
   T* pcg_[kScratch] = {};
   double* xacc_ = nullptr;  // FP64 solution of the CG loop (fp64_solution)

@@ -11,8 +11,6 @@
 #include <type_traits>
 #include <utility>
 
-#include <cooperative_groups.h>
-
 #include "topo_kclock.h"
 #include "topo_mg.h"
 #include "topo_p1.cuh"
@@ -521,97 +519,6 @@ __global__ void __launch_bounds__(kTailThreads)
     mark();
   }
   if (trace) trace[kTailTraceSlots - 1] += 1;
-}
-
-// ---------------------------------------------------------------------------
-// cluster V-cycle: the levels below the largest stencil level, whole, in one
-// thread-block cluster
-// ---------------------------------------------------------------------------
-// The mid-sized and small levels (up to kClusterMaxNodes nodes) are bound by
-// launch latency: six launches per level and V-cycle.  One cluster of
-// kClusterCtas CTAs runs their whole V-cycle instead (pre-smoothing, residual,
-// restriction per level, the dense coarsest solve, then prolongation and the two
-// post-smoothing steps per level), every phase a loop over the level's nodes with
-// the per-level kernels' node functions, the phases separated by the hardware
-// cluster barrier (~0.3 us, against ~2 us for a launch).  Vectors and stencils
-// stay in global memory (L2-resident at these sizes); the barrier's release /
-// acquire at cluster scope orders the phases' global writes and reads.
-constexpr int kClusterCtas = 16;
-constexpr int kClusterThreads = 1024;
-constexpr int kClusterMaxNodes = 40000;
-constexpr int kClusterMaxLevels = 12;
-
-template <class T, int NC>
-struct ClusterLevel {
-  P1Stencil<T, NC> P;
-  SmoothBufs<T> B;  // the first level's b and x come from the launch
-  Transfer X;       // to the next level
-  T* cb;            // next level's right-hand side (restriction output)
-  T* cx;            // next level's solution (prolongation input)
-  int nn, NX, nnc, NXc;
-};
-
-template <class T, int NC>
-struct ClusterDesc {
-  int nlev;  // levels in the cluster, the last one the dense coarsest level
-  int mc;    // dofs of the coarsest level
-  const T* cinv;
-  ClusterLevel<T, NC> lv[kClusterMaxLevels];
-};
-
-template <class T, int NC>
-__global__ void __launch_bounds__(kClusterThreads)
-    k_cluster_vcycle(const ClusterDesc<T, NC>* __restrict__ D, const T* b0, T* x0) {
-  namespace cgr = cooperative_groups;
-  cgr::cluster_group cl = cgr::this_cluster();
-  const int tid = int(cl.thread_rank()), nt = int(cl.num_threads());
-  const int nlev = D->nlev;
-  // (descriptions read in place: they hold the Dirichlet lists)
-  for (int l = 0; l + 1 < nlev; ++l) {
-    const ClusterLevel<T, NC>& L = D->lv[l];
-    SmoothBufs<T> B = L.B;
-    if (l == 0) {
-      B.b = b0;
-      B.x = x0;
-    }
-    const int NX = L.NX, nn = L.nn;
-    for (int n = tid; n < nn; n += nt) P1Smooth<T, NC>::pre(n % NX, n / NX, L.P, B);
-    cl.sync();
-    for (int n = tid; n < nn; n += nt) P1Smooth<T, NC>::res(n % NX, n / NX, L.P, B);
-    cl.sync();
-    for (int n = tid; n < L.nnc; n += nt)
-      TransferKern<T, NC>::node_restrict(n % L.NXc, n / L.NXc, L.X, static_cast<const T*>(B.r), L.cb,
-                                         static_cast<const T*>(nullptr));
-    cl.sync();
-  }
-  {  // coarsest level: x = A^-1 b with the dense inverse
-    const ClusterLevel<T, NC>& C = D->lv[nlev - 1];
-    const int m = D->mc;
-    const T* bc = (nlev == 1) ? b0 : C.B.b;
-    T* xc = (nlev == 1) ? x0 : C.B.x;
-    for (int i = tid; i < m; i += nt) {
-      T acc = T(0);
-      for (int j = 0; j < m; ++j) acc += D->cinv[i * m + j] * bc[j];
-      xc[i] = acc;
-    }
-    cl.sync();
-  }
-  for (int l = nlev - 2; l >= 0; --l) {
-    const ClusterLevel<T, NC>& L = D->lv[l];
-    SmoothBufs<T> B = L.B;
-    if (l == 0) {
-      B.b = b0;
-      B.x = x0;
-    }
-    const int NX = L.NX, nn = L.nn;
-    for (int n = tid; n < nn; n += nt)
-      TransferKern<T, NC>::node_prolong_add(n % NX, n / NX, L.X, static_cast<const T*>(L.cx), B.x);
-    cl.sync();
-    for (int n = tid; n < nn; n += nt) P1Smooth<T, NC>::first(n % NX, n / NX, L.P, B);
-    cl.sync();
-    for (int n = tid; n < nn; n += nt) P1Smooth<T, NC>::post2(n % NX, n / NX, L.P, B);
-    if (l > 0) cl.sync();  // the finer level's prolongation reads this x
-  }
 }
 
 template <class T, int NC>
@@ -1452,116 +1359,7 @@ int MG<T>::setup(cudaStream_t s) {
   if (e != cudaSuccess) return -5;
   if (st) return -2;
   tune_marches(s);
-  if (!cl_built_) {
-    build_cluster();
-    graph_valid_ = false;  // the V-cycle's launches change with it
-  }
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -5;
-}
-
-// Chooses the cluster V-cycle's levels (all levels from the first whose stencil
-// levels down to the coarsest have at most kClusterMaxNodes nodes; a hierarchy
-// truncated by the coarse Chebyshev solve keeps its own path) and writes their
-// description.  At the end of the first set-up; the pointers stay fixed after it.
-template <class T>
-void MG<T>::build_cluster() {
-  std::lock_guard<std::recursive_mutex> lock(device_lock());  // allocates and copies
-  cl_built_ = true;
-  cl_first_ = -1;
-  cl_desc_ = nullptr;
-  if (!use_cluster || cheb_coarse_ >= 0) return;
-  const int L = levels();
-  int first = L - 1;
-  while (first > 0 && !specs_[first - 1].p2 && lv_[first - 1].st && specs_[first - 1].nn() <= size_t(kClusterMaxNodes) &&
-         specs_[first - 1].NC == specs_[L - 1].NC && L - (first - 1) <= kClusterMaxLevels)
-    --first;
-  if (L - 1 - first < 2) return;  // fewer than two smoothing levels: nothing to gain
-  auto build = [&](auto nc_tag) {
-    constexpr int NC = decltype(nc_tag)::value;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kClusterCtas);
-    cfg.blockDim = dim3(kClusterThreads);
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kClusterCtas;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaFuncSetAttribute(k_cluster_vcycle<T, NC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_vcycle<T, NC>, &cfg) != cudaSuccess || nclusters < 1) {
-      cudaGetLastError();
-      return;
-    }
-    ClusterDesc<T, NC> h;
-    std::memset(&h, 0, sizeof(h));
-    h.nlev = L - first;
-    h.mc = int(specs_[L - 1].ndof());
-    h.cinv = cinv_;
-    for (int k = 0; k < h.nlev; ++k) {
-      const int l = first + k;
-      const LevelSpec& S = specs_[l];
-      Lev& v = lv_[l];
-      ClusterLevel<T, NC>& q = h.lv[k];
-      q.B = SmoothBufs<T>{v.b, v.dinv, v.x, v.x2, v.r, v.d, cheb_ + 8 * l};
-      q.nn = int(S.nn());
-      q.NX = S.NX;
-      if (l + 1 < L) {
-        q.P = P1Stencil<T, NC>{S.nx, S.ny, S.dir, v.st, v.inner};
-        q.X = make_transfer(S, specs_[l + 1]);
-        q.cb = lv_[l + 1].b;
-        q.cx = lv_[l + 1].x;
-        q.nnc = q.X.NXc * q.X.NYc;
-        q.NXc = q.X.NXc;
-      }
-    }
-    void* p = nullptr;
-    if (cudaMalloc(&p, sizeof(h)) != cudaSuccess) {
-      cudaGetLastError();
-      return;
-    }
-    cl_owned_.reset(p);
-    cudaMemcpy(p, &h, sizeof(h), cudaMemcpyHostToDevice);
-    cl_desc_ = p;
-    cl_first_ = first;
-  };
-  if (specs_[L - 1].NC == 2) build(std::integral_constant<int, 2>{});
-  else build(std::integral_constant<int, 1>{});
-}
-
-// One V-cycle from level cl_first_ down in the cluster kernel; false when the
-// cluster path is not available for this call (the per-level path runs).
-template <class T>
-bool MG<T>::run_cluster(const T* b, T* x, cudaStream_t s) {
-  if (!use_cluster || !cl_desc_) return false;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kClusterCtas);
-  cfg.blockDim = dim3(kClusterThreads);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kClusterCtas;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaError_t e;
-  {
-    KClock kc(s, "cluster V-cycle", cl_first_, 0.0);
-    if (specs_[cl_first_].NC == 2)
-      e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle<T, 2>, static_cast<const ClusterDesc<T, 2>*>(cl_desc_), b, x);
-    else
-      e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle<T, 1>, static_cast<const ClusterDesc<T, 1>*>(cl_desc_), b, x);
-  }
-  if (e != cudaSuccess) {  // nothing was launched: this and later V-cycles take the per-level path
-    cudaGetLastError();
-    use_cluster = false;
-    return false;
-  }
-  ++launches;
-  return true;
 }
 
 // One V-cycle from level l down: fused degree-2 Chebyshev pre-smoothing from
@@ -1616,7 +1414,6 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   Lev& v = lv_[l];
   const int L = levels();
   const LevelSpec& S = specs_[l];
-  if (l == cl_first_ && l != cheb_coarse_ && run_cluster(b, x, s)) return;
   if (l == cheb_coarse_ && cc_desc_) {
     KClock kc(s, "coarse Chebyshev (one CTA)", l, 0.0);
     launch_pdl(k_coarse_cheb<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
