@@ -76,27 +76,6 @@ def test_filter_matches_oracle(precision):
     assert np.max(np.abs(xi - ref)) <= 1e-10 * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("wide", ["1", "0"])
-def test_filter_truncated_at_a_wide_level_matches_oracle(wide, monkeypatch):
-    """At 400x200 the filter hierarchy's level 2 (101x51 = 5151 nodes, one shared interior
-    stencil row) is the first whose spectrum allows a short Chebyshev solve: with
-    TOPO_CHEB_WIDE=1 (the default) the V-cycle stops there (k_coarse_cheb_wide, up to 8
-    nodes per thread), with 0 one level further down (k_coarse_cheb).  Both reproduce the
-    oracle's filter to 1e-10."""
-    import topomax_gb300 as tg
-    monkeypatch.setenv("TOPO_CHEB_WIDE", wide)
-    d = _design()
-    nx, ny = 400, 200
-    mesh = tg.RectangleMesh(2.0, 1.0, nx, ny)
-    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
-    f = tg.HelmholtzFilter(0.05, V, precision="mixed", rtol=1e-12)
-    o = FEMOracle(Lattice(2.0, 1.0, nx, ny), d)
-    rho = np.random.default_rng(2).uniform(0, 1, o.L.n_vertices)
-    xi = f.apply(rho).vector()[:]
-    ref = o.filter_apply(rho)
-    assert np.max(np.abs(xi - ref)) <= 1e-10 * np.max(np.abs(ref))
-
-
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_filter_identity_at_zero_radius(precision):
     """tests/test_filter.py:25-34: epsilon = 0 leaves rho unchanged."""

@@ -450,7 +450,6 @@ int init_filter(topo_ctx* C, double eps) {
     C->fmg32.fp64_solution = true;  // FGMRES directions keep the inner solutions in FP64
     C->fmg32.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg32.use_tail = env_flag("TOPO_TAIL", true);
-    C->fmg32.use_cheb_wide = env_flag("TOPO_CHEB_WIDE", true);
     C->fmg32.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg32.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg32.set_coefficients(kK, kM);
@@ -462,7 +461,6 @@ int init_filter(topo_ctx* C, double eps) {
     C->fmg64.use_graphs = graphs_enabled();
     C->fmg64.cheb_lo_frac = C->cheb_lo_filter;
     C->fmg64.use_tail = env_flag("TOPO_TAIL", true);
-    C->fmg64.use_cheb_wide = env_flag("TOPO_CHEB_WIDE", true);
     C->fmg64.profile_levels = env_flag("TOPO_PROFILE", false);
     C->fmg64.init(C->fspec, C->frefs.data(), 0.0, 0.0, C->arena, &C->red);
     C->fmg64.set_coefficients(kK, kM);

@@ -175,9 +175,6 @@ class MG {
   // stop the V-cycle at the first P1 level whose Jacobi-scaled operator is well
   // conditioned enough for a short Chebyshev solve (scalar mass+stiffness levels)
   bool use_coarse_cheb = true;
-  // allow the truncation level to be one whose interior rows are all the same with up to
-  // 8 nodes per thread (k_coarse_cheb_wide; TOPO_CHEB_WIDE=0: at most 3, k_coarse_cheb)
-  bool use_cheb_wide = true;
   int coarse_cheb_max_degree = 16;
   int coarse_cheb_level() const { return cheb_coarse_; }
   int coarse_cheb_deg = 0;
@@ -252,7 +249,6 @@ class MG {
   int cheb_coarse_ = -1;
   void* cc_desc_ = nullptr;
   size_t cc_smem_ = 0;
-  bool cc_wide_ = false;  // the truncation level runs k_coarse_cheb_wide
   void select_coarse_cheb();
   void detect_uniform_levels();  // sets Lev::inner where every interior row is the same
   void* cc_buf_ = nullptr;

@@ -601,112 +601,6 @@ __global__ void __launch_bounds__(kTailThreads)
   }
 }
 
-// The same solve for a larger level whose interior nodes share one stencil row
-// (the filter's uniform levels, P1Stencil::inner): up to coarse_cheb_wide_npt nodes
-// per thread keep only their inverse diagonal and residual in registers, the
-// interior row is held once per thread, and the iterate and the rows of the
-// boundary nodes (the lattice's perimeter) are kept in shared memory behind the
-// two direction buffers.  Node (a, b) on the perimeter has row index a (b = 0), NX + a (b = NY-1),
-// 2 NX + b - 1 (a = 0) or 2 NX + NY - 2 + b - 1 (a = NX-1).
-template <class T>
-constexpr int coarse_cheb_wide_npt() {
-  return sizeof(T) == 4 ? 8 : 4;
-}
-
-template <class T>
-__device__ __forceinline__ int perimeter_row(int a, int b, int NX, int NY) {
-  if (b == 0) return a;
-  if (b == NY - 1) return NX + a;
-  if (a == 0) return 2 * NX + b - 1;
-  return 2 * NX + NY - 2 + b - 1;  // a == NX - 1
-}
-
-template <class T>
-__global__ void __launch_bounds__(kTailThreads)
-    k_coarse_cheb_wide(const CoarseChebDesc<T, 1>* __restrict__ D, const T* __restrict__ b, T* __restrict__ x_out) {
-  TOPO_PDL_ENTRY();
-  constexpr int NP = coarse_cheb_wide_npt<T>(), SW = StencilLayout<1>::stride;
-  extern __shared__ __align__(16) unsigned char cc_raw[];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int nn = D->nn, NX = D->NX, NY = nn / NX, nper = 2 * NX + 2 * (NY - 2);
-  T* d0 = reinterpret_cast<T*>(cc_raw);
-  T* d1 = d0 + nn;
-  T* xs = d1 + nn;    // the iterate and the residual (each node's own, kept here to spare registers)
-  T* rs = xs + nn;
-  T* prow = rs + nn;  // perimeter rows, 7 values each
-  const CoarseCheb<T>& C = D->C;
-  const T* __restrict__ sg = D->S.s;
-  for (int k = tid; k < nper * 7; k += nt) {
-    const int pr = k / 7, e = k - pr * 7;
-    int a, bb;
-    if (pr < NX) { a = pr; bb = 0; }
-    else if (pr < 2 * NX) { a = pr - NX; bb = NY - 1; }
-    else if (pr < 2 * NX + NY - 2) { a = 0; bb = pr - 2 * NX + 1; }
-    else { a = NX - 1; bb = pr - (2 * NX + NY - 2) + 1; }
-    prow[k] = sg[(size_t(bb) * NX + a) * SW + e];
-  }
-  T in[7];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) in[k] = D->S.inner[k];
-  T dv[NP];
-  int pi[NP];  // perimeter row index, or -1 for an interior node
-#pragma unroll
-  for (int q = 0; q < NP; ++q) {
-    const int n = tid + q * nt;
-    const bool on = n < nn;
-    const int bb = on ? n / NX : 1, a = on ? n - bb * NX : 1;
-    pi[q] = (on && (a == 0 || a == NX - 1 || bb == 0 || bb == NY - 1)) ? perimeter_row<T>(a, bb, NX, NY) : -1;
-    dv[q] = on ? D->dinv[n] : T(0);
-    if (on) {
-      const T rn = b[n];
-      rs[n] = rn;
-      d0[n] = C.c0 * dv[q] * rn;
-      xs[n] = T(0);
-    }
-  }
-  __syncthreads();
-  T* dc = d0;
-  T* dn = d1;
-  const int deg = C.deg;
-  for (int k = 0; k + 1 < deg; ++k) {
-    const T c1 = C.c1[k], c2 = C.c2[k];
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      const int n = tid + q * nt;
-      if (n < nn) {
-        const T dn0 = dc[n];
-        T t;
-        if (pi[q] >= 0) {  // a perimeter node: its own row (shared memory)
-          const T* row = prow + 7 * pi[q];
-          t = row[0] * dn0;
-#pragma unroll
-          for (int e = 1; e < 7; ++e) {
-            const int m = min(max(n + st_da(e) + st_db(e) * NX, 0), nn - 1);
-            t += row[e] * (dc[m] - dn0);
-          }
-        } else {  // interior: the shared row (registers), neighbours all inside the lattice
-          t = in[0] * dn0;
-#pragma unroll
-          for (int e = 1; e < 7; ++e) t += in[e] * (dc[n + st_da(e) + st_db(e) * NX] - dn0);
-        }
-        xs[n] += dn0;
-        const T rn = rs[n] - t;
-        rs[n] = rn;
-        dn[n] = c1 * dn0 + c2 * dv[q] * rn;
-      }
-    }
-    __syncthreads();
-    T* tmp = dc;
-    dc = dn;
-    dn = tmp;
-  }
-#pragma unroll
-  for (int q = 0; q < NP; ++q) {
-    const int n = tid + q * nt;
-    if (n < nn) x_out[n] = xs[n] + dc[n];
-  }
-}
-
 // ---------------------------------------------------------------------------
 // host helpers
 // ---------------------------------------------------------------------------
@@ -1128,11 +1022,8 @@ void MG<T>::select_coarse_cheb() {
   for (int l = 1; use_coarse_cheb && cc_buf_ && l < L; ++l) {
     const LevelSpec& S = specs_[l];
     if (S.p2 || S.NC != 1 || !lv_[l].st || !kK64_[l] || !kM64_[l]) continue;
-    // the two direction buffers (and, for the wide kernel, the perimeter rows)
-    const bool wide = use_cheb_wide && lv_[l].inner && S.nn() > size_t(kTailThreads) * coarse_cheb_npt<T>() &&
-                      S.nn() <= size_t(kTailThreads) * coarse_cheb_wide_npt<T>() && S.NX >= 3 && S.NY >= 3;
-    const size_t smem = (2 * S.nn() + (wide ? 2 * S.nn() + 7 * size_t(2 * S.NX + 2 * (S.NY - 2)) : 0)) * sizeof(T);
-    if ((!wide && S.nn() > size_t(kTailThreads) * coarse_cheb_npt<T>()) || smem > kTailSmemBudget) continue;
+    const size_t smem = 2 * S.nn() * sizeof(T);  // the two direction buffers
+    if (S.nn() > size_t(kTailThreads) * coarse_cheb_npt<T>() || smem > kTailSmemBudget) continue;
     const size_t nt = S.ntri();
     std::vector<double> kk(nt), km(nt);
     if (cudaMemcpy(kk.data(), kK64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
@@ -1155,7 +1046,7 @@ void MG<T>::select_coarse_cheb() {
     if (deg > coarse_cheb_max_degree || deg > kCoarseChebMax) continue;
     CoarseChebDesc<T, 1> h;
     std::memset(&h, 0, sizeof(h));
-    h.S = P1Stencil<T, 1>{S.nx, S.ny, S.dir, lv_[l].st, wide ? lv_[l].inner : nullptr};
+    h.S = P1Stencil<T, 1>{S.nx, S.ny, S.dir, lv_[l].st};
     h.dinv = lv_[l].dinv;
     h.NX = S.NX;
     h.nn = int(S.nn());
@@ -1169,16 +1060,13 @@ void MG<T>::select_coarse_cheb() {
     }
     const int limit = int(kTailSmemBudget);
     if (cudaMemcpy(cc_buf_, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaFuncSetAttribute(k_coarse_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess ||
-        cudaFuncSetAttribute(k_coarse_cheb_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) !=
-            cudaSuccess) {
+        cudaFuncSetAttribute(k_coarse_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
     cheb_coarse_ = l;
     cc_desc_ = cc_buf_;
     cc_smem_ = smem;
-    cc_wide_ = wide;
     coarse_cheb_deg = deg;
     break;
   }
@@ -1453,8 +1341,8 @@ int MG<T>::setup(cudaStream_t s) {
   cudaStreamWaitEvent(s, ev_[1], 0);
   if (!cc_selected_) {  // the coefficients of a hierarchy with a mass term do not change
     cudaStreamSynchronize(s);
-    detect_uniform_levels();  // (the wide coarse solve needs the shared interior rows)
     select_coarse_cheb();
+    detect_uniform_levels();
     cc_selected_ = true;
   }
   for (int l = 1; l + 1 < L; ++l) bounds(l);
@@ -1528,12 +1416,7 @@ void MG<T>::vcycle_level_body(int l, const T* b, T* x, cudaStream_t s) {
   const LevelSpec& S = specs_[l];
   if (l == cheb_coarse_ && cc_desc_) {
     KClock kc(s, "coarse Chebyshev (one CTA)", l, 0.0);
-    if (cc_wide_)
-      launch_pdl(k_coarse_cheb_wide<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_),
-                 b, x);
-    else
-      launch_pdl(k_coarse_cheb<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b,
-                 x);
+    launch_pdl(k_coarse_cheb<T>, 1, kTailThreads, cc_smem_, s, static_cast<const CoarseChebDesc<T, 1>*>(cc_desc_), b, x);
     ++launches;
     return;
   }
