@@ -123,15 +123,6 @@ TOPO_HD T half_of(T x) {
   else return T(0.5) * x;
 }
 
-// a - b with both parts' sums made exact (the IEEE-style addition): the error is
-// bounded relative to the result, so the difference of two nearby values (the
-// difference form's u_k - u_A) keeps about 48 bits of the difference itself
-TOPO_HD dd sub_accurate(dd a, dd b) {
-  dd s = two_sum(a.hi, -b.hi);
-  const dd t = two_sum(a.lo, -b.lo);
-  s = fast_two_sum(s.hi, ddop::add(s.lo, t.hi));
-  return fast_two_sum(s.hi, ddop::add(s.lo, t.lo));
-}
 TOPO_HD dd& operator+=(dd& a, dd b) { return a = a + b; }
 TOPO_HD dd& operator-=(dd& a, dd b) { return a = a - b; }
 TOPO_HD dd& operator*=(dd& a, dd b) { return a = a * b; }
