@@ -60,11 +60,14 @@ __global__ void k_cell_rmass(int nx, int ny, Penal<double> pen, const double* __
   TOPO_GRID_STRIDE(c, nc) cell_rmass<T>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
 }
 
-// the FP32 operator's own r-weighted mass matrices (same arithmetic as its
-// on-the-fly evaluation, so reading them instead changes no result)
-__global__ void k_cell_rmass32(int nx, int ny, Penal<float> pen, const float* __restrict__ xi, float* __restrict__ out) {
+// the FP32 operator's and its preconditioner's own r-weighted mass matrices, one
+// pass (same arithmetic as their on-the-fly evaluation, so reading them instead
+// changes no result)
+__global__ void k_cell_rmass32(int nx, int ny, Penal<float> pen_op, Penal<float> pen_pc,
+                               const float* __restrict__ xi, float* __restrict__ out_op,
+                               float* __restrict__ out_pc) {
   const size_t nc = size_t(nx) * ny;
-  TOPO_GRID_STRIDE(c, nc) cell_rmass<float>(int(c % nx), int(c / nx), nx, ny, xi, pen, out);
+  TOPO_GRID_STRIDE(c, nc) cell_rmass_pair<float>(int(c % nx), int(c / nx), nx, xi, pen_op, pen_pc, out_op, out_pc);
 }
 
 // kappa of state level 1 and the residual operator's mass matrices (RM: FP64, or
@@ -728,11 +731,10 @@ int state_setup(topo_ctx* C, const double* xi, cudaStream_t s) {
     // of seven r(xi) evaluations per triangle per apply (TOPO_RMASS32=0: on the fly)
     k_convert<float, double><<<C->grid(C->nv), kVecThreads, 0, s>>>(C->xi32, xi, 1.0, C->nv);
     if (C->rm_op32) {
-      k_cell_rmass32<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, C->p2params<float>(0).pen, C->xi32,
-                                                             C->rm_op32);
-      k_cell_rmass32<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, C->p2params<float>(1).pen, C->xi32,
+      k_cell_rmass32<<<C->grid(ncell), kVecThreads, 0, s>>>(C->nx, C->ny, C->p2params<float>(0).pen,
+                                                             C->p2params<float>(1).pen, C->xi32, C->rm_op32,
                                                              C->rm_pc32);
-      C->launches += 2;
+      C->launches += 1;
     }
     C->smg32.set_p2(C->p2params<float>(0, C->rm_op32), C->p2params<float>(1, C->rm_pc32), C->xi32);
     st = C->smg32.setup(s);

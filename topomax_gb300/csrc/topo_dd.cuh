@@ -98,6 +98,32 @@ TOPO_HD dd operator*(dd a, dd b) {
   e = ddop::fma(a.lo, b.hi, e);
   return fast_two_sum(p, e);
 }
+// a0 b0 + a1 b1 + a2 b2 with one renormalisation: the three hi products exact
+// (TwoProd), their cross terms and rounding errors summed in float, the hi parts
+// by two TwoSums.  31 FP32 operations instead of 43 for three products and two
+// sums, the error again bounded relative to sum |a_i b_i|.  Float and double keep
+// their expression unchanged.
+template <class T>
+TOPO_HD T dot3(T a0, T b0, T a1, T b1, T a2, T b2) {
+  if constexpr (IsDD<T>::value) {
+    const float p0 = ddop::mul(a0.hi, b0.hi), p1 = ddop::mul(a1.hi, b1.hi), p2 = ddop::mul(a2.hi, b2.hi);
+    float e = ddop::fma(a0.hi, b0.hi, -p0);
+    e = ddop::fma(a0.hi, b0.lo, e);
+    e = ddop::fma(a0.lo, b0.hi, e);
+    e = ddop::add(e, ddop::fma(a1.hi, b1.hi, -p1));
+    e = ddop::fma(a1.hi, b1.lo, e);
+    e = ddop::fma(a1.lo, b1.hi, e);
+    e = ddop::add(e, ddop::fma(a2.hi, b2.hi, -p2));
+    e = ddop::fma(a2.hi, b2.lo, e);
+    e = ddop::fma(a2.lo, b2.hi, e);
+    const dd s1 = two_sum(p0, p1);
+    const dd s2 = two_sum(s1.hi, p2);
+    return fast_two_sum(s2.hi, ddop::add(ddop::add(s1.lo, s2.lo), e));
+  } else {
+    return a0 * b0 + a1 * b1 + a2 * b2;
+  }
+}
+
 // K x for a small integer constant K, written so that the float and double
 // operators keep their exact arithmetic (T(K) * x) and the pair type takes the
 // cheap exact forms: a power of two scales both parts, 3 is one TwoProd.

@@ -108,6 +108,34 @@ TOPO_HD void tri_rmass(const T (&xi)[3], const Penal<T>& pen, T (&M)[6]) {
   }
 }
 
+// tri_rmass for two penalisations of the same design in one pass (the FP32
+// operator's and its preconditioner's, which differ only in the clamp): each
+// matrix with exactly the arithmetic of tri_rmass.
+template <class T>
+TOPO_HD void tri_rmass_pair(const T (&xi)[3], const Penal<T>& pa, const Penal<T>& pb, T (&Ma)[6], T (&Mb)[6]) {
+  for (int k = 0; k < 6; ++k) Ma[k] = Mb[k] = T(0);
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int q = 0; q < Rule7::n; ++q) {
+    const T l0 = T(Rule7::lam(q, 0)), l1 = T(Rule7::lam(q, 1)), l2 = T(Rule7::lam(q, 2));
+    const T x = l0 * xi[0] + l1 * xi[1] + l2 * xi[2];
+    const T wa = T(Rule7::w(q)) * pa.r(x), wb = T(Rule7::w(q)) * pb.r(x);
+    Ma[0] += wa * (l0 * l0);
+    Ma[1] += wa * (l1 * l1);
+    Ma[2] += wa * (l2 * l2);
+    Ma[3] += wa * (l0 * l1);
+    Ma[4] += wa * (l0 * l2);
+    Ma[5] += wa * (l1 * l2);
+    Mb[0] += wb * (l0 * l0);
+    Mb[1] += wb * (l1 * l1);
+    Mb[2] += wb * (l2 * l2);
+    Mb[3] += wb * (l0 * l1);
+    Mb[4] += wb * (l0 * l2);
+    Mb[5] += wb * (l1 * l2);
+  }
+}
+
 // S * g_I for symmetric S = (xx, yy, xy); g in units of (ihx, ihy).
 template <int O, int I, class T>
 TOPO_HD void sg(const T (&s)[3], T ihx, T ihy, T& ox, T& oy) {
@@ -168,9 +196,9 @@ TOPO_HD void tri_apply_m(const T (&u)[6][2], const T (&M)[6], const P2Params<T>&
 #pragma unroll
 #endif
   for (int c = 0; c < 3; ++c) {
-    S[0][c] = M[0] * sig[0][c] + M[3] * sig[1][c] + M[4] * sig[2][c];
-    S[1][c] = M[3] * sig[0][c] + M[1] * sig[1][c] + M[5] * sig[2][c];
-    S[2][c] = M[4] * sig[0][c] + M[5] * sig[1][c] + M[2] * sig[2][c];
+    S[0][c] = dot3(M[0], sig[0][c], M[3], sig[1][c], M[4], sig[2][c]);
+    S[1][c] = dot3(M[3], sig[0][c], M[1], sig[1][c], M[5], sig[2][c]);
+    S[2][c] = dot3(M[4], sig[0][c], M[5], sig[1][c], M[2], sig[2][c]);
   }
   // vertex nodes: (4 S_i - sum S) g_i
   T Q[3][3];
@@ -810,6 +838,27 @@ TOPO_HD void cell_rmass(int i, int j, int nx, int ny, const TC* xi, const Penal<
     TC M[6];
     tri_rmass(xe, pen, M);
     for (int k = 0; k < 6; ++k) out[c * 12 + o * 6 + k] = T(M[k]);
+  }
+}
+
+// cell_rmass for two penalisations in one pass (tri_rmass_pair)
+template <class T>
+TOPO_HD void cell_rmass_pair(int i, int j, int nx, const T* xi, const Penal<T>& pa, const Penal<T>& pb, T* outa,
+                             T* outb) {
+  const size_t c = size_t(j) * nx + i;
+  const int VX = nx + 1;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int o = 0; o < 2; ++o) {
+    T xe[3];
+    for (int k = 0; k < 3; ++k) xe[k] = xi[size_t(j + p1_off_b(o, k)) * VX + i + p1_off_a(o, k)];
+    T Ma[6], Mb[6];
+    tri_rmass_pair(xe, pa, pb, Ma, Mb);
+    for (int k = 0; k < 6; ++k) {
+      outa[c * 12 + o * 6 + k] = Ma[k];
+      outb[c * 12 + o * 6 + k] = Mb[k];
+    }
   }
 }
 
