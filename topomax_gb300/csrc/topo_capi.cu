@@ -110,11 +110,20 @@ __global__ void k_emd_half(const double* __restrict__ psi_prev, const double* __
 
 // One Newton step of  F(c) = int expit(half + c) - volume = 0  (src/solver.py:149-186,
 // scipy newton semantics: stop when |c_new - c| < tol).
-// warm-start guess from a solution history x1 (last), x2, x3: order 1 the linear
-// extrapolation 2 x1 - x2, order 2 the quadratic 3 (x1 - x2) + x3
-__global__ void k_extrapolate(double* __restrict__ y, const double* __restrict__ x1, const double* __restrict__ x2,
-                              const double* __restrict__ x3, size_t n, int order) {
-  TOPO_GRID_STRIDE(i, n) y[i] = order == 1 ? 2.0 * x1[i] - x2[i] : 3.0 * (x1[i] - x2[i]) + x3[i];
+// warm-start guess from a solution history x_0 (last), x_1, ...: y = sum_i c_i x_i (the
+// polynomial extrapolation's weights, see topo_ctx::fwarm)
+constexpr int kMaxExtrapolate = 4;
+struct Extrapolation {
+  const double* x[kMaxExtrapolate + 1];
+  double c[kMaxExtrapolate + 1];
+  int n;
+};
+__global__ void k_extrapolate(double* __restrict__ y, Extrapolation ex, size_t n) {
+  TOPO_GRID_STRIDE(i, n) {
+    double v = ex.c[0] * ex.x[0][i];
+    for (int k = 1; k < ex.n; ++k) v += ex.c[k] * ex.x[k][i];
+    y[i] = v;
+  }
 }
 
 // expit(half + c) = 1 / (1 + exp(-half) exp(-c)): with exp(-half) evaluated once per
@@ -267,14 +276,13 @@ struct topo_ctx {
   // the filter solves of a mixed-precision context: FP32 multigrid CG inside FP64 FGMRES
   // (true) or FP64 multigrid CG (false, TOPO_FILTER_FP64=1); FP64 contexts always use FP64
   bool filter_mixed = false;
-  double* fwarm[2] = {nullptr, nullptr};
-  // the two solutions before the last one: with them the next guess is the linear
-  // (2 x1 - x2) or quadratic (3 x1 - 3 x2 + x3) extrapolation over the design iterations
-  // (TOPO_EXTRAPOLATE: 0 keeps the last, 1 linear, 2 quadratic, the default)
-  double* fwarm_prev[2] = {nullptr, nullptr};
-  double* fwarm_prev2[2] = {nullptr, nullptr};
-  int fwarm_hist[2] = {0, 0};  // solutions held: last, previous, the one before (0..3)
-  int extrapolate = 2;
+  // each channel's last solutions, newest first (kMaxExtrapolate + 1 buffers): the next
+  // guess is their polynomial extrapolation over the design iterations,
+  //   sum_i (-1)^i binom(order + 1, i + 1) x_i   (2 x1 - x2 for order 1)
+  // (TOPO_EXTRAPOLATE: 0 keeps the last solution, 1 linear, ... 4; default 3)
+  double* fwarm[2][kMaxExtrapolate + 1] = {};
+  int fwarm_hist[2] = {0, 0};  // solutions held (0 .. kMaxExtrapolate + 1)
+  int extrapolate = 3;
   double* fr64 = nullptr;
   double* fy64 = nullptr;
   float* fd32 = nullptr;
@@ -439,13 +447,10 @@ int init_filter(topo_ctx* C, double eps) {
   C->fb64 = C->arena.alloc_n<double>(C->nv);
   C->fr64 = C->arena.alloc_n<double>(C->nv);
   C->fy64 = C->arena.alloc_n<double>(C->nv);
-  C->fwarm[0] = C->arena.alloc_n<double>(C->nv);
-  C->fwarm[1] = C->arena.alloc_n<double>(C->nv);
-  for (int k = 0; k < 2; ++k) {
-    C->fwarm_prev[k] = C->arena.alloc_n<double>(C->nv);
-    C->fwarm_prev2[k] = C->arena.alloc_n<double>(C->nv);
-  }
-  if (const char* e = std::getenv("TOPO_EXTRAPOLATE")) C->extrapolate = std::max(0, std::min(2, std::atoi(e)));
+  for (int k = 0; k < 2; ++k)
+    for (int i = 0; i <= kMaxExtrapolate; ++i) C->fwarm[k][i] = C->arena.alloc_n<double>(C->nv);
+  if (const char* e = std::getenv("TOPO_EXTRAPOLATE"))
+    C->extrapolate = std::max(0, std::min(kMaxExtrapolate, std::atoi(e)));
   int st;
   C->filter_mixed = C->precision == TOPO_PREC_MIXED && !env_flag("TOPO_FILTER_FP64", false);
   if (C->filter_mixed) {
@@ -668,11 +673,18 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   if (warm) {
     const int order = std::min(C->extrapolate, hist - 1);
     if (order > 0) {
-      k_extrapolate<<<C->grid(C->nv), kVecThreads, 0, s>>>(xi, C->fwarm[channel], C->fwarm_prev[channel],
-                                                          C->fwarm_prev2[channel], C->nv, order);
+      Extrapolation ex{};
+      ex.n = order + 1;
+      double binom = 1.0;  // binom(order + 1, i + 1), built up term by term
+      for (int i = 0; i <= order; ++i) {
+        binom = binom * double(order + 1 - i) / double(i + 1);
+        ex.x[i] = C->fwarm[channel][i];
+        ex.c[i] = (i % 2 ? -1.0 : 1.0) * binom;
+      }
+      k_extrapolate<<<C->grid(C->nv), kVecThreads, 0, s>>>(xi, ex, C->nv);
       C->launches += 1;
     } else {
-      cudaMemcpyAsync(xi, C->fwarm[channel], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(xi, C->fwarm[channel][0], C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
     }
   }
   if (channel >= 0) C->fwarm_hist[channel] = 0;  // until this solve succeeds
@@ -689,11 +701,13 @@ int filter_solve_impl(topo_ctx* C, const double* b, double* xi, double rtol, int
   if (iters) *iters = st.iterations;
   if (rc) return rc;
   if (C->filter_warm && channel >= 0) {
-    // shift the history: the one before <- previous <- last <- this solution
-    std::swap(C->fwarm_prev2[channel], C->fwarm_prev[channel]);
-    std::swap(C->fwarm_prev[channel], C->fwarm[channel]);
-    cudaMemcpyAsync(C->fwarm[channel], xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    C->fwarm_hist[channel] = std::min(3, hist + 1);
+    // shift the history by one (the oldest buffer takes this solution)
+    double** h = C->fwarm[channel];
+    double* oldest = h[kMaxExtrapolate];
+    for (int i = kMaxExtrapolate; i > 0; --i) h[i] = h[i - 1];
+    h[0] = oldest;
+    cudaMemcpyAsync(h[0], xi, C->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    C->fwarm_hist[channel] = std::min(kMaxExtrapolate + 1, hist + 1);
   }
   return C->cuda_check("filter solve");
 }

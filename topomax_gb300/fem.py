@@ -25,6 +25,7 @@ reads them; "lattice" is the device order.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import pickle
 
@@ -400,11 +401,12 @@ class ElasticityProblem(Problem):
         self.lamé_mu = self.Young_modulus / (2 * (1 + self.Poisson_ratio))
         self.lamé_lda = self.lamé_mu * self.Poisson_ratio / (0.5 - self.Poisson_ratio)
         self.u: Function | None = None
-        self._u_prev: Function | None = None
-        self._u_prev2: Function | None = None
-        # warm-start guess from the last solutions: 0 the last one, 1 linear, 2 quadratic
-        # extrapolation over the design iterations (TOPO_EXTRAPOLATE; the default is 2)
-        self.extrapolate_order = int(os.environ.get("TOPO_EXTRAPOLATE", "2"))
+        # the state's solution history, newest first (warm-start extrapolation)
+        self._u_hist: list = []
+        # warm-start guess from the last solutions: 0 the last one, else the polynomial
+        # extrapolation of that order (1 linear .. 4) over the design iterations
+        # (TOPO_EXTRAPOLATE; the default is 3, cubic)
+        self.extrapolate_order = max(0, min(4, int(os.environ.get("TOPO_EXTRAPOLATE", "3"))))
         self.extrapolate = self.extrapolate_order > 0
         self.filtered_rho: Function | None = None
         self.stats = {"state_iterations": 0, "filter_iterations": 0}
@@ -483,20 +485,20 @@ class ElasticityProblem(Problem):
         flags = 0
         if self.warm_start and self.u is not None:
             u.tensor.copy_(self.u.tensor)
-            if self.extrapolate and self._u_prev is not None:
-                if self.extrapolate_order == 2 and self._u_prev2 is not None:
-                    # 3 u_k - 3 u_(k-1) + u_(k-2)
-                    u.tensor.sub_(self._u_prev.tensor).mul_(3.0).add_(self._u_prev2.tensor)
-                else:
-                    # the design moves a little each iteration: 2 u_k - u_(k-1) starts the solve closer
-                    u.tensor.mul_(2.0).sub_(self._u_prev.tensor)
+            order = min(self.extrapolate_order, len(self._u_hist) - 1) if self.extrapolate else 0
+            if order > 0:
+                # the design moves a little each iteration: the solve starts from the polynomial
+                # extrapolation of the last order + 1 solutions,
+                #   sum_i (-1)^i binom(order + 1, i + 1) u_(k-i)   (2 u_k - u_(k-1) for order 1)
+                u.tensor.mul_(float(math.comb(order + 1, 1)))
+                for i in range(1, order + 1):
+                    u.tensor.add_(self._u_hist[i].tensor, alpha=float((-1) ** i * math.comb(order + 1, i + 1)))
             flags = _capi.SOLVE_WARM
         it = ctypes.c_int(0)
         self._ctx.check(self._ctx._lib.topo_state_solve(self._ctx.ptr, _ptr(xi), _ptr(u.tensor), self.rtol, flags,
                                                         ctypes.byref(it), _stream()))
         self.stats["state_iterations"] += it.value
-        self._u_prev2 = self._u_prev
-        self._u_prev = self.u
+        self._u_hist = ([u] + self._u_hist)[:self.extrapolate_order + 1]
         return u
 
     # -- extras ---------------------------------------------------------------
