@@ -875,6 +875,10 @@ topo_ctx* topo_create(const topo_grid_desc* grid, const topo_material* mat, cons
       if (C->arena.failed()) rc = C->fail(TOPO_ERR_CUDA, "out of device memory");
     }
     if (!rc) rc = init_filter(C, mat->filter_radius);
+    if (!rc) {
+      const cudaError_t e = settle_setup_stream();
+      if (e != cudaSuccess) rc = C->fail(TOPO_ERR_CUDA, "set-up: %s", cudaGetErrorString(e));
+    }
   } catch (...) {
     rc = TOPO_ERR_CUDA;
   }
@@ -899,6 +903,10 @@ topo_ctx* topo_create_filter(const topo_grid_desc* grid, double epsilon, int pre
     rc = init_common(C, grid, precision);
     if (!rc && !(epsilon >= 0)) rc = C->fail(TOPO_ERR_ARG, "invalid filter radius");
     if (!rc) rc = init_filter(C, epsilon);
+    if (!rc) {
+      const cudaError_t e = settle_setup_stream();
+      if (e != cudaSuccess) rc = C->fail(TOPO_ERR_CUDA, "set-up: %s", cudaGetErrorString(e));
+    }
   } catch (...) {
     rc = TOPO_ERR_CUDA;
   }

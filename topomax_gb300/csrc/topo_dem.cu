@@ -299,7 +299,8 @@ int upload(topo_dem_ctx* C, float*& dst, const float* host) {
     return C->cuda_check("clear");
   }
   if (!dst && cudaMalloc(&dst, n * sizeof(float)) != cudaSuccess) return C->fail(TOPO_ERR_CUDA, "out of device memory");
-  if (cudaMemcpy(dst, host, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (cudaMemcpy(dst, host, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      settle_setup_stream() != cudaSuccess)
     return C->fail(TOPO_ERR_CUDA, "copy failed");
   return TOPO_OK;
 }
@@ -477,7 +478,7 @@ topo_dem_ctx* topo_dem_create(const topo_dem_desc* desc, int* status) {
   C->blocks = C->sms * 8;
   if (cudaMalloc(&C->partials, size_t(C->blocks) * 2 * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&C->counter, sizeof(unsigned)) != cudaSuccess ||
-      cudaMemset(C->counter, 0, sizeof(unsigned)) != cudaSuccess) {
+      cudaMemset(C->counter, 0, sizeof(unsigned)) != cudaSuccess || settle_setup_stream() != cudaSuccess) {
     cudaGetLastError();
     delete C;
     set(TOPO_ERR_CUDA);

@@ -607,6 +607,10 @@ topo_fluid_ctx* topo_fluid_create(const topo_grid_desc* grid, double viscosity, 
   try {
     C = new topo_fluid_ctx();
     rc = fluid_init(C, grid, viscosity, flows, n_flows);
+    if (!rc) {
+      const cudaError_t e = settle_setup_stream();
+      if (e != cudaSuccess) rc = C->fail(TOPO_ERR_CUDA, "set-up: %s", cudaGetErrorString(e));
+    }
   } catch (...) {
     rc = TOPO_ERR_CUDA;
   }

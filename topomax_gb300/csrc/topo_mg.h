@@ -46,6 +46,13 @@ class Arena {
 // set-up and the recordings themselves.
 std::recursive_mutex& device_lock();
 
+// Context set-up writes device memory on the default stream: Arena::alloc zeroes
+// with cudaMemset, host tables go up with pageable cudaMemcpy (which may return
+// before its DMA lands), and set-up kernels launch without a stream.  A caller's
+// stream created non-blocking (every torch stream is) is not ordered after that
+// work, so a context is handed out only after the default stream has drained.
+inline cudaError_t settle_setup_stream() { return cudaStreamSynchronize(0); }
+
 struct LevelSpec {
   bool p2 = false;  // P2 elasticity level (only level 0 of the state hierarchy)
   int nx = 0, ny = 0;
