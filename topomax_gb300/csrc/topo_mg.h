@@ -256,8 +256,8 @@ class MG {
   int cheb_coarse_ = -1;
   void* cc_desc_ = nullptr;
   size_t cc_smem_ = 0;
-  void select_coarse_cheb();
-  void detect_uniform_levels();  // sets Lev::inner where every interior row is the same
+  void select_coarse_cheb(cudaStream_t s);
+  void detect_uniform_levels(cudaStream_t s);  // sets Lev::inner where every interior row is the same
   void* cc_buf_ = nullptr;
   T* inner_buf_ = nullptr;  // per level: one stencil row (detect_uniform_levels)
   bool cc_selected_ = false;

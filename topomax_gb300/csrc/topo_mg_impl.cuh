@@ -976,7 +976,7 @@ void MG<T>::init(const std::vector<LevelSpec>& specs, const ElemRefs* refs, doub
 // row at every interior node (constant coefficients on the uniform lattice,
 // checked on the rows themselves) read that row once instead of per node.
 template <class T>
-void MG<T>::detect_uniform_levels() {
+void MG<T>::detect_uniform_levels(cudaStream_t s) {
   const int L = levels();
   for (int l = 0; l < L; ++l) {
     const LevelSpec& S = specs_[l];
@@ -987,7 +987,8 @@ void MG<T>::detect_uniform_levels() {
     if (d.x_lo || d.y_lo || d.npts || d.x_hi_from < S.NX || d.y_hi_from < S.NY || S.NX < 3 || S.NY < 3) continue;
     constexpr int SW = StencilLayout<1>::stride;
     std::vector<T> st(S.nn() * SW);
-    if (cudaMemcpy(st.data(), v.st, st.size() * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (cudaMemcpyAsync(st.data(), v.st, st.size() * sizeof(T), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
@@ -998,7 +999,9 @@ void MG<T>::detect_uniform_levels() {
         same = std::memcmp(st.data() + (size_t(b) * S.NX + a) * SW, ref, SW * sizeof(T)) == 0;
     if (!same) continue;
     T* dst = inner_buf_ + size_t(l) * SW;
-    if (cudaMemcpy(dst, ref, SW * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+    // on s: the kernels that read the row run there (a pageable copy is staged before
+    // the call returns, so `st` may go out of scope)
+    if (cudaMemcpyAsync(dst, ref, SW * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
@@ -1013,7 +1016,7 @@ void MG<T>::detect_uniform_levels() {
 // of the level's triangles -- needs at most coarse_cheb_max_degree steps for
 // a residual reduction of 1e-2.  Levels past it are no longer visited.
 template <class T>
-void MG<T>::select_coarse_cheb() {
+void MG<T>::select_coarse_cheb(cudaStream_t s) {
   const int prev = cheb_coarse_;
   cheb_coarse_ = -1;
   cc_desc_ = nullptr;
@@ -1026,8 +1029,9 @@ void MG<T>::select_coarse_cheb() {
     if (S.nn() > size_t(kTailThreads) * coarse_cheb_npt<T>() || smem > kTailSmemBudget) continue;
     const size_t nt = S.ntri();
     std::vector<double> kk(nt), km(nt);
-    if (cudaMemcpy(kk.data(), kK64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(km.data(), kM64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (cudaMemcpyAsync(kk.data(), kK64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(km.data(), kM64_[l], nt * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
@@ -1059,7 +1063,7 @@ void MG<T>::select_coarse_cheb() {
       h.C.c2[k] = T(c2[k]);
     }
     const int limit = int(kTailSmemBudget);
-    if (cudaMemcpy(cc_buf_, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess ||
+    if (cudaMemcpyAsync(cc_buf_, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaFuncSetAttribute(k_coarse_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit) != cudaSuccess) {
       cudaGetLastError();
       return;
@@ -1341,8 +1345,8 @@ int MG<T>::setup(cudaStream_t s) {
   cudaStreamWaitEvent(s, ev_[1], 0);
   if (!cc_selected_) {  // the coefficients of a hierarchy with a mass term do not change
     cudaStreamSynchronize(s);
-    select_coarse_cheb();
-    detect_uniform_levels();
+    select_coarse_cheb(s);
+    detect_uniform_levels(s);
     cc_selected_ = true;
   }
   for (int l = 1; l + 1 < L; ++l) bounds(l);
