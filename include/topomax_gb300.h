@@ -17,7 +17,9 @@
  *   - return 0 on success, a negative TOPO_ERR_* code otherwise; the message
  *     of the last failure is available from topo_last_error();
  *   - a context is not thread-safe: use one host thread and one stream per
- *     context.
+ *     context;
+ *   - the create functions finish their device set-up before they return, so
+ *     the first call may use any stream, blocking or not.
  *
  * Each entry point names the reference interface (Emilinya/topomax) it
  * replaces.
