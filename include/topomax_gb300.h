@@ -112,8 +112,9 @@ int topo_set_penalization(topo_ctx* ctx, double p);
  * stored solutions): topo_filter_apply starts from the solution of the previous
  * topo_filter_apply on this context, topo_sensitivity from the previous topo_sensitivity's
  * (extrapolated over the design iterations once more solutions exist: 2 x1 - x2 from two,
- * 3 x1 - 3 x2 + x3 from three; environment TOPO_EXTRAPOLATE at context creation: 0 keeps x1,
- * 1 linear, 2 quadratic, the default); a failed solve is not reused.  Between design iterations both right-hand sides change little,
+ * 3 x1 - 3 x2 + x3 from three, 4 x1 - 6 x2 + 4 x3 - x4 from four; environment
+ * TOPO_EXTRAPOLATE at context creation: 0 keeps x1, 1 linear ... 4 quartic, 3 cubic the
+ * default); a failed solve is not reused.  Between design iterations both right-hand sides change little,
  * so a solve to the same rtol takes fewer iterations.  No counterpart in the reference, whose
  * HelmholtzFilter (FEM_src/filter.py:40-41) factorises and solves directly. */
 int topo_set_filter_warm_start(topo_ctx* ctx, int enable);
@@ -169,6 +170,17 @@ int topo_emd_finish(topo_ctx* ctx, const double* psi, const double* psi_prev, do
 
 /* *out = int f dx for a CG1 field: replaces FEMSolver.integrate (FEM_src/solver.py:81-84). */
 int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t stream);
+
+/* Starting point of a warm-started state solve from the last `count` solutions
+ * (history[0] the newest, 1 <= count <= 5), in one pass:
+ *   u = sum_i (-1)^i binom(count, i + 1) history[i],
+ * the polynomial extrapolation of degree count - 1 over the design iterations (count 1
+ * copies history[0]).  The reference solves each state directly
+ * (FEM_src/elasisity_problem.py:168-169); this only supplies the iterative solve's
+ * first iterate (topo_state_solve with TOPO_SOLVE_WARM).  u and every history entry
+ * hold n_dofs doubles (topo_sizes); history is a host array of device pointers. */
+int topo_state_warm_start(topo_ctx* ctx, const double* const* history, int count, double* u,
+                          topo_stream_t stream);
 
 /* y = K(xi) u in FP64 with clamped rows/columns as identity (test hook: the operator of
  * FEM_src/elasisity_problem.py:104-132 after bc.apply).  u and y 16-byte aligned. */

@@ -5,6 +5,9 @@ body force, p in {3, 4, 5}, random volume fraction and step size) runs through
 concurrent workers; every design's history must equal its single-design run,
 and one design is checked against the FP64 oracle's design loop.
 """
+import threading
+import time
+
 import numpy as np
 import pytest
 
@@ -57,3 +60,46 @@ def test_batch_matches_single_runs_and_oracle():
     assert n >= 2
     rel = max(abs(a - b) / abs(b) for a, b in zip(got[:n], run.objectives[:n]))
     assert rel <= 1e-6
+
+
+def test_contexts_created_while_the_default_stream_is_busy():
+    """Context set-up writes device memory on the default stream (arena zeroing, host
+    tables, the filter's stencils), and batch workers call on non-blocking streams that
+    are not ordered after it.  The create call returns only when that work is done, so
+    filters created and applied at once on a non-blocking stream, while another thread
+    keeps the default stream busy with bounded sleep kernels, equal one made on a quiet
+    device."""
+    import torch
+    import topomax_gb300 as tg
+    mesh = tg.RectangleMesh(2.0, 1.0, 200, 100)
+    V = tg.FunctionSpace(mesh, "CG", 1, dof_order="lattice")
+    rho = np.random.default_rng(5).uniform(0, 1, V.dim())
+    ref = tg.HelmholtzFilter(0.05, V, precision="mixed", rtol=1e-10).apply(rho).vector()[:]
+    torch.cuda.synchronize()
+    stop = threading.Event()
+
+    def busy():
+        # about 1 ms per sleep kernel at this GPU's clocks, at most two queued, for at most 5 s
+        default = torch.cuda.default_stream()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(default):
+            while not stop.is_set() and time.perf_counter() - t0 < 5.0:
+                torch.cuda._sleep(2_000_000)
+                torch.cuda._sleep(2_000_000)
+                default.synchronize()
+
+    t = threading.Thread(target=busy)
+    t.start()
+    try:
+        side = torch.cuda.Stream()
+        got = []
+        with torch.cuda.stream(side):
+            for _ in range(4):
+                f = tg.HelmholtzFilter(0.05, V, precision="mixed", rtol=1e-10)
+                got.append(f.apply(rho).vector()[:])
+                del f
+    finally:
+        stop.set()
+        t.join()
+    for g in got:
+        assert np.max(np.abs(g - ref)) <= 1e-12 * np.max(np.abs(ref))

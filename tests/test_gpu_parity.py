@@ -432,3 +432,28 @@ def test_design_loop_parity_at_320x160():
     assert len(objs) == len(robjs) == 3
     assert np.max(np.abs(objs - robjs) / np.abs(robjs)) <= 1e-6
     assert np.max(np.abs(s.rho.tensor.cpu().numpy() - ref.rho)) <= 1e-5
+
+
+def test_state_warm_start_extrapolation():
+    """topo_state_warm_start: u = sum_i (-1)^i binom(count, i + 1) h_i in one pass (count 1
+    copies h_0); a history longer than five or a null entry is refused."""
+    import ctypes
+    import math
+    import torch
+    from topomax_gb300 import _capi
+    prob, V = _gpu_problem(_design(), 40, 20)
+    ctx = prob._ctx
+    n = int(prob.solution_space.dim())
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    hist = [torch.rand(n, dtype=torch.float64, device="cuda", generator=gen) for _ in range(6)]
+    u = torch.empty(n, dtype=torch.float64, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for count in range(1, 6):
+        ptrs = (ctypes.c_void_p * count)(*[h.data_ptr() for h in hist[:count]])
+        ctx.check(ctx._lib.topo_state_warm_start(ctx.ptr, ptrs, count, ctypes.c_void_p(u.data_ptr()), stream))
+        ref = sum((-1) ** i * math.comb(count, i + 1) * hist[i] for i in range(count))
+        assert torch.max(torch.abs(u - ref)).item() <= 1e-14 * 2 ** count
+    ptrs = (ctypes.c_void_p * 6)(*[h.data_ptr() for h in hist])
+    assert ctx._lib.topo_state_warm_start(ctx.ptr, ptrs, 6, ctypes.c_void_p(u.data_ptr()), stream) == _capi.TOPO_ERR_ARG
+    ptrs = (ctypes.c_void_p * 2)(hist[0].data_ptr(), None)
+    assert ctx._lib.topo_state_warm_start(ctx.ptr, ptrs, 2, ctypes.c_void_p(u.data_ptr()), stream) == _capi.TOPO_ERR_ARG

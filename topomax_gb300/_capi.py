@@ -29,7 +29,7 @@ EXPORTED = [
     "topo_create", "topo_create_filter", "topo_destroy", "topo_last_error", "topo_sizes",
     "topo_set_penalization", "topo_set_iteration_limit", "topo_set_filter_warm_start", "topo_filter_apply", "topo_filter_solve", "topo_state_solve",
     "topo_compliance", "topo_sensitivity_rhs", "topo_sensitivity", "topo_emd_step",
-    "topo_emd_finish", "topo_integrate", "topo_apply_state", "topo_load_vector", "topo_time_operator",
+    "topo_emd_finish", "topo_integrate", "topo_state_warm_start", "topo_apply_state", "topo_load_vector", "topo_time_operator",
     "topo_launch_count", "topo_kernel_clock", "topo_kernel_clock_report", "topo_march_tiles_report", "topo_sensitivity_rhs_noalloc", "topo_mass_apply",
     "topo_dem_create", "topo_dem_destroy", "topo_dem_last_error", "topo_dem_set_penalization",
     "topo_dem_set_external", "topo_dem_set_mask", "topo_dem_enforce", "topo_dem_energy",
@@ -119,6 +119,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.topo_emd_step.argtypes = [P, P, P, D, D, P, PD, P]
     lib.topo_emd_finish.argtypes = [P, P, P, P, PD, P]
     lib.topo_integrate.argtypes = [P, P, P, P]
+    lib.topo_state_warm_start.argtypes = [P, ctypes.POINTER(P), I, P, P]
     lib.topo_apply_state.argtypes = [P, P, P, P, P]
     lib.topo_load_vector.argtypes = [P, P, P]
     lib.topo_mass_apply.argtypes = [P, P, P, P]

@@ -1194,6 +1194,29 @@ int topo_integrate(topo_ctx* ctx, const double* f, double* out, topo_stream_t st
   });
 }
 
+int topo_state_warm_start(topo_ctx* ctx, const double* const* history, int count, double* u,
+                          topo_stream_t stream) {
+  return guarded(ctx, [&]() {
+    if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");
+    if (!history || !u || count < 1 || count > kMaxExtrapolate + 1)
+      return ctx->fail(TOPO_ERR_ARG, "invalid solution history");
+    Extrapolation ex{};
+    ex.n = count;
+    double binom = 1.0;  // binom(count, i + 1), built up term by term (exact: small integers)
+    for (int i = 0; i < count; ++i) {
+      if (!history[i]) return ctx->fail(TOPO_ERR_ARG, "invalid solution history");
+      binom = binom * double(count - i) / double(i + 1);
+      ex.x[i] = history[i];
+      ex.c[i] = (i % 2 ? -1.0 : 1.0) * binom;
+    }
+    const size_t n = 2 * ctx->nn2;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    k_extrapolate<<<ctx->grid(n), kVecThreads, 0, s>>>(u, ex, n);
+    ctx->launches += 1;
+    return ctx->cuda_check("state warm start");
+  });
+}
+
 int topo_apply_state(topo_ctx* ctx, const double* xi, const double* u, double* y, topo_stream_t stream) {
   return guarded(ctx, [&]() {
     if (!ctx->has_state) return ctx->fail(TOPO_ERR_STATE, "filter-only context");

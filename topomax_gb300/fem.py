@@ -25,7 +25,6 @@ reads them; "lattice" is the device order.
 from __future__ import annotations
 
 import ctypes
-import math
 import os
 import pickle
 
@@ -484,15 +483,16 @@ class ElasticityProblem(Problem):
         u = Function(self.solution_space)
         flags = 0
         if self.warm_start and self.u is not None:
-            u.tensor.copy_(self.u.tensor)
             order = min(self.extrapolate_order, len(self._u_hist) - 1) if self.extrapolate else 0
             if order > 0:
                 # the design moves a little each iteration: the solve starts from the polynomial
-                # extrapolation of the last order + 1 solutions,
+                # extrapolation of the last order + 1 solutions, in one pass on the device,
                 #   sum_i (-1)^i binom(order + 1, i + 1) u_(k-i)   (2 u_k - u_(k-1) for order 1)
-                u.tensor.mul_(float(math.comb(order + 1, 1)))
-                for i in range(1, order + 1):
-                    u.tensor.add_(self._u_hist[i].tensor, alpha=float((-1) ** i * math.comb(order + 1, i + 1)))
+                hist = (ctypes.c_void_p * (order + 1))(*[h.tensor.data_ptr() for h in self._u_hist[:order + 1]])
+                self._ctx.check(self._ctx._lib.topo_state_warm_start(self._ctx.ptr, hist, order + 1, _ptr(u.tensor),
+                                                                     _stream()))
+            else:
+                u.tensor.copy_(self.u.tensor)
             flags = _capi.SOLVE_WARM
         it = ctypes.c_int(0)
         self._ctx.check(self._ctx._lib.topo_state_solve(self._ctx.ptr, _ptr(xi), _ptr(u.tensor), self.rtol, flags,
