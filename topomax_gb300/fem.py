@@ -480,9 +480,12 @@ class ElasticityProblem(Problem):
         """Displacement u solving the state equation for the (filtered) density rho."""
         self.penalizer.assert_has_penalization()
         xi = as_cg1_tensor(rho, self.control_space)
-        u = Function(self.solution_space)
         flags = 0
-        if self.warm_start and self.u is not None:
+        warm = self.warm_start and self.u is not None
+        # a warm start writes every entry of u before the solve reads it: no zero fill
+        u = Function(self.solution_space,
+                     torch.empty(self.solution_space.dim(), dtype=torch.float64, device=_device()) if warm else None)
+        if warm:
             order = min(self.extrapolate_order, len(self._u_hist) - 1) if self.extrapolate else 0
             if order > 0:
                 # the design moves a little each iteration: the solve starts from the polynomial
