@@ -33,6 +33,10 @@ state solve + compliance).
   march-kernel autotuner chose in this run.
 * ``fluid``: the Stokes-Brinkman diffuser's design loop on the GPU beside the fluid
   oracle on the host.
+* ``solver_iterations``: inner Krylov iterations of the headline problem over its
+  device-resident and end-to-end runs (warm-ups included), and per timed step of the
+  device-resident run (``per_timed_step``: the state solve's, and the two filter
+  solves' together).
 * ``roofline``: the dominant kernel (the FP32 matrix-free P2 operator),
   algorithmic bytes 2*V2u*4 + V1*4 per launch over its CUDA-event duration
   measured in this run, against the measured HBM copy bandwidth.
@@ -335,12 +339,15 @@ def main():
         prob._ctx._lib.topo_launch_count(prob._ctx.ptr, ctypes.byref(n))
         return n.value
 
-    def device_loop(prob, steps, warmup, time_operator=False, profile=False, space=None, start=None, on_start=None):
+    def device_loop(prob, steps, warmup, time_operator=False, profile=False, space=None, start=None, on_start=None,
+                    step_iterations=None):
         """Design-resident loop; returns per-step ms (CUDA events), objectives, launches, operator ms.
 
         With profile=True the timed steps are bracketed by cudaProfilerStart/Stop, so that a
         profiler run with --profile-from-start off records exactly those launches.  on_start()
-        runs once, after the warm-up steps."""
+        runs once, after the warm-up steps.  step_iterations (a dict of two lists), when
+        given, receives each timed step's inner Krylov iterations: its state solve's, and
+        its two filter solves' together (host counters the solves return anyway)."""
         lib = prob._ctx._lib
         rho = F.Function(space or V, (start if start is not None else rho0).cuda())
         psi = torch.log(rho.tensor / (1 - rho.tensor))
@@ -356,6 +363,7 @@ def main():
                 if profile:
                     torch.cuda.profiler.start()
             flush.zero_()
+            it0 = dict(prob.stats)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -374,6 +382,9 @@ def main():
             torch.cuda.synchronize()
             if k >= warmup:
                 times.append(e0.elapsed_time(e1))
+                if step_iterations is not None:
+                    step_iterations["state"].append(prob.stats["state_iterations"] - it0["state_iterations"])
+                    step_iterations["filter"].append(prob.stats["filter_iterations"] - it0["filter_iterations"])
         barrier()
         if profile:
             torch.cuda.profiler.stop()
@@ -418,13 +429,16 @@ def main():
     clocks = Clocks(f"r{rank}", args.clocks_dir)
     barrier()
     clocks.start(local if not os.environ.get("CUDA_VISIBLE_DEVICES") else 0)
-    times, objs, nlaunch, op_ms = device_loop(prob, args.steps, args.warmup, time_operator=True, profile=True)
+    per_step = {"state": [], "filter": []}
+    times, objs, nlaunch, op_ms = device_loop(prob, args.steps, args.warmup, time_operator=True, profile=True,
+                                              step_iterations=per_step)
     ck = clocks.stop()
     total_ms, value = job_throughput(float(np.sum(times)), args.steps, world, dist)
     ms = total_ms / args.steps
     e2e_times = e2e_loop(prob, args.e2e_steps, args.warmup)
     e2e_value = 1.0 / float(np.mean(e2e_times))
     stats = dict(prob.stats)
+    stats["per_timed_step"] = per_step
     del prob
     torch.cuda.empty_cache()
 
