@@ -45,7 +45,9 @@ state solve + compliance).
   on this host's cores over real design iterations of the same loop, on the
   --ref-grid cantilever (160x80 by default: SuperLU cannot factor the 1000x500
   state matrix on a 62 GB host).  ``same_grid``: the GPU loop on that grid, so
-  that a same-grid comparison exists beside the headline one.
+  that a same-grid comparison exists beside the headline one.  ``size_sweep``
+  (--size-sweep, off by default): the GPU loop and the oracle side by side on
+  several grids, design iterations/s each.
 """
 from __future__ import annotations
 
@@ -106,6 +108,9 @@ def parse():
     ap.add_argument("--ref-grid", default="160x80",
                     help="grid of the CPU oracle legs (cpu_baseline, --impl reference) and of the GPU same-grid leg")
     ap.add_argument("--cpu-steps", type=int, default=5, help="timed oracle design iterations of cpu_baseline")
+    ap.add_argument("--size-sweep", default="",
+                    help="comma-separated 2:1 grids (e.g. 80x40,160x80,320x160) timed on the GPU (mixed) and "
+                         "by the CPU oracle (--cpu-steps iterations each); empty skips the sweep")
     ap.add_argument("--clocks-dir", default=None,
                     help="keep the raw nvidia-smi samples of the timed region here (default: a temporary file)")
     args = ap.parse_args()
@@ -501,6 +506,24 @@ def main():
         del pr
     torch.cuda.empty_cache()
 
+    # --- the GPU loop and the CPU oracle side by side over a size sweep (off by default)
+    sweep = None
+    if args.size_sweep and world == 1:
+        sweep = []
+        for text in args.size_sweep.split(","):
+            snx, sny = _grid(text)
+            mesh_s = tg.RectangleMesh(2.0, 1.0, snx, sny)
+            V_s = tg.FunctionSpace(mesh_s, "CG", 1, dof_order="lattice")
+            ps = tg.ElasticityProblem(mesh_s, V_s, dom, par, precision="mixed", rtol=args.rtol)
+            ps.set_penalization(PENALTY)
+            ts, _, _, _ = device_loop(ps, args.steps, args.warmup, space=V_s, start=seeded_density(snx, sny))
+            del ps
+            torch.cuda.empty_cache()
+            oval, osec = time_oracle(snx, sny, args.cpu_steps, 1)
+            gval = 1000.0 / float(np.mean(ts))
+            sweep.append({"grid": f"{snx}x{sny}", "dofs": dofs(snx, sny), "gpu_mixed": gval, "gpu_steps": len(ts),
+                          "oracle": oval, "oracle_steps": args.cpu_steps, "gpu_over_oracle": gval / oval})
+
     # --- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
     alg_bytes = 2 * dofs(args.nx, args.ny) * 4 + nv * 4
@@ -541,6 +564,7 @@ def main():
                      "executed_fp32_tinst_per_s": fp32_inst / (op * 1e-3) / 1e12 if fp32_inst else None},
         "cpu_baseline": cpu,
         "same_grid": same_grid,
+        "size_sweep": sweep,
         "gpu_launches": int(nlaunch),
         "kernels": kernels,
         "c2_2000x1000": c2,
