@@ -65,7 +65,7 @@ def test_noalloc_matches_context_entry_point():
         torch.cuda.synchronize()
         outs.append(b.clone())
         free.append(torch.cuda.mem_get_info()[0])
-    # the driver materialises the fixed scratch array when the library's device code
+    # the CUDA runtime materialises the fixed scratch array when the library's device code
     # is first loaded; after that, calls take no device memory
     assert free[1] == free[0]
     scale = ref.abs().max().item()
